@@ -1,0 +1,259 @@
+/*
+ * tsvd.h — C-ABI of the GB300-native Tree-SVD per-snapshot refresh.
+ *
+ * One process, one GPU (sm_103a). Every device buffer is owned by the
+ * session (or allocated inside a call and freed before it returns); callers
+ * pass plain host pointers and sizes, except for the *_device entry points,
+ * which take device pointers that stay owned by the caller.
+ *
+ * Reference interfaces replaced (paths relative to the reference project):
+ *   frPCA(mat_csr*, mat**, mat**, mat**, int k, int q) ............ Code/frpca.c:239,
+ *                                                                    Code/matrix_vector_functions_intel_mkl_ext.h:75
+ *   mat / mat_csr layouts ........................................ Code/matrix_vector_functions_intel_mkl.h:20-23,
+ *                                                                    Code/matrix_vector_functions_intel_mkl_ext.h:22-33
+ *   UGraph::inputDynamicGraph / Graph::inputDirectedDynamicGraph .. Code/Graph_dynamic.h:530-605 / :119-238
+ *   nodegree_Dense{Undirected,Directed}_Refresh_PPR_initialization  Code/ppr_computation_store_dynamic.h:2035-2121,
+ *     (+ _Transpose)                                                 :3811-3898, :4133-4228
+ *   nodegree_DenseDynamicForwardPush / ...Directed...(Transpose) .. Code/ppr_computation_store_dynamic.h:1394-1498,
+ *                                                                    :2945-3030, :3356-3437
+ *   Log_sparse_matrix_entries[_with_norm_computation][_LP] ......... Code/ppr_computation_store_dynamic.h:2527-2561,
+ *                                                                    :2598-2638, :2649-2732, :2742-2826
+ *   sparse_sub_svd_function_with_norm_computation ................ Code/Tree_u_NC.cpp:75-226
+ *   tree merge (dense_sub_svd_function, root U*sqrt(S)) ........... Code/Tree_u_NC.cpp:723-850, :238-262
+ *   Tree_{u,d}_{NC,LP} main snapshot loop + CSV output ............ Code/Tree_u_NC.cpp:296-911, Code/Tree_d_NC.cpp:400-1171
+ *
+ * Conventions: every call returns tsvd_status; a failing call leaves a
+ * message readable through tsvd_last_error() (thread-local). A session is
+ * not thread-safe: one caller at a time.
+ */
+#ifndef TSVD_H
+#define TSVD_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum tsvd_status {
+  TSVD_OK = 0,
+  TSVD_ERR_INVALID = 1,   /* bad argument or size */
+  TSVD_ERR_OOM = 2,       /* device or pinned-host allocation failed */
+  TSVD_ERR_DEVICE = 3,    /* CUDA runtime error (message in tsvd_last_error) */
+  TSVD_ERR_TIMEOUT = 4,   /* a bounded device loop gave up (status flag set by a kernel) */
+  TSVD_ERR_STATE = 5,     /* call out of order (e.g. embedding before the first step) */
+  TSVD_ERR_IO = 6,        /* file could not be read or written */
+  TSVD_ERR_NUMERIC = 7    /* non-finite value detected in a factor */
+} tsvd_status;
+
+const char *tsvd_status_string(tsvd_status s);
+const char *tsvd_last_error(void);
+/* Build identification string ("tsvd-gb300 sm_103a ..."). */
+const char *tsvd_version(void);
+
+/* ------------------------------------------------------------------------- */
+/* Legacy drop-in types and frPCA (same memory layout as the reference).      */
+/* ------------------------------------------------------------------------- */
+#ifndef TSVD_NO_LEGACY
+/* Column-major dense matrix. Code/matrix_vector_functions_intel_mkl.h:20-23 */
+typedef struct {
+  int nrows, ncols;
+  double *d;
+} mat;
+
+/* 1-based CSR with begin/end row pointers.
+ * Code/matrix_vector_functions_intel_mkl_ext.h:22-33 */
+typedef struct {
+  int nnz;
+  int nrows, ncols;
+  double *values;
+  int *cols;
+  int *pointerB, *pointerE;
+} mat_csr;
+
+/* Drop-in for frPCA (Code/frpca.c:239-326): randomized SVD of A with
+ * oversampling 5 and q passes over A. *U (nrows x k), *S (k x 1) and
+ * *V (ncols x k) are preallocated by the caller as in
+ * Code/Tree_u_NC.cpp:139-142 and are overwritten. Singular values come
+ * back in ascending order, like the reference (dsyevd order, frpca.c:298-310).
+ * The Gaussian test matrix comes from the counter-based generator seeded by
+ * tsvd_set_frpca_seed() (the reference seeds MKL VSL with time(NULL)).
+ * Errors are reported through tsvd_last_error(); the legacy signature has no
+ * return value, and on error the outputs are left zero-filled. */
+void frPCA(mat_csr *A, mat **U, mat **S, mat **V, int k, int q);
+#endif
+
+void tsvd_set_frpca_seed(uint64_t seed);
+
+/* Status-returning frPCA over a host CSR (0- or 1-based, int64 row_ptr of
+ * nrows+1 entries). U: nrows x k, V: ncols x k (both column-major, like
+ * `mat`), S: k values in DESCENDING order. Any of U, S, V may be NULL.
+ * Replaces Code/frpca.c:239 for callers that want status codes and a seed. */
+tsvd_status tsvd_frpca(int32_t nrows, int32_t ncols, int64_t nnz,
+                       const int64_t *row_ptr, const int32_t *col_idx,
+                       const double *values, int32_t index_base, int32_t k,
+                       int32_t q, uint64_t seed, double *U, double *S,
+                       double *V);
+
+/* ------------------------------------------------------------------------- */
+/* Session: device graph store + PPR store + block factors + merge tree.      */
+/* ------------------------------------------------------------------------- */
+typedef struct tsvd_session tsvd_session;
+
+enum {
+  /* Log transform of the proximity x (Code/ppr_computation_store_dynamic.h): */
+  TSVD_TRANSFORM_LOG10_NC = 0, /* x > rmin ? log10(x/rmin) : 0      (:2549-2556) */
+  TSVD_TRANSFORM_LOG10_LP = 1, /* log10(1 + x/rmin) on stored x     (:2621-2632) */
+  TSVD_TRANSFORM_LN_N = 2      /* max(0, ln(x * N))                                */
+};
+
+enum {
+  /* Block-recompute rule once iter >= lazy_update_start_iter. */
+  TSVD_DIRTY_REFERENCE = 0, /* resid + ||A-A_old||_F >= sqrt(2)*delta*||A||_F   (:2707-2711) */
+  TSVD_DIRTY_FROBENIUS = 1, /* ||A-A_old||_F > dirty_frac * ||A||_F                           */
+  TSVD_DIRTY_ALL = 2        /* every block, every snapshot                                  */
+};
+
+enum {
+  TSVD_ROOT_SQRT_SIGMA = 0, /* U * sqrt(|S|)  (Tree_u_NC.cpp:765-772)  */
+  TSVD_ROOT_U = 1           /* U              (Tree_u_LP.cpp root)    */
+};
+
+enum {
+  /* Refresh arithmetic for a new adjacency slot j of vertex u. */
+  TSVD_REFRESH_EXACT = 0, /* p *= (j+1)/j in double (ppr:6520-6522, the sparse path)        */
+  TSVD_REFRESH_INTDIV = 1 /* p *= (j+1)/j in int   (ppr:2102, 3875, 4203, the dense path)  */
+};
+
+typedef struct tsvd_config {
+  int32_t n_vertices;       /* N (argv[9] of the reference drivers)                  */
+  int32_t directed;         /* 0: UGraph (Tree_u_*), 1: Graph + transpose (Tree_d_*)  */
+  int32_t n_sources;        /* |S|                                                   */
+  const int32_t *sources;   /* |S| vertex ids, row order of the embedding            */
+  double alpha;             /* argv[3]                                               */
+  double rmax;              /* argv[5]: residuemax == reservemin                     */
+  int32_t n_parts;          /* argv[7]: column blocks                                */
+  int32_t hierarchy_n;      /* argv[8]: merge arity h (n_parts must be a power of h) */
+  int32_t rank_d;           /* d (128 in the reference, Tree_u_NC.cpp:357)           */
+  int32_t oversample;       /* s (5 in the reference, frpca.c:242)                   */
+  int32_t passes_q;         /* argv[4]: q                                            */
+  int32_t dynamic_ppr_start_iter; /* argv[10]                                        */
+  int32_t lazy_update_start_iter; /* argv[11]                                        */
+  double delta;             /* argv[12]                                              */
+  int32_t transform;        /* TSVD_TRANSFORM_*                                      */
+  int32_t dirty_rule;       /* TSVD_DIRTY_*                                          */
+  double dirty_frac;        /* for TSVD_DIRTY_FROBENIUS                              */
+  int32_t root_scaling;     /* TSVD_ROOT_*                                           */
+  int32_t refresh_mode;     /* TSVD_REFRESH_*                                        */
+  uint64_t seed;            /* Gaussian test matrices                                */
+  int32_t device;           /* CUDA device ordinal                                   */
+  int32_t max_push_rounds;  /* bound on frontier rounds per push (0 = default)       */
+} tsvd_config;
+
+/* Fills the reference's defaults (Tree_u_NC, run.sh: alpha .5, q 12, ...). */
+void tsvd_config_default(tsvd_config *cfg);
+
+tsvd_status tsvd_session_create(const tsvd_config *cfg, tsvd_session **out);
+tsvd_status tsvd_session_destroy(tsvd_session *s);
+
+/* One snapshot (one iteration of the driver loop, Tree_u_NC.cpp:507-866):
+ * insert the edges (a delta file's worth), refresh + push PPR, log-transform
+ * and test every block, factorize dirty blocks, merge dirty ancestors.
+ * `edges` holds m (from, to) pairs of int32, host memory. */
+tsvd_status tsvd_session_step(tsvd_session *s, const int32_t *edges, int64_t m);
+/* Same, with the pairs already in device memory (owned by the caller). */
+tsvd_status tsvd_session_step_device(tsvd_session *s, const int32_t *edges_dev,
+                                     int64_t m);
+/* Current embedding, |S| x d, row-major doubles (row i = sources[i]). */
+tsvd_status tsvd_session_embedding(tsvd_session *s, double *out);
+/* Device pointer to the current embedding (|S| x d row-major float), valid
+ * until the next step. */
+tsvd_status tsvd_session_embedding_device(tsvd_session *s, const float **out);
+
+typedef struct tsvd_step_stats {
+  int32_t iter;
+  int32_t skipped;          /* 1 when the driver's lazy skip rule fired          */
+  int64_t edges_inserted;
+  int64_t push_rounds;      /* frontier rounds (both directions)                */
+  int64_t pushes;           /* (vertex, source) pushes executed                 */
+  int64_t push_edge_updates;/* sum of deg(v) over pushes                        */
+  int32_t dirty_blocks;
+  int32_t factorized_blocks;
+  int32_t merged_nodes;
+  double ms_insert, ms_refresh, ms_push, ms_log, ms_frpca, ms_merge, ms_total;
+} tsvd_step_stats;
+tsvd_status tsvd_session_last_stats(tsvd_session *s, tsvd_step_stats *out);
+
+/* ---- granular PPR-store interface (the reference's thread entry points) --- */
+/* a1: append edges to the device adjacency (both directions for undirected,
+ * out- and in-lists for directed); records former degrees. */
+tsvd_status tsvd_graph_insert(tsvd_session *s, const int32_t *edges, int64_t m);
+/* a3: refresh for snapshot `iter` (from scratch when iter <
+ * dynamic_ppr_start_iter, else the residual perturbation of the new slots).
+ * `transpose` selects the in-edge (reverse) PPR of a directed graph. */
+tsvd_status tsvd_ppr_refresh(tsvd_session *s, int32_t iter, int32_t transpose);
+/* a4: frontier push until every eligible residual is <= rmax. */
+tsvd_status tsvd_ppr_push(tsvd_session *s, int32_t transpose);
+/* a5/a6: log transform, norms and dirty test for every block; dirty[b] = 1
+ * for blocks to refactorize (host array of n_parts bytes, may be NULL). */
+tsvd_status tsvd_blocks_materialize(tsvd_session *s, int32_t iter,
+                                    uint8_t *dirty);
+/* a7/a8: frPCA of the dirty blocks, leaf factors B = U*diag(S), residuals. */
+tsvd_status tsvd_blocks_factorize(tsvd_session *s, int32_t iter);
+/* a9: merge the ancestors of refactorized leaves; writes the embedding. */
+tsvd_status tsvd_tree_merge(tsvd_session *s);
+
+/* ---- inspection (host copies; for tests and tools) ---- */
+/* Degrees (n_vertices int32 each; former = before the last insert). dir: 0 out/undirected, 1 in. */
+tsvd_status tsvd_graph_degrees(tsvd_session *s, int32_t dir, int32_t *deg,
+                               int32_t *former_deg);
+/* Adjacency in insertion order: offsets (N+1, int64) and neighbours. */
+tsvd_status tsvd_graph_adjacency(tsvd_session *s, int32_t dir, int64_t *offsets,
+                                 int32_t *nbrs, int64_t nbrs_capacity);
+/* PPR state as |S| x N row-major float: which = 0 residue, 1 reserve. */
+tsvd_status tsvd_ppr_state(tsvd_session *s, int32_t transpose, int32_t which,
+                           float *out);
+/* Per-block numbers: ||A||_F, ||A-A_old||_F, residual, nnz(A), dirty flag. */
+tsvd_status tsvd_block_info(tsvd_session *s, double *norm_a, double *norm_diff,
+                            double *resid, int64_t *nnz, uint8_t *dirty);
+/* Tree node factor (|S| x d row-major doubles) and its singular values (d). */
+tsvd_status tsvd_tree_factor(tsvd_session *s, int32_t node, double *out,
+                             double *sigma);
+/* Dense log-transformed block b as |S| x n_b row-major float (tests). */
+tsvd_status tsvd_block_dense(tsvd_session *s, int32_t b, float *out);
+
+/* ------------------------------------------------------------------------- */
+/* Synthetic inputs (seeded; stand in for the reference's datasets).           */
+/* ------------------------------------------------------------------------- */
+/* R-MAT edges (a,b,c,d) with self-loops and duplicates dropped (undirected
+ * duplicates are unordered pairs), vertex ids permuted by a seeded random
+ * permutation, then shuffled into uniform-random timestamp order.
+ * edges_out: 2*m int32. */
+tsvd_status tsvd_rmat_edges(int32_t n, int64_t m, double a, double b, double c,
+                            int32_t directed, uint64_t seed,
+                            int32_t *edges_out);
+/* Snapshot sizes: first gets round(first_frac*m), the rest split evenly. */
+tsvd_status tsvd_snapshot_sizes(int64_t m, int32_t n_snapshots,
+                                double first_frac, int64_t *sizes_out);
+/* |S| distinct vertices drawn uniformly from those touched by `edges`
+ * (the reference samples among first-snapshot nodes,
+ * Random_Sample_Points_NC.cpp), returned sorted ascending. */
+tsvd_status tsvd_sample_sources(int32_t n, const int32_t *edges, int64_t m,
+                                int32_t k, uint64_t seed, int32_t *out);
+/* Parse a "u v" per line edge file. compat_dup_last = 1 reproduces the
+ * reference reader's repeat of the last pair when the file ends in
+ * whitespace (Graph_dynamic.h:127-130, 539-542). *edges is malloc'ed; free
+ * with tsvd_free. */
+tsvd_status tsvd_read_edge_file(const char *path, int32_t compat_dup_last,
+                                int32_t **edges, int64_t *m);
+void tsvd_free(void *p);
+
+/* Gaussian test-matrix entry used by frPCA (Philox4x32-10 + Box-Muller in
+ * float, rounded to half precision); identical on host and device. */
+float tsvd_gaussian(uint64_t seed, uint32_t stream, uint32_t row, uint32_t col);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TSVD_H */

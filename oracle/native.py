@@ -1,0 +1,231 @@
+"""ctypes bindings for the CPU oracle (oracle/liboracle_ppr.so) and for the
+reference-compiled pin library (oracle/_ref/libtsvd_ref.so).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and
+bench.py's CPU-baseline leg as the checker, never by the product path.
+"""
+import ctypes
+import os
+import subprocess
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+_ORACLE_SO = os.path.join(HERE, "liboracle_ppr.so")
+_REF_SO = os.path.join(HERE, "_ref", "libtsvd_ref.so")
+
+_i32p = ctypes.POINTER(ctypes.c_int32)
+_i64p = ctypes.POINTER(ctypes.c_int64)
+_f32p = ctypes.POINTER(ctypes.c_float)
+_f64p = ctypes.POINTER(ctypes.c_double)
+
+
+def build():
+    subprocess.check_call(["sh", os.path.join(HERE, "build_oracle.sh")])
+
+
+def build_ref():
+    subprocess.check_call(["sh", os.path.join(HERE, "build_ref.sh")])
+
+
+def _ptr(a, t):
+    return a.ctypes.data_as(t)
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(_ORACLE_SO):
+            build()
+        L = ctypes.CDLL(_ORACLE_SO)
+        L.or_graph_new.restype = ctypes.c_void_p
+        L.or_graph_new.argtypes = [ctypes.c_int32, ctypes.c_int32]
+        L.or_graph_free.argtypes = [ctypes.c_void_p]
+        L.or_graph_insert.restype = ctypes.c_int
+        L.or_graph_insert.argtypes = [ctypes.c_void_p, _i32p, ctypes.c_int64]
+        L.or_graph_degrees.restype = ctypes.c_int
+        L.or_graph_degrees.argtypes = [ctypes.c_void_p, ctypes.c_int32, _i32p, _i32p]
+        L.or_graph_adjacency.restype = ctypes.c_int64
+        L.or_graph_adjacency.argtypes = [ctypes.c_void_p, ctypes.c_int32, _i64p, _i32p]
+        L.or_ppr_new.restype = ctypes.c_void_p
+        L.or_ppr_new.argtypes = [ctypes.c_int32, ctypes.c_int32, _i32p]
+        L.or_ppr_free.argtypes = [ctypes.c_void_p]
+        L.or_ppr_residue.restype = _f32p
+        L.or_ppr_residue.argtypes = [ctypes.c_void_p]
+        L.or_ppr_reserve.restype = _f32p
+        L.or_ppr_reserve.argtypes = [ctypes.c_void_p]
+        L.or_ppr_pushes.restype = ctypes.c_int64
+        L.or_ppr_pushes.argtypes = [ctypes.c_void_p]
+        L.or_ppr_edge_updates.restype = ctypes.c_int64
+        L.or_ppr_edge_updates.argtypes = [ctypes.c_void_p]
+        L.or_ppr_refresh.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32,
+                                     ctypes.c_int32, ctypes.c_int32, ctypes.c_double,
+                                     ctypes.c_double, ctypes.c_int32, ctypes.c_int32]
+        L.or_ppr_push.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32,
+                                  ctypes.c_double, ctypes.c_double, ctypes.c_int32]
+        _lib = L
+    return _lib
+
+
+class OracleGraph:
+    """Reference graph store semantics (Graph_dynamic.h): insertion-ordered lists."""
+
+    def __init__(self, n, directed):
+        self.n, self.directed = int(n), int(directed)
+        self.h = lib().or_graph_new(self.n, self.directed)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().or_graph_free(self.h)
+            self.h = None
+
+    def insert(self, edges):
+        e = np.ascontiguousarray(edges, dtype=np.int32).reshape(-1, 2)
+        rc = lib().or_graph_insert(self.h, _ptr(e, _i32p), e.shape[0])
+        if rc != 0:
+            raise ValueError("oracle graph insert failed (%d)" % rc)
+
+    def degrees(self, dir=0):
+        d = np.zeros(self.n, np.int32)
+        f = np.zeros(self.n, np.int32)
+        lib().or_graph_degrees(self.h, dir, _ptr(d, _i32p), _ptr(f, _i32p))
+        return d, f
+
+    def adjacency(self, dir=0):
+        tot = lib().or_graph_adjacency(self.h, dir, None, None)
+        off = np.zeros(self.n + 1, np.int64)
+        nb = np.zeros(max(tot, 1), np.int32)
+        lib().or_graph_adjacency(self.h, dir, _ptr(off, _i64p), _ptr(nb, _i32p))
+        return off, nb[:tot]
+
+
+class OraclePPR:
+    """Per-source FIFO push state (float residue/reserve, |S| x N)."""
+
+    def __init__(self, n, sources):
+        self.n = int(n)
+        self.sources = np.ascontiguousarray(sources, dtype=np.int32)
+        self.s = len(self.sources)
+        self.h = lib().or_ppr_new(self.n, self.s, _ptr(self.sources, _i32p))
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().or_ppr_free(self.h)
+            self.h = None
+
+    def refresh(self, g, dir, iter, dyn_start, alpha, rmax, intdiv=False, threads=1):
+        lib().or_ppr_refresh(self.h, g.h, dir, iter, dyn_start, alpha, rmax, int(intdiv), threads)
+
+    def push(self, g, dir, alpha, rmax, threads=1):
+        lib().or_ppr_push(self.h, g.h, dir, alpha, rmax, threads)
+        return lib().or_ppr_pushes(self.h), lib().or_ppr_edge_updates(self.h)
+
+    def residue(self):
+        p = lib().or_ppr_residue(self.h)
+        return np.ctypeslib.as_array(p, shape=(self.s, self.n)).copy()
+
+    def reserve(self):
+        p = lib().or_ppr_reserve(self.h)
+        return np.ctypeslib.as_array(p, shape=(self.s, self.n)).copy()
+
+
+# ---------------------------------------------------------------- reference pin
+_ref = None
+
+
+def ref_available():
+    return os.path.exists(_REF_SO)
+
+
+def ref_lib():
+    global _ref
+    if _ref is None:
+        L = ctypes.CDLL(_REF_SO)
+        L.ref_graph_new.restype = ctypes.c_void_p
+        L.ref_graph_new.argtypes = [ctypes.c_int, ctypes.c_int]
+        L.ref_graph_insert_file.restype = ctypes.c_longlong
+        L.ref_graph_insert_file.argtypes = [ctypes.c_void_p, ctypes.c_char_p]
+        L.ref_graph_degrees.argtypes = [ctypes.c_void_p, ctypes.c_int, _i32p, _i32p]
+        L.ref_graph_adjacency.restype = ctypes.c_longlong
+        L.ref_graph_adjacency.argtypes = [ctypes.c_void_p, ctypes.c_int, _i64p, _i32p]
+        L.ref_ppr_new.restype = ctypes.c_void_p
+        L.ref_ppr_new.argtypes = [ctypes.c_int, ctypes.c_int, _i32p, ctypes.c_int,
+                                  ctypes.c_double, ctypes.c_double]
+        L.ref_ppr_free.argtypes = [ctypes.c_void_p]
+        L.ref_ppr_step.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                   ctypes.c_int, ctypes.c_int]
+        L.ref_ppr_state.argtypes = [ctypes.c_void_p, ctypes.c_int, _f32p]
+        L.ref_ppr_dense.argtypes = [ctypes.c_void_p, _f64p]
+        _ref = L
+    return _ref
+
+
+def write_edge_file(path, edges, trailing_newline=True):
+    e = np.asarray(edges, dtype=np.int64).reshape(-1, 2)
+    body = "\n".join("%d %d" % (a, b) for a, b in e)
+    with open(path, "w") as f:
+        f.write(body + ("\n" if trailing_newline and len(e) else ""))
+
+
+class RefGraph:
+    """The reference's UGraph/Graph, fed through its own file reader."""
+
+    def __init__(self, n, directed):
+        self.n, self.directed = int(n), int(directed)
+        self.h = ref_lib().ref_graph_new(self.n, self.directed)
+
+    def insert_file(self, path):
+        return ref_lib().ref_graph_insert_file(self.h, path.encode())
+
+    def insert(self, edges, trailing_newline=True):
+        with tempfile.NamedTemporaryFile("w", suffix=".txt", delete=False) as f:
+            name = f.name
+        try:
+            write_edge_file(name, edges, trailing_newline)
+            return self.insert_file(name)
+        finally:
+            os.unlink(name)
+
+    def degrees(self, dir=0):
+        d = np.zeros(self.n, np.int32)
+        f = np.zeros(self.n, np.int32)
+        ref_lib().ref_graph_degrees(self.h, dir, _ptr(d, _i32p), _ptr(f, _i32p))
+        return d, f
+
+    def adjacency(self, dir=0):
+        tot = ref_lib().ref_graph_adjacency(self.h, dir, None, None)
+        off = np.zeros(self.n + 1, np.int64)
+        nb = np.zeros(max(tot, 1), np.int32)
+        ref_lib().ref_graph_adjacency(self.h, dir, _ptr(off, _i64p), _ptr(nb, _i32p))
+        return off, nb[:tot]
+
+
+class RefPPR:
+    def __init__(self, n, sources, nparts, alpha, rmax):
+        self.n = int(n)
+        self.sources = np.ascontiguousarray(sources, dtype=np.int32)
+        self.s = len(self.sources)
+        self.h = ref_lib().ref_ppr_new(self.n, self.s, _ptr(self.sources, _i32p),
+                                       nparts, alpha, rmax)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            ref_lib().ref_ppr_free(self.h)
+            self.h = None
+
+    def step(self, g, transpose, iter, dyn_start):
+        ref_lib().ref_ppr_step(self.h, g.h, int(transpose), iter, dyn_start)
+
+    def state(self, which):
+        out = np.zeros((self.s, self.n), np.float32)
+        ref_lib().ref_ppr_state(self.h, which, _ptr(out, _f32p))
+        return out
+
+    def dense(self):
+        out = np.zeros((self.s, self.n), np.float64)
+        ref_lib().ref_ppr_dense(self.h, _ptr(out, _f64p))
+        return out
