@@ -51,6 +51,8 @@ const char *tsvd_status_string(tsvd_status s);
 const char *tsvd_last_error(void);
 /* Build identification string ("tsvd-gb300 sm_103a ..."). */
 const char *tsvd_version(void);
+/* Number of kernels this library has launched in the process so far. */
+int64_t tsvd_launch_count(void);
 
 /* ------------------------------------------------------------------------- */
 /* Legacy drop-in types and frPCA (same memory layout as the reference).      */
@@ -170,6 +172,10 @@ tsvd_status tsvd_session_embedding(tsvd_session *s, double *out);
 /* Device pointer to the current embedding (|S| x d row-major float), valid
  * until the next step. */
 tsvd_status tsvd_session_embedding_device(tsvd_session *s, const float **out);
+
+/* The session's CUDA stream (cudaStream_t), for callers that order their own
+ * work or timing events against the session's kernels. */
+tsvd_status tsvd_session_stream(tsvd_session *s, void **stream);
 
 typedef struct tsvd_step_stats {
   int32_t iter;

@@ -24,6 +24,17 @@
 #include <stdlib.h>
 #include <string.h>
 
+/* The Gaussian test matrix is specified once (Philox4x32-10 + Box-Muller
+ * with bit-reproducible float arithmetic) and shared with the device. */
+#include "../tree-embedding_gb300/csrc/philox_gauss.h"
+
+void or_gaussian_matrix(uint64_t seed, uint32_t stream, int64_t nrows, int32_t ncols,
+                        double *out /* row-major nrows x ncols */) {
+  for (int64_t i = 0; i < nrows; ++i)
+    for (int32_t j = 0; j < ncols; ++j)
+      out[i * ncols + j] = tsvd_gauss_entry(seed, stream, (uint32_t)i, (uint32_t)j);
+}
+
 /* ------------------------------------------------------------------ graph */
 typedef struct {
   int32_t *v;
@@ -219,9 +230,16 @@ static void *refresh_job(void *arg) {
     for (int32_t j = former[i]; j < deg[i]; ++j) {
       int32_t to = adj[i].v[j];
       for (int32_t k = J->k0; k < J->k1; ++k) {
-        if (j == 0) continue; /* first slot of a formerly dangling vertex */
         float *r = st->r + (size_t)k * n, *p = st->p + (size_t)k * n;
         uint8_t *fl = st->flag + (size_t)k * n;
+        if (j == 0) {
+          /* First slot of a formerly dangling vertex: p(i) = 0, nothing to
+           * rescale. The reference skips it (ppr:2086-2093), which leaves the
+           * residue the vertex collected while dangling unpushed although it
+           * can now push; the exact mode queues it like any other residue. */
+          if (!J->intdiv && r[i] > rmax && !fl[i]) { q_push(st, k, i); fl[i] = 1; }
+          continue;
+        }
         if (J->intdiv) {
           p[i] *= (j + 1) / j;
           r[i] -= p[i] / (j + 1) / alpha;

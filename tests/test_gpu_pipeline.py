@@ -1,0 +1,201 @@
+"""GPU parity tests: every stage of the per-snapshot refresh, through the C-ABI,
+against the CPU oracle on the same seeded inputs."""
+import numpy as np
+import pytest
+
+import tsvd_gb300 as T
+import workloads as W
+from oracle import native
+from oracle.tree_oracle import OracleTreeSVD, frpca as oracle_frpca, gaussian_matrix, log_transform
+
+from helpers import (gap_index, gram_rel_err, max_principal_sine, push_identity_residual,
+                     reach_weight, transition)
+
+pytestmark = pytest.mark.gpu
+
+
+def small_cfg(directed=False, n=6000, m=40000, sources=64, n_parts=4, rank_d=32, snapshots=4):
+    base = "rmat-d-2.7m" if directed else "rmat-u-100k"
+    c = W.scaled(base, n=n, m=m, sources=sources, n_parts=n_parts, rank_d=rank_d,
+                 snapshots=snapshots)
+    c["rmax"] = 1e-5
+    return c
+
+
+@pytest.mark.parametrize("directed", [False, True])
+def test_graph_insert_bit_exact(directed):
+    cfg = small_cfg(directed)
+    _, snaps, src = W.build(cfg, seed=11)
+    g = native.OracleGraph(cfg["n"], directed)
+    with T.Session(cfg["n"], src, **W.session_kwargs(cfg)) as s:
+        for k, e in enumerate(snaps):
+            if k == 2:  # a batch with repeated pairs and a self loop: stored as given
+                e = np.concatenate([e, e[:5], [[7, 7]]]).astype(np.int32)
+            s.graph_insert(e)
+            g.insert(e)
+            for d in range(2 if directed else 1):
+                off_g, nb_g = s.adjacency(d)
+                off_o, nb_o = g.adjacency(d)
+                assert np.array_equal(off_g, off_o)
+                assert np.array_equal(nb_g, nb_o)
+                deg_g, fo_g = s.degrees(d)
+                deg_o, fo_o = g.degrees(d)
+                assert np.array_equal(deg_g, deg_o) and np.array_equal(fo_g, fo_o)
+
+
+def test_graph_insert_empty_and_invalid():
+    cfg = small_cfg()
+    _, snaps, src = W.build(cfg, seed=3)
+    with T.Session(cfg["n"], src, **W.session_kwargs(cfg)) as s:
+        s.graph_insert(snaps[0])
+        before = s.adjacency(0)
+        s.graph_insert(np.zeros((0, 2), np.int32))
+        with pytest.raises(T.TsvdError) as ei:
+            s.graph_insert(np.array([[0, cfg["n"]]], np.int32))
+        assert ei.value.status == 1
+        after = s.adjacency(0)
+        assert np.array_equal(before[1], after[1])
+
+
+def _ppr_checks(s, g, src, cfg, transpose, oracle_p=None):
+    d = 1 if transpose else 0
+    off, nb = g.adjacency(d)
+    P, deg = transition(cfg["n"], off, nb)
+    p = s.ppr_state(transpose, 1)
+    r = s.ppr_state(transpose, 0)
+    alpha, rmax = cfg["alpha"], cfg["rmax"]
+    # exact forward-push identity p (I - (1-a) P) = a (e_s - r), any push order
+    assert push_identity_residual(p, r, src, P, alpha) < 2e-5
+    # every residual of a vertex that can push is at most rmax
+    elig = deg > 0
+    assert (r[:, elig] <= np.float32(rmax)).all()
+    assert (p >= 0).all()
+    if oracle_p is not None:
+        c = reach_weight(P, alpha)
+        bound = 2 * rmax * c[None, :] + 1e-6
+        assert (np.abs(p.astype(np.float64) - oracle_p) <= bound).all()
+
+
+@pytest.mark.parametrize("directed", [False, True])
+def test_ppr_from_scratch_and_dynamic(directed):
+    cfg = small_cfg(directed)
+    _, snaps, src = W.build(cfg, seed=5)
+    g = native.OracleGraph(cfg["n"], directed)
+    ors = [native.OraclePPR(cfg["n"], src) for _ in range(2 if directed else 1)]
+    kw = W.session_kwargs(cfg, dynamic_start=2)
+    with T.Session(cfg["n"], src, **kw) as s:
+        for it, e in enumerate(snaps[:3], start=1):
+            s.graph_insert(e)
+            g.insert(e)
+            for t in range(2 if directed else 1):
+                s.ppr_refresh(it, bool(t))
+                s.ppr_push(bool(t))
+                ors[t].refresh(g, t, it, 2, cfg["alpha"], cfg["rmax"])
+                ors[t].push(g, t, cfg["alpha"], cfg["rmax"])
+                _ppr_checks(s, g, src, cfg, bool(t), ors[t].reserve().astype(np.float64))
+
+
+def test_ppr_intdiv_refresh_tracks_oracle():
+    cfg = small_cfg()
+    _, snaps, src = W.build(cfg, seed=9)
+    g = native.OracleGraph(cfg["n"], False)
+    o = native.OraclePPR(cfg["n"], src)
+    kw = W.session_kwargs(cfg, dynamic_start=2)
+    kw["refresh_mode"] = T.REFRESH_INTDIV
+    with T.Session(cfg["n"], src, **kw) as s:
+        for it, e in enumerate(snaps[:3], start=1):
+            s.graph_insert(e)
+            g.insert(e)
+            s.ppr_refresh(it)
+            s.ppr_push()
+            o.refresh(g, 0, it, 2, cfg["alpha"], cfg["rmax"], intdiv=True)
+            o.push(g, 0, cfg["alpha"], cfg["rmax"])
+        off, nb = g.adjacency(0)
+        P, deg = transition(cfg["n"], off, nb)
+        c = reach_weight(P, cfg["alpha"])
+        p = s.ppr_state(False, 1).astype(np.float64)
+        assert (np.abs(p - o.reserve()) <= 4 * cfg["rmax"] * c[None, :] + 1e-6).all()
+
+
+def test_block_materialize_matches_transform():
+    cfg = small_cfg()
+    _, snaps, src = W.build(cfg, seed=13)
+    kw = W.session_kwargs(cfg)
+    with T.Session(cfg["n"], src, **kw) as s:
+        s.graph_insert(snaps[0])
+        s.ppr_refresh(1)
+        s.ppr_push()
+        dirty = s.blocks_materialize(1)
+        assert dirty.all()
+        p = s.ppr_state(False, 1).astype(np.float64)
+        info = s.block_info()
+        cd = cfg["n"] // cfg["n_parts"]
+        for b in range(cfg["n_parts"]):
+            c0 = b * cd
+            c1 = cfg["n"] if b == cfg["n_parts"] - 1 else c0 + cd
+            ref = log_transform(p[:, c0:c1], cfg["rmax"], cfg["transform"], cfg["n"])
+            got = s.block_dense(b).astype(np.float64)
+            # half precision storage: |err| <= 2^-11 |a| (+ subnormal floor)
+            assert (np.abs(got - ref) <= 2.0 ** -11 * np.abs(ref) + 1e-7).all()
+            assert info["norm"][b] == pytest.approx(np.linalg.norm(ref), rel=1e-5)
+            assert info["nnz"][b] == np.count_nonzero(ref)
+
+
+def _random_lowrank_csr(m, n, rank, density, seed):
+    import scipy.sparse as sp
+    rng = np.random.default_rng(seed)
+    U = rng.standard_normal((m, rank))
+    V = rng.standard_normal((rank, n))
+    s = 0.97 ** np.arange(rank)
+    D = (U * s) @ V
+    mask = rng.random((m, n)) < density
+    D = np.where(mask, np.abs(D), 0.0)
+    return sp.csr_matrix(D)
+
+
+def test_frpca_abi_matches_oracle():
+    m, n, k, q = 300, 2000, 32, 6
+    A = _random_lowrank_csr(m, n, 80, 0.3, seed=1)
+    U, S, V = T.frpca(A.indptr, A.indices, A.data, A.shape, k, q, seed=77)
+    l = k + 5
+    omega = gaussian_matrix(77, 0, n, l)
+    Uo, So, Vo = oracle_frpca(A.toarray(), k, q, omega=omega)
+    So = So[::-1]
+    Uo = Uo[:, ::-1]
+    assert np.allclose(S, So, rtol=1e-3, atol=1e-6 * So[0])
+    j = gap_index(So, k)
+    assert j > 0
+    assert max_principal_sine(U[:, :j], Uo[:, :j]) < 1e-2
+    assert np.abs(U.T @ U - np.eye(k)).max() < 1e-3
+    # the reconstruction U S V^T agrees with the oracle's
+    R = (U * S) @ V.T
+    Ro = (Uo * So) @ Vo[:, ::-1].T
+    assert np.linalg.norm(R - Ro) / np.linalg.norm(Ro) < 1e-3
+
+
+@pytest.mark.parametrize("directed", [False, True])
+def test_session_matches_oracle_pipeline(directed):
+    cfg = small_cfg(directed, n=8000, m=60000, sources=96, n_parts=4, rank_d=32, snapshots=4)
+    _, snaps, src = W.build(cfg, seed=21)
+    kw = W.session_kwargs(cfg, dynamic_start=2, lazy_start=2)
+    okw = dict(kw)
+    okw.pop("seed")
+    o = OracleTreeSVD(cfg["n"], src, seed=20231, threads=8, **okw)
+    with T.Session(cfg["n"], src, **kw) as s:
+        for e in snaps:
+            st = s.step(e)
+            emb_o = o.step(e)
+            info = s.block_info()
+            # dirty sets agree wherever the decision is not a near-tie
+            margin = np.abs(info["norm_diff"] - cfg["dirty_frac"] * info["norm"]) > 1e-3 * info["norm"]
+            if cfg["dirty_rule"] == T.DIRTY_FROBENIUS:
+                assert np.array_equal(info["dirty"][margin], o.dirty[margin])
+            assert st["factorized_blocks"] == len(o.last_factorized) or not margin.all()
+            if emb_o is None:
+                continue
+            emb = s.embedding()
+            assert np.isfinite(emb).all()
+            _, sig = s.tree_factor(0)
+            k = cfg["rank_d"]
+            assert np.allclose(sig[:8], o.sigma[0][:8], rtol=2e-3)
+            assert gram_rel_err(emb, emb_o) < 2e-2

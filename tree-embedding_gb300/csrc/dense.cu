@@ -1,0 +1,933 @@
+// Dense kernels of the blockwise randomized SVD and the tree merge.
+//
+//  gemm_fwd / gemm_bwd : the two products of every frPCA pass,
+//      Y = A X   and   Z = A^T Y   (Code/frpca.c:259,280,282,294 via
+//      csr_matrix_{,transpose_}matrix_mult, ..._ext.c:364-398),
+//    with A stored once per block as A^T in half precision (vertex-major, the
+//    layout the PPR state has) and the skinny operand split into hi + lo
+//    halves so that it keeps ~22 significant bits. Tensor cores (mma.sync
+//    m16n8k16, fp32 accumulate), cp.async 3-stage pipeline.
+//  gram_batched : X^T X with error-free products and compensated sums per
+//    row chunk, chunks summed in fp64 (Code/frpca.c:101, cblas_dgemm TN).
+//  chol_inverse_batched / apply_right_batched : CholeskyQR2 normalization,
+//    replacing LUfraction (Code/frpca.c:4-41); the span of the basis, which
+//    is all the power iteration keeps, is the same.
+//  jacobi_eig_batched : two-sided cyclic Jacobi on the packed Gram in shared
+//    memory, replacing LAPACKE_dsyevd (frpca.c:102) and the Gram route to
+//    LAPACKE_dgesvd (..._mkl.c:1278) for the merge.
+#include <algorithm>
+#include <cfloat>
+
+#include "internal.h"
+
+namespace tsvd {
+
+namespace {
+
+constexpr unsigned kFull = 0xffffffffu;
+
+// ------------------------------------------------------------------ PTX helpers
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem, bool valid) {
+  uint32_t s = smem_u32(smem);
+  int n = valid ? 16 : 0;
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(s), "l"(gmem), "r"(n));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N));
+}
+__device__ __forceinline__ void ldsm_x4(uint32_t &r0, uint32_t &r1, uint32_t &r2, uint32_t &r3,
+                                        const void *p) {
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+               : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
+               : "r"(smem_u32(p)));
+}
+__device__ __forceinline__ void ldsm_x4_t(uint32_t &r0, uint32_t &r1, uint32_t &r2, uint32_t &r3,
+                                          const void *p) {
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+               : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
+               : "r"(smem_u32(p)));
+}
+__device__ __forceinline__ void ldsm_x2_t(uint32_t &r0, uint32_t &r1, const void *p) {
+  asm volatile("ldmatrix.sync.aligned.m8n8.x2.trans.shared.b16 {%0,%1}, [%2];\n"
+               : "=r"(r0), "=r"(r1)
+               : "r"(smem_u32(p)));
+}
+__device__ __forceinline__ void mma16816(float *c, const uint32_t *a, uint32_t b0, uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
+      "{%8,%9}, {%0,%1,%2,%3};\n"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// ------------------------------------------------------------------ GEMM tiles
+constexpr int BM = 128, BN = kLp, BK = 32, STAGES = 3, GEMM_THREADS = 256;
+constexpr int WN_TILES = 9;            // 72 columns per warp = 9 n8 tiles
+constexpr int SB_LD = BN + 8;          // 152 halves
+constexpr int SA_FWD_LD = BM + 8;      // 136 halves (rows = k)
+constexpr int SA_BWD_LD = BK + 8;      // 40 halves (rows = m)
+constexpr int SA_FWD_ELEMS = BK * SA_FWD_LD;
+constexpr int SA_BWD_ELEMS = BM * SA_BWD_LD;
+constexpr int SB_ELEMS = BK * SB_LD;
+
+struct GemmArgs {
+  const __half *const *at;
+  const int32_t *ncols;
+  int lda;  // Sp
+  const __half *const *bhi;
+  const __half *const *blo;
+  float *const *out;
+  float scale;
+  int splits;  // fwd split-K
+};
+
+// Load the skinny operand tile rows [k0, k0+BK) (all BN columns) of hi and lo.
+__device__ __forceinline__ void load_b_tile(__half *sb_hi, __half *sb_lo, const __half *bhi,
+                                            const __half *blo, int k0, int krows) {
+  constexpr int CHUNKS = BK * (BN / 8);  // 16-byte chunks per operand tile
+  for (int c = threadIdx.x; c < 2 * CHUNKS; c += GEMM_THREADS) {
+    int which = c / CHUNKS, cc = c % CHUNKS;
+    int row = cc / (BN / 8), col = (cc % (BN / 8)) * 8;
+    bool valid = k0 + row < krows && (which == 0 || blo != nullptr);
+    const __half *src = (which ? blo : bhi);
+    const __half *g = valid ? src + (int64_t)(k0 + row) * BN + col : bhi;
+    __half *s = (which ? sb_lo : sb_hi) + row * SB_LD + col;
+    cp_async16(s, g, valid);
+  }
+}
+
+// Fragments of 9 n8-tiles starting at column nbase for k16 step ks.
+__device__ __forceinline__ void load_b_frags(uint32_t (*b)[2], const __half *sb, int ks,
+                                             int nbase) {
+  const int lane = threadIdx.x & 31;
+  const int j = lane >> 3, r = lane & 7;
+#pragma unroll
+  for (int t = 0; t < 4; ++t) {
+    const __half *p = sb + (ks + (j & 1) * 8 + r) * SB_LD + nbase + (2 * t + (j >> 1)) * 8;
+    ldsm_x4_t(b[2 * t][0], b[2 * t][1], b[2 * t + 1][0], b[2 * t + 1][1], p);
+  }
+  const __half *p = sb + (ks + (j & 1) * 8 + r) * SB_LD + nbase + 8 * 8;
+  ldsm_x2_t(b[8][0], b[8][1], p);
+}
+
+__device__ __forceinline__ void store_acc(float (*acc)[WN_TILES][4], float *out, int m_base,
+                                          int nbase, int mrows, bool atomic, float scale) {
+  const int lane = threadIdx.x & 31, g = lane >> 2, t4 = lane & 3;
+#pragma unroll
+  for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+    for (int nt = 0; nt < WN_TILES; ++nt)
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        int row = m_base + mt * 16 + g + h * 8;
+        if (row >= mrows) continue;
+        int col = nbase + nt * 8 + 2 * t4;
+        float v0 = acc[mt][nt][2 * h] * scale, v1 = acc[mt][nt][2 * h + 1] * scale;
+        float *o = out + (int64_t)row * BN + col;
+        if (atomic) {
+          atomicAdd(o, v0);
+          atomicAdd(o + 1, v1);
+        } else {
+          *reinterpret_cast<float2 *>(o) = make_float2(v0, v1);
+        }
+      }
+}
+
+// Y (Sp x BN) [+]= A (Sp x nc) * B (nc x BN); A given as A^T [nc][lda].
+__global__ void __launch_bounds__(GEMM_THREADS) gemm_fwd_kernel(GemmArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __half *sA = reinterpret_cast<__half *>(smem_raw);
+  __half *sBh = sA + STAGES * SA_FWD_ELEMS;
+  __half *sBl = sBh + STAGES * SB_ELEMS;
+  const int prob = blockIdx.z;
+  const int nc = a.ncols[prob];
+  const __half *at = a.at[prob];
+  const __half *bhi = a.bhi[prob];
+  const __half *blo = a.blo ? a.blo[prob] : nullptr;
+  const int m0 = blockIdx.x * BM;
+  const int nk_total = (nc + BK - 1) / BK;
+  const int per = (nk_total + a.splits - 1) / a.splits;
+  const int kt0 = blockIdx.y * per, kt1 = min(nk_total, kt0 + per);
+  if (kt0 >= kt1) return;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int wm = warp & 3, wn = warp >> 2;
+
+  auto load_a = [&](int stage, int kt) {
+    __half *s = sA + stage * SA_FWD_ELEMS;
+    const int k0 = kt * BK;
+    for (int c = threadIdx.x; c < BK * (BM / 8); c += GEMM_THREADS) {
+      int row = c / (BM / 8), col = (c % (BM / 8)) * 8;
+      bool valid = k0 + row < nc;
+      const __half *g = valid ? at + (int64_t)(k0 + row) * a.lda + m0 + col : at;
+      cp_async16(s + row * SA_FWD_LD + col, g, valid);
+    }
+  };
+  auto load_stage = [&](int stage, int kt) {
+    load_a(stage, kt);
+    load_b_tile(sBh + stage * SB_ELEMS, sBl + stage * SB_ELEMS, bhi, blo, kt * BK, nc);
+  };
+
+  float acc[2][WN_TILES][4];
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+#pragma unroll
+    for (int j = 0; j < WN_TILES; ++j)
+#pragma unroll
+      for (int k = 0; k < 4; ++k) acc[i][j][k] = 0.f;
+
+  for (int s = 0; s < STAGES - 1; ++s) {
+    if (kt0 + s < kt1) load_stage(s, kt0 + s);
+    cp_async_commit();
+  }
+  for (int kt = kt0; kt < kt1; ++kt) {
+    cp_async_wait<STAGES - 2>();
+    __syncthreads();
+    int nxt = kt + STAGES - 1;
+    if (nxt < kt1) load_stage((nxt - kt0) % STAGES, nxt);
+    cp_async_commit();
+    const int st = (kt - kt0) % STAGES;
+    const __half *cA = sA + st * SA_FWD_ELEMS;
+    const __half *cBh = sBh + st * SB_ELEMS;
+    const __half *cBl = sBl + st * SB_ELEMS;
+#pragma unroll
+    for (int ks = 0; ks < BK; ks += 16) {
+      uint32_t af[2][4];
+      const int j = lane >> 3, r = lane & 7;
+#pragma unroll
+      for (int mt = 0; mt < 2; ++mt) {
+        const __half *p = cA + (ks + (j >> 1) * 8 + r) * SA_FWD_LD + wm * 32 + mt * 16 + (j & 1) * 8;
+        ldsm_x4_t(af[mt][0], af[mt][1], af[mt][2], af[mt][3], p);
+      }
+      uint32_t bf[WN_TILES][2];
+      load_b_frags(bf, cBh, ks, wn * 72);
+#pragma unroll
+      for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+        for (int nt = 0; nt < WN_TILES; ++nt) mma16816(acc[mt][nt], af[mt], bf[nt][0], bf[nt][1]);
+      if (blo) {
+        load_b_frags(bf, cBl, ks, wn * 72);
+#pragma unroll
+        for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+          for (int nt = 0; nt < WN_TILES; ++nt)
+            mma16816(acc[mt][nt], af[mt], bf[nt][0], bf[nt][1]);
+      }
+    }
+  }
+  cp_async_wait<0>();
+  store_acc(acc, a.out[prob], m0 + wm * 32, wn * 72, a.lda, a.splits > 1, a.scale);
+}
+
+// Z (nc x BN) = A^T (nc x Sp) * B (Sp x BN); A^T [nc][lda].
+__global__ void __launch_bounds__(GEMM_THREADS) gemm_bwd_kernel(GemmArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __half *sA = reinterpret_cast<__half *>(smem_raw);
+  __half *sBh = sA + STAGES * SA_BWD_ELEMS;
+  __half *sBl = sBh + STAGES * SB_ELEMS;
+  const int prob = blockIdx.z;
+  const int nc = a.ncols[prob];
+  const int m0 = blockIdx.x * BM;
+  if (m0 >= nc) return;
+  const __half *at = a.at[prob];
+  const __half *bhi = a.bhi[prob];
+  const __half *blo = a.blo ? a.blo[prob] : nullptr;
+  const int nk = a.lda / BK;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int wm = warp & 3, wn = warp >> 2;
+
+  auto load_stage = [&](int stage, int kt) {
+    __half *s = sA + stage * SA_BWD_ELEMS;
+    const int k0 = kt * BK;
+    for (int c = threadIdx.x; c < BM * (BK / 8); c += GEMM_THREADS) {
+      int row = c / (BK / 8), col = (c % (BK / 8)) * 8;
+      bool valid = m0 + row < nc;
+      const __half *g = valid ? at + (int64_t)(m0 + row) * a.lda + k0 + col : at;
+      cp_async16(s + row * SA_BWD_LD + col, g, valid);
+    }
+    load_b_tile(sBh + stage * SB_ELEMS, sBl + stage * SB_ELEMS, bhi, blo, k0, a.lda);
+  };
+
+  float acc[2][WN_TILES][4];
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+#pragma unroll
+    for (int j = 0; j < WN_TILES; ++j)
+#pragma unroll
+      for (int k = 0; k < 4; ++k) acc[i][j][k] = 0.f;
+
+  for (int s = 0; s < STAGES - 1; ++s) {
+    if (s < nk) load_stage(s, s);
+    cp_async_commit();
+  }
+  for (int kt = 0; kt < nk; ++kt) {
+    cp_async_wait<STAGES - 2>();
+    __syncthreads();
+    int nxt = kt + STAGES - 1;
+    if (nxt < nk) load_stage(nxt % STAGES, nxt);
+    cp_async_commit();
+    const int st = kt % STAGES;
+    const __half *cA = sA + st * SA_BWD_ELEMS;
+    const __half *cBh = sBh + st * SB_ELEMS;
+    const __half *cBl = sBl + st * SB_ELEMS;
+#pragma unroll
+    for (int ks = 0; ks < BK; ks += 16) {
+      uint32_t af[2][4];
+      const int j = lane >> 3, r = lane & 7;
+#pragma unroll
+      for (int mt = 0; mt < 2; ++mt) {
+        const __half *p = cA + (wm * 32 + mt * 16 + (j & 1) * 8 + r) * SA_BWD_LD + ks + (j >> 1) * 8;
+        ldsm_x4(af[mt][0], af[mt][1], af[mt][2], af[mt][3], p);
+      }
+      uint32_t bf[WN_TILES][2];
+      load_b_frags(bf, cBh, ks, wn * 72);
+#pragma unroll
+      for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+        for (int nt = 0; nt < WN_TILES; ++nt) mma16816(acc[mt][nt], af[mt], bf[nt][0], bf[nt][1]);
+      if (blo) {
+        load_b_frags(bf, cBl, ks, wn * 72);
+#pragma unroll
+        for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+          for (int nt = 0; nt < WN_TILES; ++nt)
+            mma16816(acc[mt][nt], af[mt], bf[nt][0], bf[nt][1]);
+      }
+    }
+  }
+  cp_async_wait<0>();
+  store_acc(acc, a.out[prob], m0 + wm * 32, wn * 72, nc, false, a.scale);
+}
+
+constexpr size_t kFwdSmem = (size_t)STAGES * (SA_FWD_ELEMS + 2 * SB_ELEMS) * sizeof(__half);
+constexpr size_t kBwdSmem = (size_t)STAGES * (SA_BWD_ELEMS + 2 * SB_ELEMS) * sizeof(__half);
+
+// ------------------------------------------------------------------ Gram
+// Error-free product + TwoSum accumulation (Ogita, Rump, Oishi, "Accurate sum
+// and dot product", SISC 2005): s + c carries the chunk sum to ~2^-44.
+struct Comp {
+  float s, c;
+};
+__device__ __forceinline__ void comp_add(Comp &acc, float a, float b) {
+  float p = a * b;
+  float e = fmaf(a, b, -p);
+  float t = acc.s + p;
+  float z = t - acc.s;
+  float err = (acc.s - (t - z)) + (p - z);
+  acc.s = t;
+  acc.c += err + e;
+}
+
+constexpr int GRAM_MIN_ROWS = 128;    // rows per CTA at least (one fp64 partial per chunk)
+constexpr int GRAM_MAX_CHUNKS = 2048;  // chunks over all problems (bounds the work buffer)
+constexpr int GRAM_SUB = 32;      // rows staged in smem at a time
+constexpr int GRAM_THREADS = 512;
+constexpr int GRAM_TPT = 2;       // 4x4 output tiles per thread
+constexpr int GRAM_TILES_PER_CTA = GRAM_THREADS * GRAM_TPT;
+constexpr int GRAM_LMAX = 256;
+
+struct GramArgs {
+  const float *const *x;
+  const int32_t *rows;
+  int ld;
+  int l;
+  int tiles;      // ceil(l/4)
+  int nchunks;    // per problem
+  int chunk_rows;
+  double *work;   // [prob][chunk][l*l]
+};
+
+// grid: (row chunk, tile group, problem). Each thread owns <= 2 upper-triangle
+// 4x4 tiles of the l x l output and accumulates them over the chunk's rows.
+__global__ void __launch_bounds__(GRAM_THREADS) gram_partial_kernel(GramArgs a) {
+  extern __shared__ __align__(16) float sx[];  // [GRAM_SUB][ld]
+  const int prob = blockIdx.z, chunk = blockIdx.x;
+  const int rows = a.rows[prob];
+  const int r0 = chunk * a.chunk_rows;
+  double *out = a.work + ((int64_t)prob * a.nchunks + chunk) * a.l * a.l;
+  const int T = a.tiles;
+  const int ntile_pairs = T * (T + 1) / 2;
+  const float *x = a.x[prob];
+  const int r1 = min(rows, r0 + a.chunk_rows);
+  Comp acc[GRAM_TPT][16];
+  int ti[GRAM_TPT], tj[GRAM_TPT];
+  int my = 0;
+#pragma unroll
+  for (int k = 0; k < GRAM_TPT; ++k) {
+    int t = blockIdx.y * GRAM_TILES_PER_CTA + k * GRAM_THREADS + threadIdx.x;
+    ti[k] = tj[k] = 0;
+    if (t < ntile_pairs) {
+      int J = (int)((sqrtf(8.f * t + 1.f) - 1.f) * 0.5f);
+      while ((J + 1) * (J + 2) / 2 <= t) ++J;
+      while (J * (J + 1) / 2 > t) --J;
+      int I = t - J * (J + 1) / 2;
+      ti[k] = I * 4;
+      tj[k] = J * 4;
+      my = k + 1;
+    }
+#pragma unroll
+    for (int e = 0; e < 16; ++e) acc[k][e] = Comp{0.f, 0.f};
+  }
+  const int sld = 4 * T;  // staged row stride covers every 4x4 tile column
+  for (int rb = r0; rb < r1; rb += GRAM_SUB) {
+    const int nr = min(GRAM_SUB, r1 - rb);
+    __syncthreads();
+    for (int i = threadIdx.x; i < GRAM_SUB * sld; i += blockDim.x) {
+      int rr = i / sld, cc = i % sld;
+      sx[i] = (rr < nr && cc < a.l) ? x[(int64_t)(rb + rr) * a.ld + cc] : 0.f;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < GRAM_TPT; ++k) {
+      if (k >= my) break;
+      for (int rr = 0; rr < nr; ++rr) {
+        const float *row = sx + rr * sld;
+        float xi[4], xj[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          xi[q] = row[ti[k] + q];
+          xj[q] = row[tj[k] + q];
+        }
+#pragma unroll
+        for (int p = 0; p < 4; ++p)
+#pragma unroll
+          for (int q = 0; q < 4; ++q) comp_add(acc[k][p * 4 + q], xi[p], xj[q]);
+      }
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < GRAM_TPT; ++k) {
+    if (k >= my) break;
+#pragma unroll
+    for (int p = 0; p < 4; ++p)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        int i = ti[k] + p, j = tj[k] + q;
+        if (i >= a.l || j >= a.l) continue;
+        double v = (double)acc[k][p * 4 + q].s + (double)acc[k][p * 4 + q].c;
+        out[i * a.l + j] = v;
+        out[j * a.l + i] = v;
+      }
+  }
+}
+
+__global__ void gram_reduce_kernel(const double *__restrict__ work, int nchunks, int l,
+                                   double *const *g, int nprob) {
+  const int prob = blockIdx.y;
+  const int64_t ll = (int64_t)l * l;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < ll;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    double s = 0.0;
+    const double *w = work + (int64_t)prob * nchunks * ll + i;
+    for (int c = 0; c < nchunks; ++c) s += w[c * ll];
+    g[prob][i] = s;
+  }
+}
+
+// ------------------------------------------------------------------ Cholesky
+constexpr int CHOL_THREADS = 512;
+__global__ void __launch_bounds__(CHOL_THREADS) chol_inverse_kernel(double *const *gs,
+                                                                    float *const *ts, int l) {
+  extern __shared__ __align__(16) float sm[];
+  const int LD = l + 1;
+  float *L = sm;              // [l][LD]
+  float *Li = sm + l * LD;    // [l][LD]
+  __shared__ int drop[kLp];
+  __shared__ float tol;
+  const double *G = gs[blockIdx.x];
+  float *T = ts[blockIdx.x];
+  for (int i = threadIdx.x; i < l * l; i += blockDim.x) {
+    int r = i / l, c = i % l;
+    L[r * LD + c] = (float)G[i];
+    Li[r * LD + c] = 0.f;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float mx = 0.f;
+    for (int i = 0; i < l; ++i) mx = fmaxf(mx, L[i * LD + i]);
+    tol = mx * 1e-12f;
+  }
+  __syncthreads();
+  for (int k = 0; k < l; ++k) {
+    if (threadIdx.x == 0) {
+      float d = L[k * LD + k];
+      if (!(d > tol) || !(d > 0.f)) {
+        drop[k] = 1;
+        L[k * LD + k] = 1.f;
+      } else {
+        drop[k] = 0;
+        L[k * LD + k] = sqrtf(d);
+      }
+    }
+    __syncthreads();
+    const float piv = L[k * LD + k];
+    const int dk = drop[k];
+    for (int i = k + 1 + threadIdx.x; i < l; i += blockDim.x)
+      L[i * LD + k] = dk ? 0.f : L[i * LD + k] / piv;
+    __syncthreads();
+    const int n = l - k - 1;
+    for (int t = threadIdx.x; t < n * n; t += blockDim.x) {
+      int i = k + 1 + t / n, j = k + 1 + t % n;
+      if (j <= i) L[i * LD + j] -= L[i * LD + k] * L[j * LD + k];
+    }
+    __syncthreads();
+  }
+  // Li = L^{-1} by forward substitution, one column per thread.
+  for (int j = threadIdx.x; j < l; j += blockDim.x) {
+    Li[j * LD + j] = 1.f / L[j * LD + j];
+    for (int i = j + 1; i < l; ++i) {
+      float s = 0.f;
+      for (int k = j; k < i; ++k) s += L[i * LD + k] * Li[k * LD + j];
+      Li[i * LD + j] = -s / L[i * LD + i];
+    }
+  }
+  __syncthreads();
+  // T = R^{-1} = (L^{-1})^T, dropped directions zeroed.
+  for (int i = threadIdx.x; i < l * kLp; i += blockDim.x) {
+    int r = i / kLp, c = i % kLp;
+    float v = 0.f;
+    if (c < l && r < l && c >= r && !drop[c]) v = Li[c * LD + r];
+    T[i] = v;
+  }
+}
+
+// ------------------------------------------------------------------ X * W
+constexpr int APPLY_ROWS = 32;
+constexpr int APPLY_THREADS = 256;
+struct ApplyArgs {
+  const float *const *x;
+  const int32_t *rows;
+  int ldx;
+  const float *const *w;
+  int ldw;
+  int n_in, n_out;
+  const float *const *colscale;
+  float *const *y;
+  int ldy;
+  __half *const *yhi;
+  __half *const *ylo;
+  float split_scale;
+};
+
+__global__ void __launch_bounds__(APPLY_THREADS) apply_right_kernel(ApplyArgs a) {
+  extern __shared__ __align__(16) float sm[];
+  float *sw = sm;                          // [n_in][n_out]
+  float *sx = sm + a.n_in * a.n_out;       // [APPLY_ROWS][n_in]
+  const int prob = blockIdx.y;
+  const int rows = a.rows[prob];
+  const float *W = a.w[prob];
+  const float *cs = a.colscale ? a.colscale[prob] : nullptr;
+  for (int i = threadIdx.x; i < a.n_in * a.n_out; i += blockDim.x) {
+    int r = i / a.n_out, c = i % a.n_out;
+    sw[i] = W[(int64_t)r * a.ldw + c] * (cs ? cs[c] : 1.f);
+  }
+  const float *X = a.x[prob];
+  float *Y = a.y[prob];
+  __half *Yh = a.yhi ? a.yhi[prob] : nullptr;
+  __half *Yl = a.ylo ? a.ylo[prob] : nullptr;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int r0 = blockIdx.x * APPLY_ROWS; r0 < rows; r0 += gridDim.x * APPLY_ROWS) {
+    __syncthreads();
+    for (int i = threadIdx.x; i < APPLY_ROWS * a.n_in; i += blockDim.x) {
+      int rr = i / a.n_in, cc = i % a.n_in;
+      sx[i] = r0 + rr < rows ? X[(int64_t)(r0 + rr) * a.ldx + cc] : 0.f;
+    }
+    __syncthreads();
+    // warp w handles rows w, w+8, w+16, w+24; lane handles columns lane+32q
+    for (int rr = warp; rr < APPLY_ROWS; rr += APPLY_THREADS / 32) {
+      const int row = r0 + rr;
+      if (row >= rows) break;
+      float acc[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) acc[q] = 0.f;
+      const float *xr = sx + rr * a.n_in;
+      for (int k = 0; k < a.n_in; ++k) {
+        float xv = xr[k];
+        const float *wr = sw + k * a.n_out;
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          int c = lane + 32 * q;
+          if (c < a.n_out) acc[q] = fmaf(xv, wr[c], acc[q]);
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        int c = lane + 32 * q;
+        if (c >= a.ldy) continue;
+        float v = c < a.n_out ? acc[q] : 0.f;
+        Y[(int64_t)row * a.ldy + c] = v;
+        if (Yh) {
+          float sv = v * a.split_scale;
+          __half h = __float2half_rn(sv);
+          Yh[(int64_t)row * a.ldy + c] = h;
+          Yl[(int64_t)row * a.ldy + c] = __float2half_rn(sv - __half2float(h));
+        }
+      }
+    }
+  }
+}
+
+// ------------------------------------------------------------------ Jacobi
+constexpr int JAC_THREADS = 1024;
+constexpr int JAC_MAX_SWEEPS = 30;
+
+__device__ __forceinline__ int packed(int i, int j) {  // i <= j
+  return j * (j + 1) / 2 + i;
+}
+__device__ __forceinline__ int pk(int i, int j) { return i <= j ? packed(i, j) : packed(j, i); }
+
+// Player at circle position `pos` in round `t` of a round-robin over np players.
+__device__ __forceinline__ int circle_player(int pos, int t, int np) {
+  return pos == 0 ? 0 : ((pos - 1 + t) % (np - 1)) + 1;
+}
+
+struct JacobiArgs {
+  double *const *g;
+  int n;
+  float *const *lambda;
+  float2 *log;        // [prob][JAC_MAX_SWEEPS][np-1][np/2]
+  int32_t *sweeps;    // [prob]
+  int32_t *rank;      // [prob][n]
+};
+
+__global__ void __launch_bounds__(JAC_THREADS) jacobi_kernel(JacobiArgs a) {
+  extern __shared__ __align__(16) float G[];  // packed upper triangle, then the pair table
+  __shared__ float pc[128], ps[128], pt[128];
+  __shared__ int pp[128], pq[128];
+  __shared__ int rotated;
+  __shared__ float dmax;
+  const int n = a.n, np = n + (n & 1), P = np / 2;
+  const int npairs = P * (P + 1) / 2;
+  uint16_t *tab = reinterpret_cast<uint16_t *>(G + n * (n + 1) / 2);
+  const int prob = blockIdx.x;
+  const double *Gin = a.g[prob];
+  for (int idx = threadIdx.x; idx < n * n; idx += blockDim.x) {
+    int i = idx / n, j = idx % n;
+    if (i <= j) G[packed(i, j)] = (float)Gin[idx];
+  }
+  // (k1 <= k2) pairs of rotation pairs, packed k1 << 8 | k2
+  for (int k2 = threadIdx.x; k2 < P; k2 += blockDim.x)
+    for (int k1 = 0; k1 <= k2; ++k1) tab[k2 * (k2 + 1) / 2 + k1] = (uint16_t)((k1 << 8) | k2);
+  float2 *log = a.log + (int64_t)prob * JAC_MAX_SWEEPS * (np - 1) * P;
+  __syncthreads();
+  int sweep = 0;
+  for (; sweep < JAC_MAX_SWEEPS; ++sweep) {
+    if (threadIdx.x == 0) {
+      rotated = 0;
+      float m = 0.f;
+      for (int i = 0; i < n; ++i) m = fmaxf(m, fabsf(G[packed(i, i)]));
+      dmax = m;
+    }
+    __syncthreads();
+    // Rotate when the pair is coupled beyond fp32 rounding: relative to the
+    // pair (Demmel-Veselic) and above the absolute noise floor eps * max|a_ii|
+    // that fp32 updates leave on every off-diagonal entry.
+    const float floor_abs = 2e-7f * dmax;
+    for (int t = 0; t < np - 1; ++t) {
+      if (threadIdx.x < P) {
+        const int k = threadIdx.x;
+        int x = circle_player(k, t, np), y = circle_player(np - 1 - k, t, np);
+        int p = min(x, y), q = max(x, y);
+        float c = 1.f, s = 0.f, tt = 0.f;
+        if (q < n) {
+          float app = G[packed(p, p)], aqq = G[packed(q, q)], apq = G[packed(p, q)];
+          if (fabsf(apq) > floor_abs && fabsf(apq) > 1e-7f * sqrtf(fabsf(app) * fabsf(aqq))) {
+            float tau = (aqq - app) / (2.f * apq);
+            float sg = tau >= 0.f ? 1.f : -1.f;
+            tt = sg / (fabsf(tau) + sqrtf(1.f + tau * tau));
+            c = rsqrtf(1.f + tt * tt);
+            s = tt * c;
+            rotated = 1;
+          }
+        }
+        pp[k] = p; pq[k] = q; pc[k] = c; ps[k] = s; pt[k] = tt;
+        log[((int64_t)sweep * (np - 1) + t) * P + k] = make_float2(c, s);
+      }
+      __syncthreads();
+      // G <- J^T G J, 2x2 block by 2x2 block; each entry belongs to one block.
+      for (int b = threadIdx.x; b < npairs; b += blockDim.x) {
+        const int k1 = tab[b] >> 8, k2 = tab[b] & 0xff;
+        const int p1 = pp[k1], q1 = pq[k1], p2 = pp[k2], q2 = pq[k2];
+        if (k1 == k2) {
+          if (q1 < n && pt[k1] != 0.f) {
+            float apq = G[packed(p1, q1)];
+            G[packed(p1, p1)] -= pt[k1] * apq;
+            G[packed(q1, q1)] += pt[k1] * apq;
+            G[packed(p1, q1)] = 0.f;
+          }
+          continue;
+        }
+        const float c1 = pc[k1], s1 = ps[k1], c2 = pc[k2], s2 = ps[k2];
+        if (s1 == 0.f && s2 == 0.f) continue;
+        const bool hq1 = q1 < n, hq2 = q2 < n;
+        float b00 = G[pk(p1, p2)];
+        float b01 = hq2 ? G[pk(p1, q2)] : 0.f;
+        float b10 = hq1 ? G[pk(q1, p2)] : 0.f;
+        float b11 = (hq1 && hq2) ? G[pk(q1, q2)] : 0.f;
+        float t00 = c1 * b00 - s1 * b10, t01 = c1 * b01 - s1 * b11;
+        float t10 = s1 * b00 + c1 * b10, t11 = s1 * b01 + c1 * b11;
+        G[pk(p1, p2)] = t00 * c2 - t01 * s2;
+        if (hq2) G[pk(p1, q2)] = t00 * s2 + t01 * c2;
+        if (hq1) G[pk(q1, p2)] = t10 * c2 - t11 * s2;
+        if (hq1 && hq2) G[pk(q1, q2)] = t10 * s2 + t11 * c2;
+      }
+      __syncthreads();
+    }
+    const int any_rotation = rotated;
+    __syncthreads();  // everyone has read `rotated` before thread 0 resets it
+    if (!any_rotation) break;
+  }
+  const int done = min(sweep + 1, JAC_MAX_SWEEPS);
+  if (threadIdx.x == 0) a.sweeps[prob] = done;
+  // eigenvalues and their descending rank
+  float *lam = a.lambda[prob];
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    float li = G[packed(i, i)];
+    int r = 0;
+    for (int j = 0; j < n; ++j) {
+      float lj = G[packed(j, j)];
+      r += (lj > li) || (lj == li && j < i);
+    }
+    a.rank[prob * n + i] = r;
+    lam[r] = li;
+  }
+}
+
+// V = product of the logged rotations, rows processed independently;
+// column c of the product lands in column rank[c] of the output.
+constexpr int REPLAY_ROWS = 16;
+__global__ void __launch_bounds__(256) jacobi_replay_kernel(JacobiArgs a, float *const *vout) {
+  extern __shared__ __align__(16) float sv[];  // [REPLAY_ROWS][n]
+  const int n = a.n, np = n + (n & 1), P = np / 2;
+  const int prob = blockIdx.y;
+  const int r0 = blockIdx.x * REPLAY_ROWS;
+  const int nr = min(REPLAY_ROWS, n - r0);
+  if (nr <= 0) return;
+  for (int i = threadIdx.x; i < REPLAY_ROWS * n; i += blockDim.x) {
+    int rr = i / n, cc = i % n;
+    sv[i] = (rr < nr && r0 + rr == cc) ? 1.f : 0.f;
+  }
+  const float2 *log = a.log + (int64_t)prob * JAC_MAX_SWEEPS * (np - 1) * P;
+  const int sweeps = a.sweeps[prob];
+  __syncthreads();
+  for (int sw = 0; sw < sweeps; ++sw)
+    for (int t = 0; t < np - 1; ++t) {
+      const float2 *lg = log + ((int64_t)sw * (np - 1) + t) * P;
+      for (int w = threadIdx.x; w < P * REPLAY_ROWS; w += blockDim.x) {
+        const int k = w % P, rr = w / P;
+        if (rr >= nr) continue;
+        float2 cs = lg[k];
+        if (cs.y == 0.f) continue;
+        int x = circle_player(k, t, np), y = circle_player(np - 1 - k, t, np);
+        int p = min(x, y), q = max(x, y);
+        if (q >= n) continue;
+        float vp = sv[rr * n + p], vq = sv[rr * n + q];
+        sv[rr * n + p] = cs.x * vp - cs.y * vq;
+        sv[rr * n + q] = cs.y * vp + cs.x * vq;
+      }
+      __syncthreads();
+    }
+  float *V = vout[prob];
+  const int32_t *rank = a.rank + prob * n;
+  for (int i = threadIdx.x; i < nr * n; i += blockDim.x) {
+    int rr = i / n, cc = i % n;
+    V[(int64_t)(r0 + rr) * n + rank[cc]] = sv[rr * n + cc];
+  }
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ host side
+int sm_count() {
+  static int n = 0;
+  if (n == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    if (n <= 0) n = 1;
+  }
+  return n;
+}
+
+int grid_for(int64_t work_items, int threads_per_block, int blocks_per_sm) {
+  int64_t need = ceil_div(std::max<int64_t>(work_items, 1), threads_per_block);
+  int64_t cap = (int64_t)sm_count() * blocks_per_sm;
+  return (int)std::max<int64_t>(1, std::min(need, cap));
+}
+
+static tsvd_status set_smem(const void *fn, size_t bytes) {
+  TSVD_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+  return TSVD_OK;
+}
+
+tsvd_status gemm_fwd(const GemmBatch &gb, const __half *const *xhi, const __half *const *xlo,
+                     float *const *y, float *y_base, size_t y_bytes, int sp, int max_nc,
+                     float inv_xscale, cudaStream_t st) {
+  static bool init = false;
+  if (!init) {
+    TSVD_TRY(set_smem((const void *)gemm_fwd_kernel, kFwdSmem));
+    init = true;
+  }
+  if (gb.nprob == 0) return TSVD_OK;
+  const int mtiles = sp / BM;
+  int splits = 1;
+  int64_t base_ctas = (int64_t)mtiles * gb.nprob;
+  int64_t target = 2ll * sm_count();
+  if (base_ctas < target)
+    splits = (int)std::min<int64_t>(ceil_div(target, base_ctas),
+                                    std::max<int64_t>(1, ceil_div(max_nc, 1024)));
+  // split-K partial tiles are accumulated with atomics into zeroed outputs
+  if (splits > 1) TSVD_CUDA(cudaMemsetAsync(y_base, 0, y_bytes, st));
+  GemmArgs a{gb.at, gb.ncols, gb.lda, xhi, xlo, y, inv_xscale, splits};
+  dim3 grid(mtiles, splits, gb.nprob);
+  gemm_fwd_kernel<<<grid, GEMM_THREADS, kFwdSmem, st>>>(a);
+  TSVD_LAUNCH_CHECK();
+  return TSVD_OK;
+}
+
+tsvd_status gemm_bwd(const GemmBatch &gb, const __half *const *yhi, const __half *const *ylo,
+                     float *const *z, int sp, int max_nc, float inv_yscale, cudaStream_t st) {
+  static bool init = false;
+  if (!init) {
+    TSVD_TRY(set_smem((const void *)gemm_bwd_kernel, kBwdSmem));
+    init = true;
+  }
+  if (gb.nprob == 0 || max_nc == 0) return TSVD_OK;
+  GemmArgs a{gb.at, gb.ncols, sp, yhi, ylo, z, inv_yscale, 1};
+  dim3 grid((unsigned)ceil_div(max_nc, BM), 1, gb.nprob);
+  gemm_bwd_kernel<<<grid, GEMM_THREADS, kBwdSmem, st>>>(a);
+  TSVD_LAUNCH_CHECK();
+  return TSVD_OK;
+}
+
+static void gram_chunks(int max_rows, int nprob, int *nchunks, int *chunk_rows) {
+  int64_t want = ceil_div(std::max(max_rows, 1), GRAM_MIN_ROWS);
+  int64_t cap = std::max<int64_t>(1, GRAM_MAX_CHUNKS / std::max(nprob, 1));
+  int64_t nc = std::max<int64_t>(1, std::min(want, cap));
+  int64_t cr = round_up(ceil_div(std::max(max_rows, 1), nc), 32);
+  *chunk_rows = (int)cr;
+  *nchunks = (int)ceil_div(std::max(max_rows, 1), cr);
+}
+
+size_t gram_work_bytes(int max_rows, int l, int nprob) {
+  int nchunks, cr;
+  gram_chunks(max_rows, nprob, &nchunks, &cr);
+  return (size_t)nprob * nchunks * l * l * sizeof(double);
+}
+
+tsvd_status gram_batched(const float *const *x, const int32_t *rows, int max_rows, int l, int ld,
+                         double *const *g, double *work, size_t work_bytes, int nprob,
+                         cudaStream_t st) {
+  if (nprob == 0) return TSVD_OK;
+  if (l > GRAM_LMAX) return fail(TSVD_ERR_INVALID, "gram: l=%d > %d", l, GRAM_LMAX);
+  int nchunks, chunk_rows;
+  gram_chunks(max_rows, nprob, &nchunks, &chunk_rows);
+  if (gram_work_bytes(max_rows, l, nprob) > work_bytes)
+    return fail(TSVD_ERR_INVALID, "gram: work buffer too small");
+  int tiles = (l + 3) / 4;
+  int groups = (int)ceil_div(tiles * (tiles + 1) / 2, GRAM_TILES_PER_CTA);
+  static size_t cur_smem = 0;
+  size_t smem = (size_t)GRAM_SUB * (4 * tiles) * sizeof(float);
+  if (smem > cur_smem) {
+    TSVD_TRY(set_smem((const void *)gram_partial_kernel, smem));
+    cur_smem = smem;
+  }
+  // chunks past a problem's row count must contribute zeros
+  TSVD_CUDA(cudaMemsetAsync(work, 0, gram_work_bytes(max_rows, l, nprob), st));
+  GramArgs a{x, rows, ld, l, tiles, nchunks, chunk_rows, work};
+  gram_partial_kernel<<<dim3(nchunks, groups, nprob), GRAM_THREADS, smem, st>>>(a);
+  TSVD_LAUNCH_CHECK();
+  gram_reduce_kernel<<<dim3((unsigned)ceil_div((int64_t)l * l, 256), nprob), 256, 0, st>>>(
+      work, nchunks, l, g, nprob);
+  TSVD_LAUNCH_CHECK();
+  return TSVD_OK;
+}
+
+tsvd_status chol_inverse_batched(double *const *g, float *const *t, int l, int nprob,
+                                 cudaStream_t st) {
+  if (nprob == 0) return TSVD_OK;
+  if (l > kLp) return fail(TSVD_ERR_INVALID, "chol: l=%d > %d", l, kLp);
+  size_t smem = (size_t)2 * l * (l + 1) * sizeof(float);
+  static size_t cur = 0;
+  if (smem > cur) {
+    TSVD_TRY(set_smem((const void *)chol_inverse_kernel, smem));
+    cur = smem;
+  }
+  chol_inverse_kernel<<<nprob, CHOL_THREADS, smem, st>>>(g, t, l);
+  TSVD_LAUNCH_CHECK();
+  return TSVD_OK;
+}
+
+tsvd_status apply_right_batched(const float *const *x, const int32_t *rows, int max_rows, int ldx,
+                                const float *const *w, int ldw, int n_in, int n_out,
+                                const float *const *colscale, float *const *y, int ldy,
+                                __half *const *yhi, __half *const *ylo, float split_scale,
+                                int nprob, cudaStream_t st) {
+  if (nprob == 0 || max_rows == 0) return TSVD_OK;
+  if (n_out > 256 || ldy > 256 || n_in > 256)
+    return fail(TSVD_ERR_INVALID, "apply_right: sizes %d %d", n_in, n_out);
+  size_t smem = ((size_t)n_in * n_out + (size_t)APPLY_ROWS * n_in) * sizeof(float);
+  static size_t cur = 0;
+  if (smem > cur) {
+    TSVD_TRY(set_smem((const void *)apply_right_kernel, smem));
+    cur = smem;
+  }
+  ApplyArgs a{x, rows, ldx, w, ldw, n_in, n_out, colscale, y, ldy, yhi, ylo, split_scale};
+  int gx = (int)std::min<int64_t>(ceil_div(max_rows, APPLY_ROWS), 4ll * sm_count());
+  apply_right_kernel<<<dim3(gx, nprob), APPLY_THREADS, smem, st>>>(a);
+  TSVD_LAUNCH_CHECK();
+  return TSVD_OK;
+}
+
+size_t jacobi_work_bytes(int n, int nprob) {
+  int np = n + (n & 1);
+  size_t logb = (size_t)nprob * JAC_MAX_SWEEPS * (np - 1) * (np / 2) * sizeof(float2);
+  return round_up(logb, 256) + round_up((size_t)nprob * sizeof(int32_t), 256) +
+         round_up((size_t)nprob * n * sizeof(int32_t), 256);
+}
+
+tsvd_status jacobi_eig_batched(double *const *g, int n, float *const *lambda, float *const *v,
+                               int nprob, void *work, size_t work_bytes, cudaStream_t st,
+                               int *sweeps_out) {
+  if (nprob == 0) return TSVD_OK;
+  if (n > 256 || n < 2) return fail(TSVD_ERR_INVALID, "jacobi: n=%d", n);
+  if (jacobi_work_bytes(n, nprob) > work_bytes) return fail(TSVD_ERR_INVALID, "jacobi: work");
+  int np = n + (n & 1);
+  char *w = (char *)work;
+  JacobiArgs a;
+  a.g = g;
+  a.n = n;
+  a.lambda = lambda;
+  a.log = (float2 *)w;
+  w += round_up((size_t)nprob * JAC_MAX_SWEEPS * (np - 1) * (np / 2) * sizeof(float2), 256);
+  a.sweeps = (int32_t *)w;
+  w += round_up((size_t)nprob * sizeof(int32_t), 256);
+  a.rank = (int32_t *)w;
+  const int P = np / 2;
+  size_t smem = (size_t)n * (n + 1) / 2 * sizeof(float) + (size_t)P * (P + 1) / 2 * sizeof(uint16_t);
+  static size_t cur = 0;
+  if (smem > cur) {
+    TSVD_TRY(set_smem((const void *)jacobi_kernel, smem));
+    cur = smem;
+  }
+  jacobi_kernel<<<nprob, JAC_THREADS, smem, st>>>(a);
+  TSVD_LAUNCH_CHECK();
+  size_t rsmem = (size_t)REPLAY_ROWS * n * sizeof(float);
+  jacobi_replay_kernel<<<dim3((unsigned)ceil_div(n, REPLAY_ROWS), nprob), 256, rsmem, st>>>(a, v);
+  TSVD_LAUNCH_CHECK();
+  if (sweeps_out) {
+    std::vector<int32_t> h(nprob);
+    TSVD_CUDA(cudaMemcpyAsync(h.data(), a.sweeps, nprob * sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+    TSVD_CUDA(cudaStreamSynchronize(st));
+    int mx = 0;
+    for (int x : h) mx = std::max(mx, x);
+    *sweeps_out = mx;
+  }
+  return TSVD_OK;
+}
+
+}  // namespace tsvd

@@ -1,0 +1,371 @@
+// Batched frPCA over dirty column blocks and batched tree merges.
+//
+// frPCA follows Code/frpca.c:239-326 (k = d, s = l - d oversampling, q
+// passes over A): a Gaussian start (frpca.c:257), products with A and A^T,
+// a normalization after every product, and a final eigSVD of A^T Q
+// (frpca.c:294-312). Normalizations use CholeskyQR2 where the reference uses
+// LU (LUfraction) or eigSVD; all three return a basis of the same column
+// space, which is the only thing the next product consumes. Normalizing
+// A^T Q as well keeps every basis within one condition number of A, so the
+// half-precision split operands stay accurate.
+//
+// The merge follows Code/Tree_u_NC.cpp:723-850: M = [B_1 ... B_h], the
+// truncated SVD of M (dgesvd, ..._mkl.c:1259-1300) keeps U_d S_d; here the
+// Gram M^T M is diagonalized by Jacobi and B_parent = M V_d (= U_d S_d); the
+// root keeps U sqrt(S) = M V_d S^-1/2 (NC) or U = M V_d S^-1 (LP).
+#include <algorithm>
+#include <cmath>
+
+#include "factor.h"
+#include "philox_gauss.h"
+
+namespace tsvd {
+
+namespace {
+
+constexpr float kSplitScale = 4096.f;  // orthonormal bases: |x| <= 1 -> fp16 hi/lo
+
+// Pointer arrays for one batch, staged in pinned memory and uploaded at once.
+struct PtrPack {
+  FrpcaWork &W;
+  size_t used = 0;
+  size_t iused = 0;
+  explicit PtrPack(FrpcaWork &w) : W(w) {}
+  template <typename T>
+  T *const *add(const std::vector<T *> &v) {
+    size_t at = used;
+    for (size_t i = 0; i < v.size(); ++i) W.hptr[used++] = (void *)v[i];
+    return reinterpret_cast<T *const *>(W.dptr + at);
+  }
+  const int32_t *add_int(const std::vector<int32_t> &v) {
+    size_t at = iused;
+    for (size_t i = 0; i < v.size(); ++i) W.hint[iused++] = v[i];
+    return W.dint + at;
+  }
+  tsvd_status upload(cudaStream_t st) {
+    if (used > W.ptr_slots || iused > W.ptr_slots)
+      return fail(TSVD_ERR_INVALID, "pointer pack overflow");
+    TSVD_CUDA(cudaMemcpyAsync(W.dptr, W.hptr, used * sizeof(void *), cudaMemcpyHostToDevice, st));
+    TSVD_CUDA(cudaMemcpyAsync(W.dint, W.hint, iused * sizeof(int32_t), cudaMemcpyHostToDevice, st));
+    return TSVD_OK;
+  }
+};
+
+__global__ void omega_kernel(__half *const *xhi, const int32_t *ncols, const int32_t *const *colmap,
+                             const int32_t *col_base, const int32_t *block, int64_t rows_max, int l,
+                             uint64_t seed) {
+  const int prob = blockIdx.y;
+  const int32_t nc = ncols[prob];
+  __half *X = xhi[prob];
+  const int32_t *cm = colmap[prob];
+  const int32_t base = col_base[prob];
+  const uint32_t stream = (uint32_t)block[prob];
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < (int64_t)nc * kLp;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    int32_t c = (int32_t)(i / kLp);
+    int j = (int)(i % kLp);
+    float val = 0.f;
+    if (j < l) {
+      int32_t col = cm ? cm[c] - base : c;
+      val = tsvd_gauss_entry(seed, stream, (uint32_t)col, (uint32_t)j);
+    }
+    X[i] = __float2half_rn(val);
+  }
+}
+
+__global__ void randq_kernel(float *const *y, __half *const *qhi, __half *const *qlo,
+                             const int32_t *block, int sp, int nsrc, int l, uint64_t seed,
+                             float split) {
+  const int prob = blockIdx.y;
+  const uint32_t stream = 0x80000000u | (uint32_t)block[prob];
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < (int64_t)sp * kLp;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    int32_t s = (int32_t)(i / kLp);
+    int j = (int)(i % kLp);
+    float val = (s < nsrc && j < l) ? tsvd_gauss_entry(seed, stream, (uint32_t)s, (uint32_t)j) : 0.f;
+    y[prob][i] = val;
+    float sv = val * split;
+    __half h = __float2half_rn(sv);
+    qhi[prob][i] = h;
+    qlo[prob][i] = __float2half_rn(sv - __half2float(h));
+  }
+}
+
+// sigma_j = sqrt(max(lambda_j, 0)), zeroed at or below 1e-4 (frpca.c:106-122).
+__global__ void sigma_kernel(const float *const *lambda, int d, float *const *colscale,
+                             float *const *colscale_inv, float *const *sigma_out,
+                             double *sum_sigma2) {
+  const int prob = blockIdx.x;
+  __shared__ double red[32];
+  double acc = 0.0;
+  for (int j = threadIdx.x; j < d; j += blockDim.x) {
+    float lam = lambda[prob][j];
+    float s = sqrtf(fmaxf(lam, 0.f));
+    if (s <= 1e-4f) s = 0.f;
+    colscale[prob][j] = s;
+    if (colscale_inv) colscale_inv[prob][j] = s > 0.f ? 1.f / s : 0.f;
+    if (sigma_out && sigma_out[prob]) sigma_out[prob][j] = s;
+    acc += (double)s * (double)s;
+  }
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+    sum_sigma2[prob] = t;
+  }
+}
+
+// Root/inner scaling of the merged factor: 1, s^-1/2 or s^-1.
+__global__ void merge_scale_kernel(const float *const *lambda, int d, int mode,
+                                   float *const *colscale, float *const *sigma_out) {
+  const int prob = blockIdx.x;
+  for (int j = threadIdx.x; j < d; j += blockDim.x) {
+    float s = sqrtf(fmaxf(lambda[prob][j], 0.f));
+    float f = 1.f;
+    if (mode == 1) f = s > 0.f ? rsqrtf(s) : 0.f;
+    if (mode == 2) f = s > 0.f ? 1.f / s : 0.f;
+    colscale[prob][j] = f;
+    if (sigma_out[prob]) sigma_out[prob][j] = s;
+  }
+}
+
+__global__ void concat_kernel(const float *const *children, int h, int d, int nsrc,
+                              float *const *m) {
+  const int prob = blockIdx.y;
+  const int n = h * d;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < (int64_t)nsrc * n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    int64_t s = i / n;
+    int c = (int)(i % n);
+    m[prob][i] = children[prob * h + c / d][s * d + c % d];
+  }
+}
+
+tsvd_status cholqr2(FrpcaWork &W, float *const *x, const int32_t *rows, int max_rows,
+                    double *const *g, float *const *t, __half *const *hi, __half *const *lo,
+                    int nprob, cudaStream_t st) {
+  for (int pass = 0; pass < 2; ++pass) {
+    TSVD_TRY(gram_batched((const float *const *)x, rows, max_rows, W.l, kLp, g, W.gram_work,
+                          W.gram_bytes, nprob, st));
+    TSVD_TRY(chol_inverse_batched(g, t, W.l, nprob, st));
+    TSVD_TRY(apply_right_batched((const float *const *)x, rows, max_rows, kLp,
+                                 (const float *const *)t, kLp, W.l, W.l, nullptr, x, kLp,
+                                 pass ? hi : nullptr, pass ? lo : nullptr, kSplitScale, nprob,
+                                 st));
+  }
+  return TSVD_OK;
+}
+
+}  // namespace
+
+tsvd_status frpca_work_alloc(FrpcaWork &W, int nmax, int64_t rows_max, int sp, int l, int d) {
+  W.nmax = nmax;
+  W.rows_max = std::max<int64_t>(rows_max, 1);
+  W.sp = sp;
+  W.l = l;
+  W.d = d;
+  size_t rk = (size_t)nmax * W.rows_max * kLp;
+  size_t sk = (size_t)nmax * sp * kLp;
+  TSVD_CUDA(cudaMalloc(&W.xhi, rk * sizeof(__half)));
+  TSVD_CUDA(cudaMalloc(&W.xlo, rk * sizeof(__half)));
+  TSVD_CUDA(cudaMalloc(&W.z, std::max(rk, (size_t)nmax * sp * 256) * sizeof(float)));
+  TSVD_CUDA(cudaMalloc(&W.y, sk * sizeof(float)));
+  TSVD_CUDA(cudaMalloc(&W.qhi, sk * sizeof(__half)));
+  TSVD_CUDA(cudaMalloc(&W.qlo, sk * sizeof(__half)));
+  TSVD_CUDA(cudaMalloc(&W.g, (size_t)nmax * 256 * 256 * sizeof(double)));
+  TSVD_CUDA(cudaMalloc(&W.t, (size_t)nmax * kLp * kLp * sizeof(float)));
+  TSVD_CUDA(cudaMalloc(&W.lambda, (size_t)nmax * 256 * sizeof(float)));
+  TSVD_CUDA(cudaMalloc(&W.v, (size_t)nmax * 256 * 256 * sizeof(float)));
+  TSVD_CUDA(cudaMalloc(&W.colscale, (size_t)nmax * 2 * 256 * sizeof(float)));
+  TSVD_CUDA(cudaMalloc(&W.sums, (size_t)nmax * sizeof(double)));
+  {
+    // every batched Gram uses at most min(nprob * rows/128, 2048) row chunks
+    const int64_t rows = std::max<int64_t>(W.rows_max, sp);
+    const int64_t chunks = std::min<int64_t>((int64_t)nmax * ceil_div(rows, 128), 2048) + nmax;
+    W.gram_bytes = (size_t)chunks * 256 * 256 * sizeof(double);
+  }
+  TSVD_CUDA(cudaMalloc(&W.gram_work, W.gram_bytes));
+  W.jac_bytes = std::max(jacobi_work_bytes(256, nmax), jacobi_work_bytes(l, nmax));
+  TSVD_CUDA(cudaMalloc(&W.jac_work, W.jac_bytes));
+  W.ptr_slots = (size_t)nmax * 64 + 256;
+  TSVD_CUDA(cudaMalloc(&W.dptr, W.ptr_slots * sizeof(void *)));
+  TSVD_CUDA(cudaMallocHost(&W.hptr, W.ptr_slots * sizeof(void *)));
+  TSVD_CUDA(cudaMalloc(&W.dint, W.ptr_slots * sizeof(int32_t)));
+  TSVD_CUDA(cudaMallocHost(&W.hint, W.ptr_slots * sizeof(int32_t)));
+  return TSVD_OK;
+}
+
+void frpca_work_free(FrpcaWork &W) {
+  cudaFree(W.xhi); cudaFree(W.xlo); cudaFree(W.z); cudaFree(W.y); cudaFree(W.qhi);
+  cudaFree(W.qlo); cudaFree(W.g); cudaFree(W.t); cudaFree(W.lambda); cudaFree(W.v);
+  cudaFree(W.colscale); cudaFree(W.sums); cudaFree(W.gram_work); cudaFree(W.jac_work); cudaFree(W.dptr);
+  cudaFreeHost(W.hptr); cudaFree(W.dint); cudaFreeHost(W.hint);
+  W = FrpcaWork();
+}
+
+tsvd_status frpca_batch(FrpcaWork &W, const FrpcaProblem *probs, int nprob, int q, uint64_t seed,
+                        int nsrc, cudaStream_t st, double *sum_sigma2) {
+  if (nprob == 0) return TSVD_OK;
+  if (nprob > W.nmax) return fail(TSVD_ERR_INVALID, "frpca: %d problems > %d", nprob, W.nmax);
+  if (q < 1) return fail(TSVD_ERR_INVALID, "frpca: q=%d", q);
+  TSVD_CUDA(cudaStreamSynchronize(st));  // staging buffers are free again
+  const int sp = W.sp, l = W.l, d = W.d;
+  const int64_t RK = W.rows_max * kLp, SK = (int64_t)sp * kLp;
+  std::vector<const __half *> at(nprob);
+  std::vector<__half *> xhi(nprob), xlo(nprob), qhi(nprob), qlo(nprob);
+  std::vector<float *> z(nprob), y(nprob), t(nprob), lam(nprob), v(nprob), cs(nprob), csi(nprob),
+      bout(nprob), sout(nprob), uout(nprob), vout(nprob);
+  std::vector<double *> g(nprob);
+  std::vector<const int32_t *> cmap(nprob);
+  std::vector<int32_t> ncols(nprob), sprows(nprob, sp), cbase(nprob), blk(nprob), srcrows(nprob, nsrc);
+  int max_nc = 0;
+  bool want_uv = false;
+  for (int i = 0; i < nprob; ++i) {
+    const FrpcaProblem &P = probs[i];
+    at[i] = P.at;
+    ncols[i] = P.ncols;
+    max_nc = std::max(max_nc, P.ncols);
+    if (P.ncols > W.rows_max) return fail(TSVD_ERR_INVALID, "frpca: block too wide");
+    xhi[i] = W.xhi + i * RK;
+    xlo[i] = W.xlo + i * RK;
+    z[i] = W.z + i * RK;
+    y[i] = W.y + i * SK;
+    qhi[i] = W.qhi + i * SK;
+    qlo[i] = W.qlo + i * SK;
+    g[i] = W.g + (int64_t)i * 256 * 256;
+    t[i] = W.t + (int64_t)i * kLp * kLp;
+    lam[i] = W.lambda + i * 256;
+    v[i] = W.v + (int64_t)i * 256 * 256;
+    cs[i] = W.colscale + i * 512;
+    csi[i] = W.colscale + i * 512 + 256;
+    bout[i] = P.b_out;
+    sout[i] = P.sigma_out;
+    uout[i] = P.u_out;
+    vout[i] = P.v_out;
+    want_uv = want_uv || P.u_out || P.v_out;
+    cmap[i] = P.colmap;
+    cbase[i] = P.col_base;
+    blk[i] = P.block;
+  }
+  PtrPack pk(W);
+  auto d_at = pk.add(at);
+  auto d_xhi = pk.add(xhi), d_xlo = pk.add(xlo), d_qhi = pk.add(qhi), d_qlo = pk.add(qlo);
+  auto d_z = pk.add(z), d_y = pk.add(y), d_t = pk.add(t), d_lam = pk.add(lam), d_v = pk.add(v);
+  auto d_cs = pk.add(cs), d_csi = pk.add(csi), d_bout = pk.add(bout), d_sout = pk.add(sout);
+  auto d_uout = pk.add(uout), d_vout = pk.add(vout);
+  auto d_g = pk.add(g);
+  auto d_cmap = pk.add(cmap);
+  const int32_t *d_nc = pk.add_int(ncols), *d_sprows = pk.add_int(sprows),
+                *d_cbase = pk.add_int(cbase), *d_blk = pk.add_int(blk),
+                *d_srcrows = pk.add_int(srcrows);
+  TSVD_TRY(pk.upload(st));
+
+  GemmBatch gb{d_at, d_nc, sp, nprob};
+  const size_t ybytes = (size_t)nprob * SK * sizeof(float);
+  float in_scale = 1.f / kSplitScale;
+  if (q % 2 == 0) {
+    omega_kernel<<<dim3(grid_for((int64_t)max_nc * kLp, 256, 4), nprob), 256, 0, st>>>(
+        d_xhi, d_nc, d_cmap, d_cbase, d_blk, W.rows_max, l, seed);
+    TSVD_LAUNCH_CHECK();
+    TSVD_TRY(gemm_fwd(gb, (const __half *const *)d_xhi, nullptr, d_y, W.y, ybytes, sp, max_nc,
+                      1.f, st));
+    TSVD_TRY(cholqr2(W, d_y, d_sprows, sp, d_g, d_t, d_qhi, d_qlo, nprob, st));
+  } else {
+    const float split = 2048.f;
+    randq_kernel<<<dim3(grid_for(SK, 256, 4), nprob), 256, 0, st>>>(d_y, d_qhi, d_qlo, d_blk, sp,
+                                                                      nsrc, l, seed, split);
+    TSVD_LAUNCH_CHECK();
+    in_scale = 1.f / split;
+  }
+  const int niter = (q - 1) / 2;
+  for (int it = 1; it <= niter; ++it) {
+    TSVD_TRY(gemm_bwd(gb, (const __half *const *)d_qhi, (const __half *const *)d_qlo, d_z, sp,
+                      max_nc, in_scale, st));
+    TSVD_TRY(cholqr2(W, d_z, d_nc, max_nc, d_g, d_t, d_xhi, d_xlo, nprob, st));
+    TSVD_TRY(gemm_fwd(gb, (const __half *const *)d_xhi, (const __half *const *)d_xlo, d_y, W.y,
+                      ybytes, sp, max_nc, 1.f / kSplitScale, st));
+    TSVD_TRY(cholqr2(W, d_y, d_sprows, sp, d_g, d_t, d_qhi, d_qlo, nprob, st));
+    in_scale = 1.f / kSplitScale;
+  }
+  TSVD_TRY(gemm_bwd(gb, (const __half *const *)d_qhi, (const __half *const *)d_qlo, d_z, sp,
+                    max_nc, in_scale, st));
+  // eigSVD of Z = A^T Q (frpca.c:99-136): Gram, eigenpairs, top-d.
+  TSVD_TRY(gram_batched((const float *const *)d_z, d_nc, max_nc, l, kLp, d_g, W.gram_work,
+                        W.gram_bytes, nprob, st));
+  TSVD_TRY(jacobi_eig_batched(d_g, l, d_lam, d_v, nprob, W.jac_work, W.jac_bytes, st,
+                              &W.last_sweeps));
+  double *d_sum2 = W.sums;
+  sigma_kernel<<<nprob, 128, 0, st>>>((const float *const *)d_lam, d, d_cs, d_csi, d_sout, d_sum2);
+  TSVD_LAUNCH_CHECK();
+  // B = Q V_d diag(sigma) (Tree_u_NC.cpp:148-154)
+  bool any_b = false;
+  for (int i = 0; i < nprob; ++i) any_b = any_b || bout[i];
+  if (any_b)
+    TSVD_TRY(apply_right_batched((const float *const *)d_y, d_srcrows, nsrc, kLp,
+                                 (const float *const *)d_v, l, l, d, (const float *const *)d_cs,
+                                 d_bout, d, nullptr, nullptr, 1.f, nprob, st));
+  if (want_uv) {
+    TSVD_TRY(apply_right_batched((const float *const *)d_y, d_srcrows, nsrc, kLp,
+                                 (const float *const *)d_v, l, l, d, nullptr, d_uout, d, nullptr,
+                                 nullptr, 1.f, nprob, st));
+    TSVD_TRY(apply_right_batched((const float *const *)d_z, d_nc, max_nc, kLp,
+                                 (const float *const *)d_v, l, l, d, (const float *const *)d_csi,
+                                 d_vout, d, nullptr, nullptr, 1.f, nprob, st));
+  }
+  std::vector<double> hs(nprob);
+  TSVD_CUDA(cudaMemcpyAsync(hs.data(), d_sum2, sizeof(double) * nprob, cudaMemcpyDeviceToHost, st));
+  TSVD_CUDA(cudaStreamSynchronize(st));
+  if (sum_sigma2)
+    for (int i = 0; i < nprob; ++i) sum_sigma2[i] = hs[i];
+  return TSVD_OK;
+}
+
+tsvd_status merge_batch(FrpcaWork &W, const MergeProblem *probs, int nprob, int h, int nsrc,
+                        int root_mode, cudaStream_t st) {
+  if (nprob == 0) return TSVD_OK;
+  const int d = W.d, n = h * d;
+  if (n > 256) return fail(TSVD_ERR_INVALID, "merge: h*d = %d > 256", n);
+  if (nprob > W.nmax) return fail(TSVD_ERR_INVALID, "merge: too many parents");
+  TSVD_CUDA(cudaStreamSynchronize(st));
+  // per-parent concatenation buffers inside the z area (sized for both uses)
+  const int64_t RK = std::max<int64_t>(W.rows_max * kLp, (int64_t)W.sp * 256);
+  std::vector<const float *> ch((size_t)nprob * h);
+  std::vector<float *> m(nprob), lam(nprob), v(nprob), cs(nprob), out(nprob), sout(nprob);
+  std::vector<double *> g(nprob);
+  std::vector<int32_t> rows(nprob, nsrc);
+  for (int i = 0; i < nprob; ++i) {
+    for (int c = 0; c < h; ++c) ch[(size_t)i * h + c] = probs[i].children[c];
+    m[i] = W.z + i * RK;
+    g[i] = W.g + (int64_t)i * 256 * 256;
+    lam[i] = W.lambda + i * 256;
+    v[i] = W.v + (int64_t)i * 256 * 256;
+    cs[i] = W.colscale + i * 512;
+    out[i] = probs[i].out;
+    sout[i] = probs[i].sigma_out;
+  }
+  PtrPack pk(W);
+  auto d_ch = pk.add(ch);
+  auto d_m = pk.add(m), d_lam = pk.add(lam), d_v = pk.add(v), d_cs = pk.add(cs),
+       d_out = pk.add(out), d_sout = pk.add(sout);
+  auto d_g = pk.add(g);
+  const int32_t *d_rows = pk.add_int(rows);
+  TSVD_TRY(pk.upload(st));
+  concat_kernel<<<dim3(grid_for((int64_t)nsrc * n, 256, 4), nprob), 256, 0, st>>>(d_ch, h, d, nsrc,
+                                                                                 d_m);
+  TSVD_LAUNCH_CHECK();
+  TSVD_TRY(gram_batched((const float *const *)d_m, d_rows, nsrc, n, n, d_g, W.gram_work,
+                        W.gram_bytes, nprob, st));
+  TSVD_TRY(jacobi_eig_batched(d_g, n, d_lam, d_v, nprob, W.jac_work, W.jac_bytes, st,
+                              &W.last_sweeps));
+  merge_scale_kernel<<<nprob, 128, 0, st>>>((const float *const *)d_lam, d, root_mode, d_cs,
+                                            d_sout);
+  TSVD_LAUNCH_CHECK();
+  TSVD_TRY(apply_right_batched((const float *const *)d_m, d_rows, nsrc, n,
+                               (const float *const *)d_v, n, n, d, (const float *const *)d_cs,
+                               d_out, d, nullptr, nullptr, 1.f, nprob, st));
+  return TSVD_OK;
+}
+
+}  // namespace tsvd

@@ -1,0 +1,64 @@
+// Batched frPCA of column blocks and batched tree merges.
+#pragma once
+#include "internal.h"
+
+namespace tsvd {
+
+struct FrpcaWork {
+  int nmax = 0;           // problems (blocks or merge parents) per batch
+  int64_t rows_max = 0;   // max block width (rows of A^T)
+  int sp = 0, l = 0, d = 0;
+  __half *xhi = nullptr, *xlo = nullptr;  // [nmax][rows_max][kLp]
+  float *z = nullptr;                      // [nmax][rows_max][kLp]
+  float *y = nullptr;                      // [nmax][sp][kLp]
+  __half *qhi = nullptr, *qlo = nullptr;  // [nmax][sp][kLp]
+  double *g = nullptr;                     // [nmax][256*256]
+  float *t = nullptr;                      // [nmax][kLp*kLp]
+  float *lambda = nullptr;                 // [nmax][256]
+  float *v = nullptr;                      // [nmax][256*256]
+  float *colscale = nullptr;               // [nmax][512]: scale, inverse scale
+  double *sums = nullptr;                  // [nmax] sum of kept sigma^2
+  double *gram_work = nullptr;
+  size_t gram_bytes = 0;
+  void *jac_work = nullptr;
+  size_t jac_bytes = 0;
+  void **dptr = nullptr;   // device pointer-array area
+  void **hptr = nullptr;   // pinned staging for the pointer arrays
+  size_t ptr_slots = 0;
+  int32_t *dint = nullptr; // device int area (row counts, block ids)
+  int32_t *hint = nullptr;
+  int last_sweeps = 0;
+};
+
+tsvd_status frpca_work_alloc(FrpcaWork &W, int nmax, int64_t rows_max, int sp, int l, int d);
+void frpca_work_free(FrpcaWork &W);
+
+struct FrpcaProblem {
+  int32_t block;            // Gaussian stream id
+  const __half *at;         // A^T [ncols][sp]
+  int32_t ncols;
+  const int32_t *colmap;    // device: compacted column -> global column id
+  int32_t col_base;         // global id of the block's first column
+  float *b_out;             // |S| x d (ld d): U * diag(sigma), or null
+  float *sigma_out;         // d, or null
+  float *u_out;             // sp x d (ld d): U, or null
+  float *v_out;             // ncols x d (ld d): V, or null
+};
+
+// Runs frPCA (k = d, oversampling l - d, q passes) on every problem. sum_sigma2
+// (host, nprob) receives the sum of the kept squared singular values.
+tsvd_status frpca_batch(FrpcaWork &W, const FrpcaProblem *probs, int nprob, int q,
+                        uint64_t seed, int nsrc, cudaStream_t st, double *sum_sigma2);
+
+struct MergeProblem {
+  const float *children[16];  // h child factors, |S| x d (ld d)
+  float *out;                 // |S| x d (ld d)
+  float *sigma_out;           // d
+};
+
+// Truncated SVD of [B_1 ... B_h] for every problem; out = U_d * diag(s_d) * f(s_d)
+// with f = 1 (inner node), s^-1/2 (root, U sqrt(S)) or s^-1 (root, U).
+tsvd_status merge_batch(FrpcaWork &W, const MergeProblem *probs, int nprob, int h, int nsrc,
+                        int root_mode, cudaStream_t st);
+
+}  // namespace tsvd

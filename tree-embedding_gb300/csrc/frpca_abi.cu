@@ -1,0 +1,187 @@
+// frPCA over a caller's CSR matrix: the drop-in for Code/frpca.c:239-326
+// (frPCA(mat_csr*, mat**, mat**, mat**, k, q)) and a status-returning form.
+//
+// The CSR is densified on the device into the same half-precision A^T layout
+// the pipeline uses (non-empty columns only, values scaled by a power of two
+// into half range), then factorized by frpca_batch.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "factor.h"
+#include "internal.h"
+
+using namespace tsvd;
+
+namespace {
+
+uint64_t g_frpca_seed = 20231;
+
+__global__ void scatter_csr_kernel(const int32_t *rows, const int32_t *cidx, const float *vals,
+                                   int64_t nnz, int sp, __half *at) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nnz;
+       i += (int64_t)gridDim.x * blockDim.x)
+    at[(int64_t)cidx[i] * sp + rows[i]] = __float2half_rn(vals[i]);
+}
+
+template <typename T>
+struct DevBuf {
+  T *p = nullptr;
+  ~DevBuf() { cudaFree(p); }
+  tsvd_status alloc(size_t n) {
+    TSVD_CUDA(cudaMalloc(&p, sizeof(T) * std::max<size_t>(n, 1)));
+    return TSVD_OK;
+  }
+};
+
+}  // namespace
+
+extern "C" void tsvd_set_frpca_seed(uint64_t seed) { g_frpca_seed = seed; }
+
+extern "C" tsvd_status tsvd_frpca(int32_t nrows, int32_t ncols, int64_t nnz, const int64_t *row_ptr,
+                                  const int32_t *col_idx, const double *values, int32_t index_base,
+                                  int32_t k, int32_t q, uint64_t seed, double *U, double *S,
+                                  double *V) {
+  if (nrows < 1 || ncols < 1 || nnz < 0 || !row_ptr || (nnz > 0 && (!col_idx || !values)))
+    return fail(TSVD_ERR_INVALID, "frpca: bad matrix arguments");
+  if (k < 1 || k + 5 > kLp || q < 1) return fail(TSVD_ERR_INVALID, "frpca: k=%d q=%d", k, q);
+  if (index_base != 0 && index_base != 1) return fail(TSVD_ERR_INVALID, "frpca: index_base");
+  // non-empty columns and triplets
+  std::vector<int32_t> cmap_inv(ncols, -1);
+  std::vector<int32_t> trow, tcol;
+  std::vector<float> tval;
+  trow.reserve(nnz);
+  tcol.reserve(nnz);
+  tval.reserve(nnz);
+  double vmax = 0.0;
+  for (int32_t i = 0; i < nrows; ++i) {
+    int64_t b = row_ptr[i] - index_base, e = row_ptr[i + 1] - index_base;
+    if (b < 0 || e < b || e > nnz) return fail(TSVD_ERR_INVALID, "frpca: bad row pointers");
+    for (int64_t t = b; t < e; ++t) {
+      int32_t c = col_idx[t] - index_base;
+      if (c < 0 || c >= ncols) return fail(TSVD_ERR_INVALID, "frpca: column out of range");
+      if (values[t] == 0.0) continue;
+      if (!std::isfinite(values[t])) return fail(TSVD_ERR_NUMERIC, "frpca: non-finite value");
+      cmap_inv[c] = 1;
+      trow.push_back(i);
+      tcol.push_back(c);
+      tval.push_back((float)values[t]);
+      vmax = std::max(vmax, std::fabs(values[t]));
+    }
+  }
+  std::vector<int32_t> cmap;
+  for (int32_t c = 0; c < ncols; ++c)
+    if (cmap_inv[c] > 0) {
+      cmap_inv[c] = (int32_t)cmap.size();
+      cmap.push_back(c);
+    }
+  const int32_t nc = (int32_t)cmap.size();
+  for (auto &c : tcol) c = cmap_inv[c];
+  // power-of-two scale so that max |a| lands at 2^14 (exact, undone on sigma)
+  int e2 = 0;
+  if (vmax > 0) std::frexp(vmax, &e2);
+  const double scale = std::ldexp(1.0, 14 - e2);
+  for (auto &v : tval) v = (float)(v * scale);
+  const int sp = (int)round_up(nrows, kRowPad);
+  const int l = k + 5;
+  std::vector<double> sig(k, 0.0);
+  std::vector<float> hu((size_t)sp * k, 0.f), hv((size_t)std::max(nc, 1) * k, 0.f), hs(k, 0.f);
+  if (nc > 0) {
+    DevBuf<__half> at;
+    DevBuf<int32_t> drow, dcol, dcmap;
+    DevBuf<float> dval, du, dv, ds;
+    TSVD_TRY(at.alloc((size_t)nc * sp));
+    TSVD_TRY(drow.alloc(trow.size()));
+    TSVD_TRY(dcol.alloc(tcol.size()));
+    TSVD_TRY(dval.alloc(tval.size()));
+    TSVD_TRY(dcmap.alloc(nc));
+    TSVD_TRY(du.alloc((size_t)sp * k));
+    TSVD_TRY(dv.alloc((size_t)nc * k));
+    TSVD_TRY(ds.alloc(k));
+    cudaStream_t st;
+    TSVD_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    TSVD_CUDA(cudaMemsetAsync(at.p, 0, sizeof(__half) * nc * sp, st));
+    TSVD_CUDA(cudaMemcpyAsync(drow.p, trow.data(), sizeof(int32_t) * trow.size(), cudaMemcpyHostToDevice, st));
+    TSVD_CUDA(cudaMemcpyAsync(dcol.p, tcol.data(), sizeof(int32_t) * tcol.size(), cudaMemcpyHostToDevice, st));
+    TSVD_CUDA(cudaMemcpyAsync(dval.p, tval.data(), sizeof(float) * tval.size(), cudaMemcpyHostToDevice, st));
+    TSVD_CUDA(cudaMemcpyAsync(dcmap.p, cmap.data(), sizeof(int32_t) * nc, cudaMemcpyHostToDevice, st));
+    scatter_csr_kernel<<<grid_for((int64_t)tval.size(), 256), 256, 0, st>>>(
+        drow.p, dcol.p, dval.p, (int64_t)tval.size(), sp, at.p);
+    TSVD_LAUNCH_CHECK();
+    FrpcaWork W;
+    tsvd_status s1 = frpca_work_alloc(W, 1, nc, sp, l, k);
+    if (s1 == TSVD_OK) {
+      FrpcaProblem P;
+      P.block = 0;
+      P.at = at.p;
+      P.ncols = nc;
+      P.colmap = dcmap.p;
+      P.col_base = 0;
+      P.b_out = nullptr;
+      P.sigma_out = ds.p;
+      P.u_out = du.p;
+      P.v_out = dv.p;
+      double ssum = 0;
+      s1 = frpca_batch(W, &P, 1, q, seed, nrows, st, &ssum);
+    }
+    if (s1 == TSVD_OK) {
+      cudaMemcpyAsync(hu.data(), du.p, sizeof(float) * hu.size(), cudaMemcpyDeviceToHost, st);
+      cudaMemcpyAsync(hv.data(), dv.p, sizeof(float) * (size_t)nc * k, cudaMemcpyDeviceToHost, st);
+      cudaMemcpyAsync(hs.data(), ds.p, sizeof(float) * k, cudaMemcpyDeviceToHost, st);
+      cudaError_t e = cudaStreamSynchronize(st);
+      if (e != cudaSuccess) s1 = fail(TSVD_ERR_DEVICE, "frpca: %s", cudaGetErrorString(e));
+    }
+    frpca_work_free(W);
+    cudaStreamDestroy(st);
+    if (s1 != TSVD_OK) return s1;
+  }
+  // outputs: descending sigma; U nrows x k, V ncols x k, column-major
+  for (int j = 0; j < k; ++j) {
+    if (S) S[j] = hs[j] / scale;
+    if (U)
+      for (int32_t i = 0; i < nrows; ++i) U[(size_t)j * nrows + i] = hu[(size_t)i * k + j];
+    if (V) {
+      for (int32_t c = 0; c < ncols; ++c) V[(size_t)j * ncols + c] = 0.0;
+      for (int32_t c = 0; c < nc; ++c) V[(size_t)j * ncols + cmap[c]] = hv[(size_t)c * k + j];
+    }
+  }
+  return TSVD_OK;
+}
+
+extern "C" void frPCA(mat_csr *A, mat **U, mat **S, mat **V, int k, int q) {
+  if (!A || !U || !S || !V || !*U || !*S || !*V) {
+    fail(TSVD_ERR_INVALID, "frPCA: null argument");
+    return;
+  }
+  const int m = A->nrows, n = A->ncols;
+  std::vector<int64_t> rp(m + 1, 0);
+  std::vector<int32_t> ci;
+  std::vector<double> va;
+  ci.reserve(A->nnz > 0 ? A->nnz : 0);
+  va.reserve(A->nnz > 0 ? A->nnz : 0);
+  for (int i = 0; i < m; ++i) {
+    for (int t = A->pointerB[i] - 1; t < A->pointerE[i] - 1; ++t) {
+      ci.push_back(A->cols[t] - 1);
+      va.push_back(A->values[t]);
+    }
+    rp[i + 1] = (int64_t)ci.size();
+  }
+  std::vector<double> u((size_t)m * k), s(k), v((size_t)n * k);
+  tsvd_status st = tsvd_frpca(m, n, (int64_t)ci.size(), rp.data(), ci.data(), va.data(), 0, k, q,
+                              g_frpca_seed, u.data(), s.data(), v.data());
+  mat *Um = *U, *Sm = *S, *Vm = *V;
+  if (st != TSVD_OK) {
+    std::memset(Um->d, 0, sizeof(double) * (size_t)Um->nrows * Um->ncols);
+    std::memset(Sm->d, 0, sizeof(double) * (size_t)Sm->nrows * Sm->ncols);
+    std::memset(Vm->d, 0, sizeof(double) * (size_t)Vm->nrows * Vm->ncols);
+    return;
+  }
+  // ascending order, as dsyevd hands them to the reference (frpca.c:298-310)
+  for (int j = 0; j < k; ++j) {
+    int src = k - 1 - j;
+    Sm->d[j] = s[src];
+    std::memcpy(Um->d + (size_t)j * Um->nrows, u.data() + (size_t)src * m, sizeof(double) * m);
+    std::memcpy(Vm->d + (size_t)j * Vm->nrows, v.data() + (size_t)src * n, sizeof(double) * n);
+  }
+}

@@ -1,0 +1,432 @@
+// Dynamic forward-push PPR for all sources at once, vertex-major state.
+//
+// State: r[v][s], p[v][s] (float, v-major, |S| padded to Sp) so that one warp
+// holds 32 consecutive sources of one vertex: a push of vertex v for a chunk
+// of sources is one 128-byte atomic add per neighbour.
+//
+// Reference: the per-source FIFO push of Code/ppr_computation_store_dynamic.h
+// (nodegree_DenseDynamicForwardPush :1394-1498, nodegree_DenseDirected...
+// :2945-3030, ...Transpose :3356-3437) and its dynamic refresh (:2035-2121,
+// :3811-3898, :4133-4228). The FIFO becomes frontier-synchronous rounds:
+//   push round : every (v, chunk) in the frontier exchanges r[v][s] > rmax to
+//                zero, adds alpha*r to p[v][s] and scatters (1-alpha)*r/deg(v)
+//                to every neighbour, marking (u, chunk) as touched;
+//   collect    : every touched (u, chunk) whose residue exceeds rmax for some
+//                lane and whose degree is non-zero joins the next frontier.
+// Kernel boundaries order the two phases, so no flag/residue race exists.
+// The loop ends when a frontier is empty: every eligible residue <= rmax,
+// the same invariant the FIFO leaves behind.
+#include <algorithm>
+
+#include "internal.h"
+#include "ppr.h"
+
+namespace tsvd {
+
+namespace {
+
+constexpr int kHeavy = 1024;  // neighbours per warp work unit for hub vertices
+constexpr unsigned kFull = 0xffffffffu;
+
+__device__ __forceinline__ void mark_touched(uint32_t *tflag, int32_t u, int32_t c, int32_t C) {
+  int64_t idx = (int64_t)u * C + c;
+  uint32_t bit = 1u << (idx & 31);
+  uint32_t *w = tflag + (idx >> 5);
+  if (!(__ldcg(w) & bit)) atomicOr(w, bit);
+}
+
+struct StatAcc {
+  unsigned long long pushes = 0, upd = 0;
+};
+
+__device__ void flush_stats(StatAcc acc, unsigned long long *gstats) {
+  __shared__ unsigned long long sp[32], su[32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  unsigned long long a = acc.pushes, b = acc.upd;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_down_sync(kFull, a, o);
+    b += __shfl_down_sync(kFull, b, o);
+  }
+  if (lane == 0) { sp[warp] = a; su[warp] = b; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long ta = 0, tb = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) { ta += sp[w]; tb += su[w]; }
+    if (ta) atomicAdd(&gstats[0], ta);
+    if (tb) atomicAdd(&gstats[1], tb);
+  }
+}
+
+// Scatter w (per lane) of vertex v's chunk c to neighbours [j0, j1).
+__device__ __forceinline__ void scatter_range(const PushArgs &a, int32_t v, int32_t c,
+                                              bool act, float w, int32_t j0, int32_t j1) {
+  const int lane = threadIdx.x & 31;
+  const int32_t s = c * 32 + lane;
+  const int32_t *nb = a.nbr + a.off[v];
+  for (int32_t jb = j0; jb < j1; jb += 32) {
+    int32_t jn = min(32, j1 - jb);
+    int32_t mine = lane < jn ? __ldg(nb + jb + lane) : 0;
+    for (int32_t t = 0; t < jn; ++t) {
+      int32_t u = __shfl_sync(kFull, mine, t);
+      if (act) atomicAdd(a.r + (int64_t)u * a.sp + s, w);
+      if (lane == 0) mark_touched(a.tflag, u, c, a.chunks);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(256) push_kernel(PushArgs a) {
+  const int lane = threadIdx.x & 31;
+  const int64_t gw = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const int32_t nitems = *a.front_count;
+  StatAcc acc;
+  for (int64_t i = gw; i < nitems; i += nw) {
+    int2 it = a.front[i];
+    const int32_t v = it.x, c = it.y;
+    const int32_t d = a.deg[v];
+    const int32_t s = c * 32 + lane;
+    float *rp = a.r + (int64_t)v * a.sp + s;
+    float x = __ldcg(rp);
+    bool act = s < a.nsrc && x > a.rmax_f;
+    unsigned mask = __ballot_sync(kFull, act);
+    if (!mask) continue;
+    if (d == 0) {
+      // Isolated source of an undirected graph: the reference assigns
+      // pi = alpha * r and keeps r (ppr:1433-1441); directed dangling
+      // vertices are skipped (ppr:2971-2976).
+      if (a.undirected && act) a.p[(int64_t)v * a.sp + s] = a.alpha_f * x;
+      if (a.undirected && lane == 0 && a.vmark[v] == 0) a.vmark[v] = 1;
+      continue;
+    }
+    if (act) x = atomicExch(rp, 0.0f);
+    const float w = act ? x * (a.one_minus_alpha_f / (float)d) : 0.0f;
+    if (act) {
+      float *pp = a.p + (int64_t)v * a.sp + s;
+      *pp = fmaf(a.alpha_f, x, *pp);
+    }
+    if (lane == 0) {
+      if (a.vmark[v] == 0) a.vmark[v] = 1;
+      acc.pushes += __popc(mask);
+      acc.upd += (unsigned long long)__popc(mask) * (unsigned long long)d;
+    }
+    if (d > kHeavy) {
+      // Hub vertex: park the lane weights and split the neighbour list into
+      // kHeavy-sized units processed by push_heavy_kernel.
+      const int32_t units = (d + kHeavy - 1) / kHeavy;
+      int32_t slot = 0, u0 = 0, ok = 0;
+      if (lane == 0) {
+        slot = atomicAdd(a.heavy_count, 1);
+        u0 = atomicAdd(a.unit_count, units);
+        ok = slot < a.heavy_cap && (int64_t)u0 + units <= a.unit_cap;
+      }
+      ok = __shfl_sync(kFull, ok, 0);
+      slot = __shfl_sync(kFull, slot, 0);
+      u0 = __shfl_sync(kFull, u0, 0);
+      const bool units_reserved = (int64_t)u0 + units <= a.unit_cap;
+      if (ok) {
+        a.heavy_w[(int64_t)slot * 32 + lane] = w;
+        if (lane == 0) {
+          a.heavy_item[slot] = make_int2(v, c);
+          a.heavy_mask[slot] = mask;
+        }
+      }
+      if (units_reserved)
+        for (int32_t k = lane; k < units; k += 32)
+          a.units[u0 + k] = make_int2(ok ? slot : -1, k * kHeavy);
+      if (ok) continue;
+      // buffers full: process this hub inline
+    }
+    scatter_range(a, v, c, act, w, 0, d);
+  }
+  flush_stats(acc, a.stats);
+}
+
+__global__ void __launch_bounds__(256) push_heavy_kernel(PushArgs a) {
+  const int lane = threadIdx.x & 31;
+  const int64_t gw = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const int32_t nunits = min(*a.unit_count, a.unit_cap);
+  for (int64_t i = gw; i < nunits; i += nw) {
+    int2 u = a.units[i];
+    if (u.x < 0) continue;
+    int2 it = a.heavy_item[u.x];
+    unsigned mask = a.heavy_mask[u.x];
+    float w = a.heavy_w[(int64_t)u.x * 32 + lane];
+    bool act = (mask >> lane) & 1u;
+    int32_t d = a.deg[it.x];
+    scatter_range(a, it.x, it.y, act, w, u.y, min(d, u.y + kHeavy));
+  }
+}
+
+// Scan the touched bitset; for each touched (u, chunk) with some residue
+// above rmax and deg(u) > 0, append it to the next frontier. Clears the bits.
+__global__ void __launch_bounds__(256) collect_kernel(CollectArgs a) {
+  __shared__ int2 buf[2048];
+  __shared__ int32_t nbuf, gbase;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t words_per_iter = 64;  // 8 warps x 8 words
+  for (int64_t w0 = (int64_t)blockIdx.x * words_per_iter; w0 < a.nwords;
+       w0 += (int64_t)gridDim.x * words_per_iter) {
+    if (threadIdx.x == 0) nbuf = 0;
+    __syncthreads();
+    for (int k = 0; k < 8; ++k) {
+      int64_t wi = w0 + warp * 8 + k;
+      if (wi >= a.nwords) break;
+      uint32_t bits = __ldcg(a.tflag + wi);
+      if (!bits) continue;
+      if (lane == 0) a.tflag[wi] = 0;
+      while (bits) {
+        int b = __ffs(bits) - 1;
+        bits &= bits - 1;
+        int64_t idx = wi * 32 + b;
+        int32_t u = (int32_t)(idx / a.chunks), c = (int32_t)(idx % a.chunks);
+        if (a.deg[u] == 0) continue;
+        int32_t s = c * 32 + lane;
+        float x = s < a.nsrc ? __ldcg(a.r + (int64_t)u * a.sp + s) : 0.0f;
+        if (__ballot_sync(kFull, x > a.rmax_f)) {
+          if (lane == 0) {
+            int32_t pos = atomicAdd(&nbuf, 1);
+            buf[pos] = make_int2(u, c);
+          }
+        }
+      }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) gbase = nbuf ? atomicAdd(a.next_count, nbuf) : 0;
+    __syncthreads();
+    for (int i = threadIdx.x; i < nbuf; i += blockDim.x) {
+      int64_t dst = (int64_t)gbase + i;
+      if (dst < a.cap) a.next[dst] = buf[i];
+      else atomicExch(a.overflow, 1);
+    }
+    __syncthreads();
+  }
+}
+
+// Dynamic refresh of the new adjacency slots of vertex u, for one chunk of
+// sources: for slot j >= 1 (the reference skips j == 0, ppr:2086-2093),
+//   p_u *= (j+1)/j ; r_u -= p_u/(j+1)/alpha ; r_w += (1-alpha) p_u/(j+1)/alpha.
+__global__ void __launch_bounds__(256) refresh_kernel(RefreshArgs a) {
+  const int lane = threadIdx.x & 31;
+  const int64_t gw = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const int64_t nitems = (int64_t)(*a.nupd) * a.chunks;
+  for (int64_t i = gw; i < nitems; i += nw) {
+    const int32_t u = a.upd[i / a.chunks];
+    const int32_t c = (int32_t)(i % a.chunks);
+    const int32_t s = c * 32 + lane;
+    const bool valid = s < a.nsrc;
+    const int32_t j0 = a.former[u], j1 = a.deg[u];
+    const int32_t *nb = a.nbr + a.off[u];
+    float pf = valid ? a.p[(int64_t)u * a.sp + s] : 0.0f;
+    float rdelta = 0.0f;
+    bool any = false;
+    for (int32_t j = max(j0, 1); j < j1; ++j) {
+      any = true;
+      const int32_t w = __ldg(nb + j);
+      const float jp1 = (float)(j + 1);
+      if (a.intdiv) {
+        pf = pf * (float)((j + 1) / j);
+      } else {
+        pf = pf * (jp1 / (float)j);
+      }
+      const float q = pf / jp1;                 // p_u / (j+1)
+      rdelta -= q * a.inv_alpha_f;
+      if (valid) atomicAdd(a.r + (int64_t)w * a.sp + s, q * a.oma_over_alpha_f);
+      if (lane == 0) mark_touched(a.tflag, w, c, a.chunks);
+    }
+    if (any) {
+      if (valid) {
+        a.p[(int64_t)u * a.sp + s] = pf;
+        atomicAdd(a.r + (int64_t)u * a.sp + s, rdelta);
+      }
+    }
+    // A formerly dangling vertex (j0 == 0) may hold residue it could not
+    // push; in exact mode it is re-examined like any touched vertex. The
+    // reference's dense path skips slot 0 entirely (ppr:2086-2093).
+    if ((any || (!a.intdiv && j0 == 0 && j1 > 0)) && lane == 0)
+      mark_touched(a.tflag, u, c, a.chunks);
+  }
+}
+
+__global__ void list_updated_kernel(const int32_t *__restrict__ deg,
+                                    const int32_t *__restrict__ former, int32_t n,
+                                    int32_t *__restrict__ out, int32_t *__restrict__ count) {
+  const int lane = threadIdx.x & 31;
+  for (int64_t base = (blockIdx.x * (int64_t)blockDim.x) & ~31ll; base < n;
+       base += (int64_t)gridDim.x * blockDim.x) {
+    int64_t v = base + (threadIdx.x & ~31) + lane;
+    bool f = v < n && deg[v] > former[v];
+    unsigned m = __ballot_sync(kFull, f);
+    if (!m) continue;
+    int32_t pos = 0;
+    if (lane == 0) pos = atomicAdd(count, __popc(m));
+    pos = __shfl_sync(kFull, pos, 0);
+    if (f) out[pos + __popc(m & ((1u << lane) - 1u))] = (int32_t)v;
+  }
+}
+
+__global__ void init_sources_kernel(const int32_t *__restrict__ sources, int32_t nsrc,
+                                    float *__restrict__ r, int32_t sp,
+                                    int2 *__restrict__ front, int32_t *__restrict__ count) {
+  for (int32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < nsrc;
+       k += gridDim.x * blockDim.x) {
+    int32_t v = sources[k];
+    r[(int64_t)v * sp + k] = 1.0f;
+    front[k] = make_int2(v, k / 32);
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) *count = nsrc;
+}
+
+float largest_float_not_above(double x) {
+  float f = (float)x;
+  if ((double)f > x) f = nextafterf(f, -INFINITY);
+  return f;
+}
+
+}  // namespace
+
+tsvd_status ppr_alloc(PprState &P, int32_t n, int32_t nsrc, int32_t sp) {
+  P.n = n;
+  P.nsrc = nsrc;
+  P.sp = sp;
+  P.chunks = sp / 32;
+  size_t cells = (size_t)n * sp;
+  TSVD_CUDA(cudaMalloc(&P.r, cells * sizeof(float)));
+  TSVD_CUDA(cudaMalloc(&P.p, cells * sizeof(float)));
+  TSVD_CUDA(cudaMemset(P.r, 0, cells * sizeof(float)));
+  TSVD_CUDA(cudaMemset(P.p, 0, cells * sizeof(float)));
+  P.nwords = ceil_div((int64_t)n * P.chunks, 32);
+  TSVD_CUDA(cudaMalloc(&P.tflag, P.nwords * sizeof(uint32_t)));
+  TSVD_CUDA(cudaMemset(P.tflag, 0, P.nwords * sizeof(uint32_t)));
+  P.cap = (int64_t)n * P.chunks;
+  for (int i = 0; i < 2; ++i) TSVD_CUDA(cudaMalloc(&P.front[i], P.cap * sizeof(int2)));
+  P.heavy_cap = 1 << 20;
+  P.unit_cap = 1 << 22;
+  TSVD_CUDA(cudaMalloc(&P.heavy_w, (size_t)P.heavy_cap * 32 * sizeof(float)));
+  TSVD_CUDA(cudaMalloc(&P.heavy_item, (size_t)P.heavy_cap * sizeof(int2)));
+  TSVD_CUDA(cudaMalloc(&P.heavy_mask, (size_t)P.heavy_cap * sizeof(uint32_t)));
+  TSVD_CUDA(cudaMalloc(&P.units, (size_t)P.unit_cap * sizeof(int2)));
+  TSVD_CUDA(cudaMalloc(&P.upd, (size_t)n * sizeof(int32_t)));
+  TSVD_CUDA(cudaMalloc(&P.counters, 16 * sizeof(int32_t)));
+  TSVD_CUDA(cudaMemset(P.counters, 0, 16 * sizeof(int32_t)));
+  TSVD_CUDA(cudaMalloc(&P.stats, 4 * sizeof(unsigned long long)));
+  TSVD_CUDA(cudaMallocHost(&P.host_counters, 16 * sizeof(int32_t)));
+  return TSVD_OK;
+}
+
+void ppr_free(PprState &P) {
+  cudaFree(P.r); cudaFree(P.p); cudaFree(P.tflag);
+  cudaFree(P.front[0]); cudaFree(P.front[1]);
+  cudaFree(P.heavy_w); cudaFree(P.heavy_item); cudaFree(P.heavy_mask); cudaFree(P.units);
+  cudaFree(P.upd); cudaFree(P.counters); cudaFree(P.stats);
+  cudaFreeHost(P.host_counters);
+  P = PprState();
+}
+
+// counters: [0],[1] frontier counts, [2] heavy count, [3] unit count,
+// [4] overflow flag, [5] number of updated vertices.
+tsvd_status ppr_refresh(PprState &P, const Adjacency &A, const int32_t *sources_dev,
+                        bool from_scratch, const PprParams &prm, uint8_t *vmark,
+                        cudaStream_t st) {
+  (void)vmark;
+  if (from_scratch) {
+    TSVD_CUDA(cudaMemsetAsync(P.r, 0, (size_t)P.n * P.sp * sizeof(float), st));
+    TSVD_CUDA(cudaMemsetAsync(P.p, 0, (size_t)P.n * P.sp * sizeof(float), st));
+    TSVD_CUDA(cudaMemsetAsync(P.tflag, 0, P.nwords * sizeof(uint32_t), st));
+    P.cur = 0;
+    init_sources_kernel<<<grid_for(P.nsrc, 256), 256, 0, st>>>(sources_dev, P.nsrc, P.r, P.sp,
+                                                                  P.front[0], P.counters + 0);
+    TSVD_LAUNCH_CHECK();
+    P.seeded = true;
+    return TSVD_OK;
+  }
+  // vertices with new slots
+  TSVD_CUDA(cudaMemsetAsync(P.counters + 5, 0, sizeof(int32_t), st));
+  list_updated_kernel<<<grid_for(A.n, 256), 256, 0, st>>>(A.deg, A.former, A.n, P.upd,
+                                                            P.counters + 5);
+  TSVD_LAUNCH_CHECK();
+  RefreshArgs ra;
+  ra.upd = P.upd; ra.nupd = P.counters + 5; ra.chunks = P.chunks; ra.nsrc = P.nsrc;
+  ra.sp = P.sp; ra.off = A.off; ra.deg = A.deg; ra.former = A.former; ra.nbr = A.nbr;
+  ra.r = P.r; ra.p = P.p; ra.tflag = P.tflag; ra.intdiv = prm.intdiv;
+  ra.inv_alpha_f = (float)(1.0 / prm.alpha);
+  ra.oma_over_alpha_f = (float)((1.0 - prm.alpha) / prm.alpha);
+  refresh_kernel<<<grid_for((int64_t)A.n * 32, 256, 16), 256, 0, st>>>(ra);
+  TSVD_LAUNCH_CHECK();
+  // seed the frontier from the touched (vertex, chunk) pairs
+  P.cur = 0;
+  TSVD_CUDA(cudaMemsetAsync(P.counters + 0, 0, sizeof(int32_t), st));
+  CollectArgs ca;
+  ca.tflag = P.tflag; ca.nwords = P.nwords; ca.chunks = P.chunks; ca.nsrc = P.nsrc;
+  ca.sp = P.sp; ca.r = P.r; ca.deg = A.deg; ca.rmax_f = largest_float_not_above(prm.rmax);
+  ca.next = P.front[0]; ca.next_count = P.counters + 0; ca.cap = P.cap;
+  ca.overflow = P.counters + 4;
+  collect_kernel<<<grid_for(ceil_div(P.nwords, 64) * 256, 256, 8), 256, 0, st>>>(ca);
+  TSVD_LAUNCH_CHECK();
+  P.seeded = true;
+  return TSVD_OK;
+}
+
+tsvd_status ppr_push(PprState &P, const Adjacency &A, const PprParams &prm, uint8_t *vmark,
+                     cudaStream_t st, PushStats *out) {
+  if (!P.seeded) return fail(TSVD_ERR_STATE, "push before refresh");
+  TSVD_CUDA(cudaMemsetAsync(P.stats, 0, 2 * sizeof(unsigned long long), st));
+  TSVD_CUDA(cudaMemsetAsync(P.counters + 4, 0, sizeof(int32_t), st));
+  const float rmax_f = largest_float_not_above(prm.rmax);
+  PushArgs pa;
+  pa.r = P.r; pa.p = P.p; pa.off = A.off; pa.deg = A.deg; pa.nbr = A.nbr;
+  pa.sp = P.sp; pa.nsrc = P.nsrc; pa.chunks = P.chunks; pa.tflag = P.tflag;
+  pa.alpha_f = (float)prm.alpha; pa.one_minus_alpha_f = (float)(1.0 - prm.alpha);
+  pa.rmax_f = rmax_f; pa.undirected = prm.undirected; pa.vmark = vmark;
+  pa.heavy_w = P.heavy_w; pa.heavy_item = P.heavy_item; pa.heavy_mask = P.heavy_mask;
+  pa.heavy_count = P.counters + 2; pa.heavy_cap = P.heavy_cap;
+  pa.units = P.units; pa.unit_count = P.counters + 3; pa.unit_cap = P.unit_cap;
+  pa.overflow = P.counters + 4; pa.stats = P.stats;
+  CollectArgs ca;
+  ca.tflag = P.tflag; ca.nwords = P.nwords; ca.chunks = P.chunks; ca.nsrc = P.nsrc;
+  ca.sp = P.sp; ca.r = P.r; ca.deg = A.deg; ca.rmax_f = rmax_f; ca.cap = P.cap;
+  ca.overflow = P.counters + 4;
+  const int gpush = grid_for((int64_t)1 << 30, 256, 8);
+  const int gcol = grid_for(ceil_div(P.nwords, 64) * 256, 256, 8);
+  const int check_every = prm.check_every > 0 ? prm.check_every : 4;
+  int64_t rounds = 0;
+  for (;;) {
+    for (int k = 0; k < check_every; ++k) {
+      int cur = P.cur, nxt = 1 - P.cur;
+      pa.front = P.front[cur];
+      pa.front_count = P.counters + cur;
+      TSVD_CUDA(cudaMemsetAsync(P.counters + 2, 0, 2 * sizeof(int32_t), st));
+      TSVD_CUDA(cudaMemsetAsync(P.counters + nxt, 0, sizeof(int32_t), st));
+      push_kernel<<<gpush, 256, 0, st>>>(pa);
+      TSVD_LAUNCH_CHECK();
+      push_heavy_kernel<<<gpush, 256, 0, st>>>(pa);
+      TSVD_LAUNCH_CHECK();
+      ca.next = P.front[nxt];
+      ca.next_count = P.counters + nxt;
+      collect_kernel<<<gcol, 256, 0, st>>>(ca);
+      TSVD_LAUNCH_CHECK();
+      P.cur = nxt;
+      ++rounds;
+    }
+    TSVD_CUDA(cudaMemcpyAsync(P.host_counters, P.counters, 8 * sizeof(int32_t),
+                              cudaMemcpyDeviceToHost, st));
+    TSVD_CUDA(cudaStreamSynchronize(st));
+    if (P.host_counters[4]) return fail(TSVD_ERR_STATE, "push: frontier buffer overflow");
+    if (P.host_counters[P.cur] == 0) break;
+    if (rounds >= prm.max_rounds)
+      return fail(TSVD_ERR_TIMEOUT, "push: %lld rounds without convergence", (long long)rounds);
+  }
+  unsigned long long hs[2];
+  TSVD_CUDA(cudaMemcpy(hs, P.stats, sizeof hs, cudaMemcpyDeviceToHost));
+  if (out) {
+    out->rounds = rounds;
+    out->pushes = (int64_t)hs[0];
+    out->edge_updates = (int64_t)hs[1];
+  }
+  P.seeded = false;
+  return TSVD_OK;
+}
+
+}  // namespace tsvd

@@ -1,0 +1,763 @@
+// Session: the per-snapshot refresh of Code/Tree_{u,d}_{NC,LP}.cpp
+// (Tree_u_NC.cpp:507-866, Tree_d_NC.cpp:566-1140) on one GPU, plus the
+// C-ABI entry points declared in include/tsvd.h.
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "blocks.h"
+#include "factor.h"
+#include "internal.h"
+#include "ppr.h"
+
+// ------------------------------------------------------------------ errors
+namespace tsvd {
+static std::atomic<long long> g_launches{0};
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+static thread_local char g_err[1024] = "";
+tsvd_status fail(tsvd_status s, const char *fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof g_err, fmt, ap);
+  va_end(ap);
+  return s;
+}
+}  // namespace tsvd
+
+extern "C" const char *tsvd_last_error(void) { return tsvd::g_err; }
+extern "C" const char *tsvd_status_string(tsvd_status s) {
+  switch (s) {
+    case TSVD_OK: return "ok";
+    case TSVD_ERR_INVALID: return "invalid argument";
+    case TSVD_ERR_OOM: return "out of memory";
+    case TSVD_ERR_DEVICE: return "device error";
+    case TSVD_ERR_TIMEOUT: return "timeout";
+    case TSVD_ERR_STATE: return "bad state";
+    case TSVD_ERR_IO: return "i/o error";
+    case TSVD_ERR_NUMERIC: return "numeric error";
+  }
+  return "unknown";
+}
+extern "C" const char *tsvd_version(void) { return "tsvd-gb300 0.1 sm_103a"; }
+extern "C" int64_t tsvd_launch_count(void) { return tsvd::g_launches.load(); }
+
+using namespace tsvd;
+
+// ------------------------------------------------------------------ session
+struct tsvd_session {
+  tsvd_config cfg{};
+  std::vector<int32_t> sources;
+  int n = 0, S = 0, sp = 0, nparts = 0, col_dim = 0, h = 0, d = 0, l = 0, q = 0;
+  int directed = 0;
+  cudaStream_t st = nullptr;
+  Adjacency adj[2];
+  InsertScratch ins;
+  PprState ppr[2];
+  uint8_t *vmark = nullptr;
+  int32_t *sources_dev = nullptr;
+  int32_t *colmap = nullptr, *ncols_dev = nullptr, *ncols_old_dev = nullptr;
+  std::vector<int32_t> ncols_h, ncols_old_h;
+  __half *atbuf[2] = {nullptr, nullptr};
+  std::vector<int> atcur;
+  __half **at_ptrs_dev = nullptr;  // [2][nparts]: old, new
+  double *norm2_dev = nullptr, *diff2_dev = nullptr;
+  unsigned long long *nnz_dev = nullptr, *stored_dev = nullptr;
+  std::vector<double> norm2_h, diff2_h, norm2_acc, resid;
+  std::vector<int64_t> nnz_h, stored_h;
+  std::vector<uint8_t> dirty_h;
+  std::vector<int> factor_now;
+  int total_nodes = 0, leaf_start = 0;
+  float *tree_b = nullptr, *tree_sigma = nullptr;
+  float *embedding = nullptr;
+  bool has_embedding = false;
+  FrpcaWork fw;
+  int32_t *edges_dev = nullptr;
+  int64_t edges_cap = 0;
+  uint32_t *keys = nullptr, *vals = nullptr;
+  int64_t kv_cap = 0;
+  int32_t *bad_dev = nullptr;
+  int iter = 0;
+  tsvd_step_stats last{};
+  cudaEvent_t ev[8]{};
+
+  size_t node_elems() const { return (size_t)S * d; }
+  float *node_b(int i) { return tree_b + (size_t)i * node_elems(); }
+  float *node_sigma(int i) { return tree_sigma + (size_t)i * d; }
+  __half *at_block(int which, int b) { return atbuf[which] + (size_t)b * col_dim * sp; }
+};
+
+namespace {
+
+__global__ void expand_edges_kernel(const int32_t *__restrict__ e, int64_t m, int32_t n,
+                                    int directed, uint32_t *__restrict__ k0,
+                                    uint32_t *__restrict__ v0, uint32_t *__restrict__ k1,
+                                    uint32_t *__restrict__ v1, int32_t *__restrict__ bad) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    int32_t a = e[2 * i], b = e[2 * i + 1];
+    if (a < 0 || b < 0 || a >= n || b >= n) {
+      *bad = 1;
+      a = 0;
+      b = 0;
+    }
+    if (directed) {
+      k0[i] = (uint32_t)a; v0[i] = (uint32_t)b;   // out-list of a
+      k1[i] = (uint32_t)b; v1[i] = (uint32_t)a;   // in-list of b
+    } else {
+      k0[2 * i] = (uint32_t)a; v0[2 * i] = (uint32_t)b;
+      k0[2 * i + 1] = (uint32_t)b; v0[2 * i + 1] = (uint32_t)a;
+    }
+  }
+}
+
+__global__ void f32_to_f64_kernel(const float *in, double *out, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = (double)in[i];
+}
+
+bool is_power_of(int n, int h) {
+  if (h < 2) return false;
+  while (n > 1 && n % h == 0) n /= h;
+  return n == 1;
+}
+
+float ms_between(cudaEvent_t a, cudaEvent_t b) {
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, a, b);
+  return ms;
+}
+
+}  // namespace
+
+extern "C" void tsvd_config_default(tsvd_config *c) {
+  std::memset(c, 0, sizeof *c);
+  c->alpha = 0.5;  // run.sh
+  c->rmax = 1e-7;
+  c->n_parts = 64;
+  c->hierarchy_n = 2;
+  c->rank_d = 128;
+  c->oversample = 5;
+  c->passes_q = 12;
+  c->dynamic_ppr_start_iter = 100;
+  c->lazy_update_start_iter = 100;
+  c->delta = 0.3;
+  c->transform = TSVD_TRANSFORM_LOG10_NC;
+  c->dirty_rule = TSVD_DIRTY_REFERENCE;
+  c->dirty_frac = 0.01;
+  c->root_scaling = TSVD_ROOT_SQRT_SIGMA;
+  c->refresh_mode = TSVD_REFRESH_EXACT;
+  c->seed = 20231;
+  c->device = 0;
+  c->max_push_rounds = 0;
+}
+
+static tsvd_status session_alloc(tsvd_session *s) {
+  const tsvd_config &c = s->cfg;
+  TSVD_CUDA(cudaSetDevice(c.device));
+  TSVD_CUDA(cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking));
+  for (auto &e : s->ev) TSVD_CUDA(cudaEventCreate(&e));
+  const int ndir = s->directed ? 2 : 1;
+  for (int dd = 0; dd < ndir; ++dd) {
+    Adjacency &A = s->adj[dd];
+    A.n = s->n;
+    TSVD_CUDA(cudaMalloc(&A.off, sizeof(int64_t) * (s->n + 1)));
+    TSVD_CUDA(cudaMemset(A.off, 0, sizeof(int64_t) * (s->n + 1)));
+    TSVD_CUDA(cudaMalloc(&A.deg, sizeof(int32_t) * s->n));
+    TSVD_CUDA(cudaMemset(A.deg, 0, sizeof(int32_t) * s->n));
+    TSVD_CUDA(cudaMalloc(&A.former, sizeof(int32_t) * s->n));
+    TSVD_CUDA(cudaMemset(A.former, 0, sizeof(int32_t) * s->n));
+    TSVD_TRY(ppr_alloc(s->ppr[dd], s->n, s->S, s->sp));
+  }
+  TSVD_CUDA(cudaMalloc(&s->vmark, s->n));
+  TSVD_CUDA(cudaMemset(s->vmark, 0, s->n));
+  TSVD_CUDA(cudaMalloc(&s->sources_dev, sizeof(int32_t) * s->S));
+  TSVD_CUDA(cudaMemcpy(s->sources_dev, s->sources.data(), sizeof(int32_t) * s->S,
+                       cudaMemcpyHostToDevice));
+  TSVD_CUDA(cudaMalloc(&s->colmap, sizeof(int32_t) * s->n));
+  TSVD_CUDA(cudaMalloc(&s->ncols_dev, sizeof(int32_t) * s->nparts));
+  TSVD_CUDA(cudaMalloc(&s->ncols_old_dev, sizeof(int32_t) * s->nparts));
+  TSVD_CUDA(cudaMemset(s->ncols_dev, 0, sizeof(int32_t) * s->nparts));
+  TSVD_CUDA(cudaMemset(s->ncols_old_dev, 0, sizeof(int32_t) * s->nparts));
+  s->ncols_h.assign(s->nparts, 0);
+  s->ncols_old_h.assign(s->nparts, 0);
+  const size_t at_elems = (size_t)s->n * s->sp;
+  // the last block is wider: col_dim*(nparts-1) + last = n, fits in n*sp
+  for (int w = 0; w < 2; ++w) {
+    TSVD_CUDA(cudaMalloc(&s->atbuf[w], at_elems * sizeof(__half)));
+  }
+  s->atcur.assign(s->nparts, 0);
+  TSVD_CUDA(cudaMalloc(&s->at_ptrs_dev, sizeof(__half *) * 2 * s->nparts));
+  TSVD_CUDA(cudaMalloc(&s->norm2_dev, sizeof(double) * s->nparts));
+  TSVD_CUDA(cudaMalloc(&s->diff2_dev, sizeof(double) * s->nparts));
+  TSVD_CUDA(cudaMalloc(&s->nnz_dev, sizeof(unsigned long long) * s->nparts));
+  TSVD_CUDA(cudaMalloc(&s->stored_dev, sizeof(unsigned long long) * s->nparts));
+  s->norm2_h.assign(s->nparts, 0);
+  s->diff2_h.assign(s->nparts, 0);
+  s->norm2_acc.assign(s->nparts, 0);
+  s->resid.assign(s->nparts, 0);
+  s->nnz_h.assign(s->nparts, 0);
+  s->stored_h.assign(s->nparts, 0);
+  s->dirty_h.assign(s->nparts, 0);
+  // tree: complete h-ary tree with nparts leaves (ppr:225-245)
+  int levels = 1;
+  for (int t = s->nparts; t > 1; t /= s->h) ++levels;
+  int64_t total = 0, pw = 1;
+  for (int i = 0; i < levels; ++i, pw *= s->h) total += pw;
+  s->total_nodes = (int)total;
+  s->leaf_start = s->total_nodes - s->nparts;
+  TSVD_CUDA(cudaMalloc(&s->tree_b, sizeof(float) * s->node_elems() * s->total_nodes));
+  TSVD_CUDA(cudaMemset(s->tree_b, 0, sizeof(float) * s->node_elems() * s->total_nodes));
+  TSVD_CUDA(cudaMalloc(&s->tree_sigma, sizeof(float) * s->d * s->total_nodes));
+  TSVD_CUDA(cudaMemset(s->tree_sigma, 0, sizeof(float) * s->d * s->total_nodes));
+  TSVD_CUDA(cudaMalloc(&s->embedding, sizeof(float) * s->node_elems()));
+  TSVD_CUDA(cudaMemset(s->embedding, 0, sizeof(float) * s->node_elems()));
+  TSVD_CUDA(cudaMalloc(&s->bad_dev, sizeof(int32_t)));
+  const int last_w = s->n - (s->nparts - 1) * s->col_dim;
+  TSVD_TRY(frpca_work_alloc(s->fw, s->nparts, std::max(last_w, s->col_dim), s->sp, s->l, s->d));
+  return TSVD_OK;
+}
+
+static void session_release(tsvd_session *s) {
+  if (!s) return;
+  cudaSetDevice(s->cfg.device);
+  if (s->st) cudaStreamSynchronize(s->st);
+  for (int dd = 0; dd < 2; ++dd) {
+    adjacency_free(s->adj[dd]);
+    if (s->ppr[dd].r) ppr_free(s->ppr[dd]);
+  }
+  cudaFree(s->ins.buf);
+  cudaFree(s->vmark); cudaFree(s->sources_dev); cudaFree(s->colmap);
+  cudaFree(s->ncols_dev); cudaFree(s->ncols_old_dev);
+  cudaFree(s->atbuf[0]); cudaFree(s->atbuf[1]); cudaFree(s->at_ptrs_dev);
+  cudaFree(s->norm2_dev); cudaFree(s->diff2_dev); cudaFree(s->nnz_dev); cudaFree(s->stored_dev);
+  cudaFree(s->tree_b); cudaFree(s->tree_sigma); cudaFree(s->embedding);
+  cudaFree(s->edges_dev); cudaFree(s->keys); cudaFree(s->vals); cudaFree(s->bad_dev);
+  frpca_work_free(s->fw);
+  for (auto &e : s->ev)
+    if (e) cudaEventDestroy(e);
+  if (s->st) cudaStreamDestroy(s->st);
+}
+
+extern "C" tsvd_status tsvd_session_create(const tsvd_config *cfg, tsvd_session **out) {
+  if (!cfg || !out) return fail(TSVD_ERR_INVALID, "null argument");
+  *out = nullptr;
+  const tsvd_config &c = *cfg;
+  if (c.n_vertices < 2 || c.n_sources < 1 || !c.sources)
+    return fail(TSVD_ERR_INVALID, "need n_vertices >= 2 and at least one source");
+  if (!(c.alpha > 0 && c.alpha < 1) || !(c.rmax > 0))
+    return fail(TSVD_ERR_INVALID, "alpha must be in (0,1) and rmax > 0");
+  if (c.n_parts < 1 || c.n_parts > c.n_vertices)
+    return fail(TSVD_ERR_INVALID, "n_parts=%d", c.n_parts);
+  if (c.hierarchy_n < 2 || !is_power_of(c.n_parts, c.hierarchy_n) || c.n_parts < c.hierarchy_n)
+    return fail(TSVD_ERR_INVALID,
+                "n_parts (%d) must be a power of hierarchy_n (%d), at least one merge",
+                c.n_parts, c.hierarchy_n);
+  if (c.rank_d < 1 || c.oversample < 0 || c.rank_d + c.oversample > kLp)
+    return fail(TSVD_ERR_INVALID, "rank_d + oversample must be <= %d", kLp);
+  if ((int64_t)c.hierarchy_n * c.rank_d > 256)
+    return fail(TSVD_ERR_INVALID, "hierarchy_n * rank_d must be <= 256 (merge width)");
+  if (c.passes_q < 1) return fail(TSVD_ERR_INVALID, "passes_q must be >= 1");
+  if (c.transform < 0 || c.transform > 2 || c.dirty_rule < 0 || c.dirty_rule > 2)
+    return fail(TSVD_ERR_INVALID, "bad transform or dirty rule");
+  std::vector<int32_t> src(c.sources, c.sources + c.n_sources);
+  {
+    std::vector<int32_t> chk = src;
+    std::sort(chk.begin(), chk.end());
+    for (size_t i = 0; i < chk.size(); ++i) {
+      if (chk[i] < 0 || chk[i] >= c.n_vertices)
+        return fail(TSVD_ERR_INVALID, "source %d out of range", chk[i]);
+      if (i && chk[i] == chk[i - 1]) return fail(TSVD_ERR_INVALID, "duplicate source %d", chk[i]);
+    }
+  }
+  tsvd_session *s = new tsvd_session;
+  s->cfg = c;
+  s->cfg.sources = nullptr;
+  s->sources = src;
+  s->n = c.n_vertices;
+  s->S = c.n_sources;
+  s->sp = (int)round_up(s->S, kRowPad);
+  s->nparts = c.n_parts;
+  s->col_dim = c.n_vertices / c.n_parts;
+  s->h = c.hierarchy_n;
+  s->d = c.rank_d;
+  s->l = c.rank_d + c.oversample;
+  s->q = c.passes_q;
+  s->directed = c.directed ? 1 : 0;
+  tsvd_status st = session_alloc(s);
+  if (st != TSVD_OK) {
+    std::string msg = tsvd_last_error();
+    session_release(s);
+    delete s;
+    return fail(st, "%s", msg.c_str());
+  }
+  *out = s;
+  return TSVD_OK;
+}
+
+extern "C" tsvd_status tsvd_session_destroy(tsvd_session *s) {
+  if (!s) return TSVD_OK;
+  session_release(s);
+  delete s;
+  return TSVD_OK;
+}
+
+// ------------------------------------------------------------------ stages
+static PprParams ppr_params(const tsvd_session *s) {
+  PprParams p;
+  p.alpha = s->cfg.alpha;
+  p.rmax = s->cfg.rmax;
+  p.intdiv = s->cfg.refresh_mode == TSVD_REFRESH_INTDIV;
+  p.undirected = !s->directed;
+  p.max_rounds = s->cfg.max_push_rounds > 0 ? s->cfg.max_push_rounds : 1000000;
+  return p;
+}
+
+static tsvd_status insert_device(tsvd_session *s, const int32_t *edges_dev, int64_t m) {
+  const int64_t entries = s->directed ? m : 2 * m;
+  if (entries > s->kv_cap) {
+    cudaFree(s->keys);
+    cudaFree(s->vals);
+    s->keys = s->vals = nullptr;
+    s->kv_cap = 0;
+    int64_t cap = std::max<int64_t>(entries, 1024);
+    // directed keeps both lists: [0, m) out, [cap, cap+m) in
+    TSVD_CUDA(cudaMalloc(&s->keys, sizeof(uint32_t) * cap * 2));
+    TSVD_CUDA(cudaMalloc(&s->vals, sizeof(uint32_t) * cap * 2));
+    s->kv_cap = cap;
+  }
+  TSVD_CUDA(cudaMemsetAsync(s->bad_dev, 0, sizeof(int32_t), s->st));
+  if (m > 0) {
+    expand_edges_kernel<<<grid_for(m, 256), 256, 0, s->st>>>(
+        edges_dev, m, s->n, s->directed, s->keys, s->vals, s->keys + s->kv_cap,
+        s->vals + s->kv_cap, s->bad_dev);
+    TSVD_LAUNCH_CHECK();
+  }
+  int32_t bad = 0;
+  TSVD_CUDA(cudaMemcpyAsync(&bad, s->bad_dev, sizeof(int32_t), cudaMemcpyDeviceToHost, s->st));
+  TSVD_CUDA(cudaStreamSynchronize(s->st));
+  if (bad) return fail(TSVD_ERR_INVALID, "edge endpoint outside [0, %d)", s->n);
+  TSVD_TRY(adjacency_append(s->adj[0], s->keys, s->vals, entries, s->ins, s->st));
+  if (s->directed)
+    TSVD_TRY(adjacency_append(s->adj[1], s->keys + s->kv_cap, s->vals + s->kv_cap, m, s->ins,
+                              s->st));
+  s->last.edges_inserted = m;
+  return TSVD_OK;
+}
+
+static tsvd_status stage_materialize(tsvd_session *s, int iter) {
+  const int P = s->nparts;
+  TSVD_TRY(colmap_update(s->vmark, s->colmap, s->ncols_dev, s->n, s->col_dim, P, s->st));
+  TSVD_CUDA(cudaMemcpyAsync(s->ncols_h.data(), s->ncols_dev, sizeof(int32_t) * P,
+                            cudaMemcpyDeviceToHost, s->st));
+  TSVD_CUDA(cudaStreamSynchronize(s->st));
+  std::vector<__half *> ptrs(2 * P);
+  for (int b = 0; b < P; ++b) {
+    ptrs[b] = s->at_block(s->atcur[b], b);
+    ptrs[P + b] = s->at_block(1 - s->atcur[b], b);
+  }
+  TSVD_CUDA(cudaMemcpyAsync(s->at_ptrs_dev, ptrs.data(), sizeof(__half *) * 2 * P,
+                            cudaMemcpyHostToDevice, s->st));
+  MaterializeArgs a;
+  a.p1 = s->ppr[0].p;
+  a.p2 = s->directed ? s->ppr[1].p : nullptr;
+  a.colmap = s->colmap;
+  a.ncols = s->ncols_dev;
+  a.ncols_old = s->ncols_old_dev;
+  a.at_old = s->at_ptrs_dev;
+  a.at_new = s->at_ptrs_dev + P;
+  a.sp = s->sp;
+  a.nsrc = s->S;
+  a.col_dim = s->col_dim;
+  a.transform = s->cfg.transform;
+  a.rmin_f = (float)s->cfg.rmax;
+  a.inv_rmin_f = (float)(1.0 / s->cfg.rmax);
+  a.n_f = (float)s->n;
+  a.norm2 = s->norm2_dev;
+  a.diff2 = s->diff2_dev;
+  a.nnz = s->nnz_dev;
+  a.stored = s->stored_dev;
+  int32_t max_nc = 0;
+  for (int32_t x : s->ncols_h) max_nc = std::max(max_nc, x);
+  TSVD_TRY(materialize_blocks(a, P, max_nc, s->st));
+  std::vector<unsigned long long> nn(P), ss(P);
+  TSVD_CUDA(cudaMemcpyAsync(s->norm2_h.data(), s->norm2_dev, sizeof(double) * P, cudaMemcpyDeviceToHost, s->st));
+  TSVD_CUDA(cudaMemcpyAsync(s->diff2_h.data(), s->diff2_dev, sizeof(double) * P, cudaMemcpyDeviceToHost, s->st));
+  TSVD_CUDA(cudaMemcpyAsync(nn.data(), s->nnz_dev, sizeof(unsigned long long) * P, cudaMemcpyDeviceToHost, s->st));
+  TSVD_CUDA(cudaMemcpyAsync(ss.data(), s->stored_dev, sizeof(unsigned long long) * P, cudaMemcpyDeviceToHost, s->st));
+  TSVD_CUDA(cudaStreamSynchronize(s->st));
+  // Lazy-update decision (ppr:2700-2729) or unconditional refresh (Tree_u_NC.cpp:642-668).
+  const bool with_norm = iter >= s->cfg.lazy_update_start_iter;
+  s->factor_now.clear();
+  int ndirty = 0;
+  for (int b = 0; b < P; ++b) {
+    s->nnz_h[b] = (int64_t)nn[b];
+    s->stored_h[b] = (int64_t)ss[b];
+    bool dirty = true;
+    if (with_norm) {
+      const double a_norm = std::sqrt(std::max(s->norm2_h[b], 0.0));
+      const double ei = std::sqrt(std::max(s->diff2_h[b], 0.0));
+      switch (s->cfg.dirty_rule) {
+        case TSVD_DIRTY_REFERENCE:
+          dirty = !(s->resid[b] + ei < s->cfg.delta * std::sqrt(2.0) * a_norm);
+          break;
+        case TSVD_DIRTY_FROBENIUS:
+          dirty = ei > s->cfg.dirty_frac * a_norm;
+          break;
+        default:
+          dirty = true;
+      }
+    }
+    s->dirty_h[b] = dirty ? 1 : 0;
+    if (!dirty) continue;
+    ++ndirty;
+    // accept: the new matrix becomes the reference for the next comparison
+    s->atcur[b] = 1 - s->atcur[b];
+    s->ncols_old_h[b] = s->ncols_h[b];
+    s->norm2_acc[b] = s->norm2_h[b];
+    if (ss[b] > 0) s->factor_now.push_back(b);  // nonZeros() == 0 blocks are skipped
+  }
+  TSVD_CUDA(cudaMemcpyAsync(s->ncols_old_dev, s->ncols_old_h.data(), sizeof(int32_t) * P,
+                            cudaMemcpyHostToDevice, s->st));
+  TSVD_CUDA(cudaStreamSynchronize(s->st));
+  s->last.dirty_blocks = ndirty;
+  return TSVD_OK;
+}
+
+static tsvd_status stage_factorize(tsvd_session *s, int iter) {
+  const int nf = (int)s->factor_now.size();
+  s->last.factorized_blocks = nf;
+  if (nf == 0) return TSVD_OK;
+  std::vector<FrpcaProblem> probs(nf);
+  for (int i = 0; i < nf; ++i) {
+    int b = s->factor_now[i];
+    FrpcaProblem &P = probs[i];
+    P.block = b;
+    P.at = s->at_block(s->atcur[b], b);
+    P.ncols = s->ncols_h[b];
+    P.colmap = s->colmap + (size_t)b * s->col_dim;
+    P.col_base = b * s->col_dim;
+    P.b_out = s->node_b(s->leaf_start + b);
+    P.sigma_out = s->node_sigma(s->leaf_start + b);
+    P.u_out = nullptr;
+    P.v_out = nullptr;
+  }
+  std::vector<double> ssum(nf);
+  TSVD_TRY(frpca_batch(s->fw, probs.data(), nf, s->q, s->cfg.seed, s->S, s->st, ssum.data()));
+  // Residual ||A - U S V^T||_F = sqrt(||A||^2 - sum sigma^2) for an orthonormal
+  // basis (the reference forms the dense product, Tree_u_NC.cpp:158-204).
+  if (iter >= s->cfg.lazy_update_start_iter - 1)
+    for (int i = 0; i < nf; ++i) {
+      int b = s->factor_now[i];
+      s->resid[b] = std::sqrt(std::max(s->norm2_acc[b] - ssum[i], 0.0));
+    }
+  return TSVD_OK;
+}
+
+static tsvd_status stage_merge(tsvd_session *s) {
+  s->last.merged_nodes = 0;
+  if (s->factor_now.empty()) return TSVD_OK;
+  const int h = s->h;
+  std::vector<int> level;
+  for (int b : s->factor_now) {
+    int par = (s->leaf_start + b - 1) / h;
+    if (std::find(level.begin(), level.end(), par) == level.end()) level.push_back(par);
+  }
+  std::sort(level.begin(), level.end());
+  while (!level.empty()) {
+    const bool root = level.size() == 1 && level[0] == 0;
+    std::vector<MergeProblem> probs(level.size());
+    for (size_t i = 0; i < level.size(); ++i) {
+      int p = level[i];
+      for (int c = 0; c < h; ++c) probs[i].children[c] = s->node_b(p * h + 1 + c);
+      probs[i].out = root ? s->embedding : s->node_b(p);
+      probs[i].sigma_out = s->node_sigma(p);
+    }
+    int mode = 0;
+    if (root) mode = s->cfg.root_scaling == TSVD_ROOT_U ? 2 : 1;
+    TSVD_TRY(merge_batch(s->fw, probs.data(), (int)probs.size(), h, s->S, mode, s->st));
+    s->last.merged_nodes += (int)probs.size();
+    if (root) {
+      TSVD_CUDA(cudaMemcpyAsync(s->node_b(0), s->embedding, sizeof(float) * s->node_elems(),
+                                cudaMemcpyDeviceToDevice, s->st));
+      s->has_embedding = true;
+      break;
+    }
+    std::vector<int> next;
+    for (int p : level) {
+      int par = (p - 1) / h;
+      if (std::find(next.begin(), next.end(), par) == next.end()) next.push_back(par);
+    }
+    std::sort(next.begin(), next.end());
+    level.swap(next);
+  }
+  TSVD_CUDA(cudaStreamSynchronize(s->st));
+  return TSVD_OK;
+}
+
+static tsvd_status stage_ppr(tsvd_session *s, int iter, int dir) {
+  const bool scratch = iter < s->cfg.dynamic_ppr_start_iter;
+  PprParams prm = ppr_params(s);
+  TSVD_TRY(ppr_refresh(s->ppr[dir], s->adj[dir], s->sources_dev, scratch, prm, s->vmark, s->st));
+  PushStats ps;
+  TSVD_TRY(ppr_push(s->ppr[dir], s->adj[dir], prm, s->vmark, s->st, &ps));
+  s->last.push_rounds += ps.rounds;
+  s->last.pushes += ps.pushes;
+  s->last.push_edge_updates += ps.edge_updates;
+  return TSVD_OK;
+}
+
+static tsvd_status step_device(tsvd_session *s, const int32_t *edges_dev, int64_t m) {
+  TSVD_CUDA(cudaSetDevice(s->cfg.device));
+  const int iter = ++s->iter;
+  std::memset(&s->last, 0, sizeof s->last);
+  s->last.iter = iter;
+  cudaEvent_t *ev = s->ev;
+  TSVD_CUDA(cudaEventRecord(ev[0], s->st));
+  TSVD_TRY(insert_device(s, edges_dev, m));
+  TSVD_CUDA(cudaEventRecord(ev[1], s->st));
+  // Tree_u_NC.cpp:516 — snapshots before lazy_update_start_iter-1 only grow the graph
+  if (s->cfg.lazy_update_start_iter != 100 && iter < s->cfg.lazy_update_start_iter - 1) {
+    s->last.skipped = 1;
+    TSVD_CUDA(cudaStreamSynchronize(s->st));
+    s->last.ms_insert = s->last.ms_total = ms_between(ev[0], ev[1]);
+    return TSVD_OK;
+  }
+  TSVD_TRY(stage_ppr(s, iter, 0));
+  if (s->directed) TSVD_TRY(stage_ppr(s, iter, 1));
+  TSVD_CUDA(cudaEventRecord(ev[2], s->st));
+  TSVD_TRY(stage_materialize(s, iter));
+  TSVD_CUDA(cudaEventRecord(ev[3], s->st));
+  TSVD_TRY(stage_factorize(s, iter));
+  TSVD_CUDA(cudaEventRecord(ev[4], s->st));
+  TSVD_TRY(stage_merge(s));
+  TSVD_CUDA(cudaEventRecord(ev[5], s->st));
+  TSVD_CUDA(cudaEventSynchronize(ev[5]));
+  s->last.ms_insert = ms_between(ev[0], ev[1]);
+  s->last.ms_push = ms_between(ev[1], ev[2]);
+  s->last.ms_log = ms_between(ev[2], ev[3]);
+  s->last.ms_frpca = ms_between(ev[3], ev[4]);
+  s->last.ms_merge = ms_between(ev[4], ev[5]);
+  s->last.ms_total = ms_between(ev[0], ev[5]);
+  return TSVD_OK;
+}
+
+static tsvd_status stage_edges_to_device(tsvd_session *s, const int32_t *edges, int64_t m) {
+  if (m > s->edges_cap) {
+    cudaFree(s->edges_dev);
+    s->edges_dev = nullptr;
+    s->edges_cap = 0;
+    int64_t cap = std::max<int64_t>(m, 1024);
+    TSVD_CUDA(cudaMalloc(&s->edges_dev, sizeof(int32_t) * 2 * cap));
+    s->edges_cap = cap;
+  }
+  if (m > 0)
+    TSVD_CUDA(cudaMemcpyAsync(s->edges_dev, edges, sizeof(int32_t) * 2 * m, cudaMemcpyHostToDevice,
+                              s->st));
+  return TSVD_OK;
+}
+
+extern "C" tsvd_status tsvd_session_step(tsvd_session *s, const int32_t *edges, int64_t m) {
+  if (!s || (m > 0 && !edges) || m < 0) return fail(TSVD_ERR_INVALID, "bad arguments");
+  TSVD_CUDA(cudaSetDevice(s->cfg.device));
+  TSVD_TRY(stage_edges_to_device(s, edges, m));
+  return step_device(s, s->edges_dev, m);
+}
+
+extern "C" tsvd_status tsvd_session_step_device(tsvd_session *s, const int32_t *edges_dev,
+                                                int64_t m) {
+  if (!s || (m > 0 && !edges_dev) || m < 0) return fail(TSVD_ERR_INVALID, "bad arguments");
+  return step_device(s, edges_dev, m);
+}
+
+extern "C" tsvd_status tsvd_session_embedding(tsvd_session *s, double *out) {
+  if (!s || !out) return fail(TSVD_ERR_INVALID, "null argument");
+  if (!s->has_embedding) return fail(TSVD_ERR_STATE, "no embedding yet");
+  std::vector<float> tmp(s->node_elems());
+  TSVD_CUDA(cudaMemcpyAsync(tmp.data(), s->embedding, sizeof(float) * tmp.size(),
+                            cudaMemcpyDeviceToHost, s->st));
+  TSVD_CUDA(cudaStreamSynchronize(s->st));
+  for (size_t i = 0; i < tmp.size(); ++i) out[i] = tmp[i];
+  return TSVD_OK;
+}
+
+extern "C" tsvd_status tsvd_session_embedding_device(tsvd_session *s, const float **out) {
+  if (!s || !out) return fail(TSVD_ERR_INVALID, "null argument");
+  if (!s->has_embedding) return fail(TSVD_ERR_STATE, "no embedding yet");
+  *out = s->embedding;
+  return TSVD_OK;
+}
+
+extern "C" tsvd_status tsvd_session_stream(tsvd_session *s, void **stream) {
+  if (!s || !stream) return fail(TSVD_ERR_INVALID, "null argument");
+  *stream = (void *)s->st;
+  return TSVD_OK;
+}
+
+extern "C" tsvd_status tsvd_session_last_stats(tsvd_session *s, tsvd_step_stats *out) {
+  if (!s || !out) return fail(TSVD_ERR_INVALID, "null argument");
+  *out = s->last;
+  return TSVD_OK;
+}
+
+// ------------------------------------------------------------------ granular API
+extern "C" tsvd_status tsvd_graph_insert(tsvd_session *s, const int32_t *edges, int64_t m) {
+  if (!s || (m > 0 && !edges) || m < 0) return fail(TSVD_ERR_INVALID, "bad arguments");
+  TSVD_CUDA(cudaSetDevice(s->cfg.device));
+  TSVD_TRY(stage_edges_to_device(s, edges, m));
+  return insert_device(s, s->edges_dev, m);
+}
+
+extern "C" tsvd_status tsvd_ppr_refresh(tsvd_session *s, int32_t iter, int32_t transpose) {
+  if (!s) return fail(TSVD_ERR_INVALID, "null session");
+  if (transpose && !s->directed) return fail(TSVD_ERR_INVALID, "transpose on undirected graph");
+  TSVD_CUDA(cudaSetDevice(s->cfg.device));
+  PprParams prm = ppr_params(s);
+  const int dir = transpose ? 1 : 0;
+  return ppr_refresh(s->ppr[dir], s->adj[dir], s->sources_dev,
+                     iter < s->cfg.dynamic_ppr_start_iter, prm, s->vmark, s->st);
+}
+
+extern "C" tsvd_status tsvd_ppr_push(tsvd_session *s, int32_t transpose) {
+  if (!s) return fail(TSVD_ERR_INVALID, "null session");
+  if (transpose && !s->directed) return fail(TSVD_ERR_INVALID, "transpose on undirected graph");
+  TSVD_CUDA(cudaSetDevice(s->cfg.device));
+  PprParams prm = ppr_params(s);
+  const int dir = transpose ? 1 : 0;
+  PushStats ps;
+  TSVD_TRY(ppr_push(s->ppr[dir], s->adj[dir], prm, s->vmark, s->st, &ps));
+  s->last.push_rounds += ps.rounds;
+  s->last.pushes += ps.pushes;
+  s->last.push_edge_updates += ps.edge_updates;
+  TSVD_CUDA(cudaStreamSynchronize(s->st));
+  return TSVD_OK;
+}
+
+extern "C" tsvd_status tsvd_blocks_materialize(tsvd_session *s, int32_t iter, uint8_t *dirty) {
+  if (!s) return fail(TSVD_ERR_INVALID, "null session");
+  TSVD_CUDA(cudaSetDevice(s->cfg.device));
+  s->iter = iter;
+  TSVD_TRY(stage_materialize(s, iter));
+  if (dirty) std::memcpy(dirty, s->dirty_h.data(), s->nparts);
+  return TSVD_OK;
+}
+
+extern "C" tsvd_status tsvd_blocks_factorize(tsvd_session *s, int32_t iter) {
+  if (!s) return fail(TSVD_ERR_INVALID, "null session");
+  TSVD_CUDA(cudaSetDevice(s->cfg.device));
+  return stage_factorize(s, iter);
+}
+
+extern "C" tsvd_status tsvd_tree_merge(tsvd_session *s) {
+  if (!s) return fail(TSVD_ERR_INVALID, "null session");
+  TSVD_CUDA(cudaSetDevice(s->cfg.device));
+  return stage_merge(s);
+}
+
+// ------------------------------------------------------------------ inspection
+extern "C" tsvd_status tsvd_graph_degrees(tsvd_session *s, int32_t dir, int32_t *deg,
+                                          int32_t *former) {
+  if (!s || dir < 0 || dir > (s->directed ? 1 : 0)) return fail(TSVD_ERR_INVALID, "bad dir");
+  TSVD_CUDA(cudaStreamSynchronize(s->st));
+  if (deg) TSVD_CUDA(cudaMemcpy(deg, s->adj[dir].deg, sizeof(int32_t) * s->n, cudaMemcpyDeviceToHost));
+  if (former)
+    TSVD_CUDA(cudaMemcpy(former, s->adj[dir].former, sizeof(int32_t) * s->n, cudaMemcpyDeviceToHost));
+  return TSVD_OK;
+}
+
+extern "C" tsvd_status tsvd_graph_adjacency(tsvd_session *s, int32_t dir, int64_t *offsets,
+                                            int32_t *nbrs, int64_t cap) {
+  if (!s || dir < 0 || dir > (s->directed ? 1 : 0)) return fail(TSVD_ERR_INVALID, "bad dir");
+  TSVD_CUDA(cudaStreamSynchronize(s->st));
+  const Adjacency &A = s->adj[dir];
+  std::vector<int32_t> deg(s->n);
+  std::vector<int64_t> off(s->n + 1);
+  TSVD_CUDA(cudaMemcpy(deg.data(), A.deg, sizeof(int32_t) * s->n, cudaMemcpyDeviceToHost));
+  TSVD_CUDA(cudaMemcpy(off.data(), A.off, sizeof(int64_t) * (s->n + 1), cudaMemcpyDeviceToHost));
+  std::vector<int32_t> all((size_t)std::max<int64_t>(A.cap_total, 1));
+  if (A.cap_total > 0)
+    TSVD_CUDA(cudaMemcpy(all.data(), A.nbr, sizeof(int32_t) * A.cap_total, cudaMemcpyDeviceToHost));
+  int64_t pos = 0;
+  for (int v = 0; v < s->n; ++v) {
+    if (offsets) offsets[v] = pos;
+    if (nbrs) {
+      if (pos + deg[v] > cap) return fail(TSVD_ERR_INVALID, "adjacency buffer too small");
+      std::memcpy(nbrs + pos, all.data() + off[v], sizeof(int32_t) * deg[v]);
+    }
+    pos += deg[v];
+  }
+  if (offsets) offsets[s->n] = pos;
+  return TSVD_OK;
+}
+
+extern "C" tsvd_status tsvd_ppr_state(tsvd_session *s, int32_t transpose, int32_t which,
+                                      float *out) {
+  if (!s || !out || (transpose && !s->directed)) return fail(TSVD_ERR_INVALID, "bad arguments");
+  TSVD_CUDA(cudaStreamSynchronize(s->st));
+  const PprState &P = s->ppr[transpose ? 1 : 0];
+  std::vector<float> tmp((size_t)s->n * s->sp);
+  TSVD_CUDA(cudaMemcpy(tmp.data(), which ? P.p : P.r, sizeof(float) * tmp.size(),
+                       cudaMemcpyDeviceToHost));
+  for (int v = 0; v < s->n; ++v)
+    for (int k = 0; k < s->S; ++k) out[(size_t)k * s->n + v] = tmp[(size_t)v * s->sp + k];
+  return TSVD_OK;
+}
+
+extern "C" tsvd_status tsvd_block_info(tsvd_session *s, double *norm_a, double *norm_diff,
+                                       double *resid, int64_t *nnz, uint8_t *dirty) {
+  if (!s) return fail(TSVD_ERR_INVALID, "null session");
+  for (int b = 0; b < s->nparts; ++b) {
+    if (norm_a) norm_a[b] = std::sqrt(std::max(s->norm2_h[b], 0.0));
+    if (norm_diff) norm_diff[b] = std::sqrt(std::max(s->diff2_h[b], 0.0));
+    if (resid) resid[b] = s->resid[b];
+    if (nnz) nnz[b] = s->nnz_h[b];
+    if (dirty) dirty[b] = s->dirty_h[b];
+  }
+  return TSVD_OK;
+}
+
+extern "C" tsvd_status tsvd_tree_factor(tsvd_session *s, int32_t node, double *out,
+                                        double *sigma) {
+  if (!s || node < 0 || node >= s->total_nodes) return fail(TSVD_ERR_INVALID, "bad node");
+  TSVD_CUDA(cudaStreamSynchronize(s->st));
+  if (out) {
+    std::vector<float> tmp(s->node_elems());
+    TSVD_CUDA(cudaMemcpy(tmp.data(), s->node_b(node), sizeof(float) * tmp.size(),
+                         cudaMemcpyDeviceToHost));
+    for (size_t i = 0; i < tmp.size(); ++i) out[i] = tmp[i];
+  }
+  if (sigma) {
+    std::vector<float> tmp(s->d);
+    TSVD_CUDA(cudaMemcpy(tmp.data(), s->node_sigma(node), sizeof(float) * s->d,
+                         cudaMemcpyDeviceToHost));
+    for (int i = 0; i < s->d; ++i) sigma[i] = tmp[i];
+  }
+  return TSVD_OK;
+}
+
+extern "C" tsvd_status tsvd_block_dense(tsvd_session *s, int32_t b, float *out) {
+  if (!s || !out || b < 0 || b >= s->nparts) return fail(TSVD_ERR_INVALID, "bad block");
+  TSVD_CUDA(cudaStreamSynchronize(s->st));
+  const int nb = b == s->nparts - 1 ? s->n - (s->nparts - 1) * s->col_dim : s->col_dim;
+  const int nc = s->ncols_old_h[b];
+  std::vector<__half> at((size_t)std::max(nc, 1) * s->sp);
+  std::vector<int32_t> cm(std::max(nc, 1));
+  if (nc > 0) {
+    TSVD_CUDA(cudaMemcpy(at.data(), s->at_block(s->atcur[b], b), sizeof(__half) * nc * s->sp,
+                         cudaMemcpyDeviceToHost));
+    TSVD_CUDA(cudaMemcpy(cm.data(), s->colmap + (size_t)b * s->col_dim, sizeof(int32_t) * nc,
+                         cudaMemcpyDeviceToHost));
+  }
+  std::memset(out, 0, sizeof(float) * (size_t)s->S * nb);
+  for (int c = 0; c < nc; ++c) {
+    int col = cm[c] - b * s->col_dim;
+    for (int k = 0; k < s->S; ++k)
+      out[(size_t)k * nb + col] = __half2float(at[(size_t)c * s->sp + k]);
+  }
+  return TSVD_OK;
+}
