@@ -290,6 +290,23 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def aggregate(ms, edges, device=None):
+    """Whole-job throughput of independent replicas: every rank's edges over
+    the slowest rank's time (max over ranks; identity without a process group)."""
+    import torch
+    import torch.distributed as tdist
+    world = tdist.get_world_size() if tdist.is_available() and tdist.is_initialized() else 1
+    if world > 1:
+        t = torch.tensor([float(ms), float(edges)], dtype=torch.float64,
+                         device=device if device is not None else "cpu")
+        mx = t.clone()
+        tdist.all_reduce(mx, op=tdist.ReduceOp.MAX)
+        tot = t.clone()
+        tdist.all_reduce(tot, op=tdist.ReduceOp.SUM)
+        ms, edges = float(mx[0].item()), float(tot[1].item())
+    return ms, edges, edges / (ms / 1e3)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -300,17 +317,13 @@ def main():
     if dist:
         import torch.distributed as tdist
         tdist.init_process_group("nccl")
+        tdist.barrier()
     cfg, snaps, sources = workload(args)
     res = run_ours(args, cfg, snaps, sources, local)
-    ms = res["ms"]
     if dist:
-        import torch
         import torch.distributed as tdist
-        t = torch.tensor([ms], device=f"cuda:{local}")
-        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
-        ms = float(t.item())
-    edges_all = res["edges"] * world
-    value = edges_all / (ms / 1e3)
+        tdist.barrier()
+    ms, edges_all, value = aggregate(res["ms"], res["edges"], f"cuda:{local}" if dist else None)
     lat = res["per_step"]
     line = {"metric": METRIC, "value": value, "unit": "edge updates/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,

@@ -161,8 +161,8 @@ class OracleTreeSVD:
             upd += b
         self.push_counts = (pushes, upd)
 
-    def blocks_stage(self, iter):
-        p = self.reserve()
+    def blocks_stage(self, iter, p=None):
+        p = self.reserve() if p is None else np.asarray(p, dtype=np.float64)
         with_norm = iter >= self.lazy
         todo = []
         for b in range(self.P):
@@ -221,14 +221,17 @@ class OracleTreeSVD:
                 self.sigma[p] = S[:self.d]
             level = sorted({(p - 1) // h for p in level})
 
-    def step(self, edges):
+    def step(self, edges, reserve=None):
+        """One snapshot. With `reserve` (|S| x N, forward + reverse summed) the
+        PPR stage is skipped and the block stages run on the given reserve."""
         self.iter += 1
         it = self.iter
         self.g.insert(edges)
         if self.lazy != 100 and it < self.lazy - 1:
             return None
-        self.ppr_stage(it)
-        todo = self.blocks_stage(it)
+        if reserve is None:
+            self.ppr_stage(it)
+        todo = self.blocks_stage(it, reserve)
         for b in todo:
             self.factor_block(b, it)
         self.last_factorized = todo

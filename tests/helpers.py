@@ -36,6 +36,19 @@ def reach_weight(P, alpha, iters=400):
     return alpha * y
 
 
+def residual_error_bound(r, P, alpha, iters=400):
+    """|p_s - pi_s| <= (alpha |r_s| (I - (1-alpha) P)^-1) entrywise, for any
+    state satisfying the push identity (the dynamic refresh can leave negative
+    residues, so rmax alone does not bound the error). Solved by the fixed
+    point x = alpha |r| + (1-alpha) x P, one row per source."""
+    a = np.abs(r.astype(np.float64))
+    x = alpha * a
+    PT = P.T.tocsr()
+    for _ in range(iters):
+        x = alpha * a + (1 - alpha) * (PT @ x.T).T
+    return x
+
+
 def max_principal_sine(A, B):
     """Largest principal-angle sine between the column spaces of A and B."""
     qa = scipy.linalg.orth(A)

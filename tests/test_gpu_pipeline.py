@@ -9,7 +9,7 @@ from oracle import native
 from oracle.tree_oracle import OracleTreeSVD, frpca as oracle_frpca, gaussian_matrix, log_transform
 
 from helpers import (gap_index, gram_rel_err, max_principal_sine, push_identity_residual,
-                     reach_weight, transition)
+                     residual_error_bound, transition)
 
 pytestmark = pytest.mark.gpu
 
@@ -57,7 +57,7 @@ def test_graph_insert_empty_and_invalid():
         assert np.array_equal(before[1], after[1])
 
 
-def _ppr_checks(s, g, src, cfg, transpose, oracle_p=None):
+def _ppr_checks(s, g, src, cfg, transpose, oracle=None):
     d = 1 if transpose else 0
     off, nb = g.adjacency(d)
     P, deg = transition(cfg["n"], off, nb)
@@ -70,10 +70,11 @@ def _ppr_checks(s, g, src, cfg, transpose, oracle_p=None):
     elig = deg > 0
     assert (r[:, elig] <= np.float32(rmax)).all()
     assert (p >= 0).all()
-    if oracle_p is not None:
-        c = reach_weight(P, alpha)
-        bound = 2 * rmax * c[None, :] + 1e-6
-        assert (np.abs(p.astype(np.float64) - oracle_p) <= bound).all()
+    if oracle is not None:
+        # both states are within alpha |r| (I-(1-a)P)^-1 of the exact PPR
+        po, ro = oracle.reserve().astype(np.float64), oracle.residue()
+        bound = residual_error_bound(r, P, alpha) + residual_error_bound(ro, P, alpha)
+        assert (np.abs(p.astype(np.float64) - po) <= bound * (1 + 1e-3) + 1e-6).all()
 
 
 @pytest.mark.parametrize("directed", [False, True])
@@ -92,7 +93,7 @@ def test_ppr_from_scratch_and_dynamic(directed):
                 s.ppr_push(bool(t))
                 ors[t].refresh(g, t, it, 2, cfg["alpha"], cfg["rmax"])
                 ors[t].push(g, t, cfg["alpha"], cfg["rmax"])
-                _ppr_checks(s, g, src, cfg, bool(t), ors[t].reserve().astype(np.float64))
+                _ppr_checks(s, g, src, cfg, bool(t), ors[t])
 
 
 def test_ppr_intdiv_refresh_tracks_oracle():
@@ -112,9 +113,13 @@ def test_ppr_intdiv_refresh_tracks_oracle():
             o.push(g, 0, cfg["alpha"], cfg["rmax"])
         off, nb = g.adjacency(0)
         P, deg = transition(cfg["n"], off, nb)
-        c = reach_weight(P, cfg["alpha"])
         p = s.ppr_state(False, 1).astype(np.float64)
-        assert (np.abs(p - o.reserve()) <= 4 * cfg["rmax"] * c[None, :] + 1e-6).all()
+        r = s.ppr_state(False, 0)
+        # the integer-division refresh breaks the push identity (in the
+        # reference as here), so compare the states directly
+        assert (r[:, deg > 0] <= np.float32(cfg["rmax"])).all()
+        po = o.reserve().astype(np.float64)
+        assert np.linalg.norm(p - po) <= 1e-2 * np.linalg.norm(po)
 
 
 def test_block_materialize_matches_transform():
@@ -175,27 +180,42 @@ def test_frpca_abi_matches_oracle():
 
 @pytest.mark.parametrize("directed", [False, True])
 def test_session_matches_oracle_pipeline(directed):
+    """Whole snapshots through tsvd_session_step. The block stages (log
+    transform, lazy test, frPCA, merge) are checked against the oracle run on
+    the GPU's own reserve, so the comparison isolates their arithmetic; the
+    PPR stage is covered by test_ppr_from_scratch_and_dynamic."""
     cfg = small_cfg(directed, n=8000, m=60000, sources=96, n_parts=4, rank_d=32, snapshots=4)
     _, snaps, src = W.build(cfg, seed=21)
     kw = W.session_kwargs(cfg, dynamic_start=2, lazy_start=2)
     okw = dict(kw)
     okw.pop("seed")
-    o = OracleTreeSVD(cfg["n"], src, seed=20231, threads=8, **okw)
+    o = OracleTreeSVD(cfg["n"], src, seed=kw["seed"], **okw)
+    frac = kw["dirty_frac"]
     with T.Session(cfg["n"], src, **kw) as s:
         for e in snaps:
             st = s.step(e)
-            emb_o = o.step(e)
+            p = s.ppr_state(False, 1).astype(np.float64)
+            if directed:
+                p += s.ppr_state(True, 1)
+            emb_o = o.step(e, reserve=p)
             info = s.block_info()
-            # dirty sets agree wherever the decision is not a near-tie
-            margin = np.abs(info["norm_diff"] - cfg["dirty_frac"] * info["norm"]) > 1e-3 * info["norm"]
-            if cfg["dirty_rule"] == T.DIRTY_FROBENIUS:
-                assert np.array_equal(info["dirty"][margin], o.dirty[margin])
-            assert st["factorized_blocks"] == len(o.last_factorized) or not margin.all()
-            if emb_o is None:
-                continue
+            assert np.allclose(info["norm"], o.norm, rtol=1e-5)
+            if kw["dirty_rule"] == T.DIRTY_FROBENIUS:
+                tie = np.abs(o.norm_diff - frac * o.norm) <= 1e-3 * o.norm
+            else:
+                lhs = o.resid + o.norm_diff
+                tie = np.abs(lhs - kw["delta"] * np.sqrt(2) * o.norm) <= 1e-3 * o.norm
+            assert np.array_equal(info["dirty"][~tie], o.dirty[~tie])
+            if tie.any():
+                continue  # a near-tie decision may legitimately differ
+            assert st["factorized_blocks"] == len(o.last_factorized)
+            for b in o.last_factorized:
+                _, sg = s.tree_factor(s.leaf_start + b)
+                so = o.sigma[s.leaf_start + b]
+                j = gap_index(so, cfg["rank_d"])
+                assert np.allclose(sg[:j], so[:j], rtol=1e-3), (b, np.abs(sg[:j] / so[:j] - 1).max())
             emb = s.embedding()
             assert np.isfinite(emb).all()
             _, sig = s.tree_factor(0)
-            k = cfg["rank_d"]
-            assert np.allclose(sig[:8], o.sigma[0][:8], rtol=2e-3)
-            assert gram_rel_err(emb, emb_o) < 2e-2
+            assert np.allclose(sig[:16], o.sigma[0][:16], rtol=1e-3)
+            assert gram_rel_err(emb, emb_o) < 5e-3

@@ -1,0 +1,150 @@
+// tree_svd — command-line drop-in for the reference drivers Tree_u_NC,
+// Tree_d_NC, Tree_u_LP and Tree_d_LP (Code/Tree_u_NC.cpp:296-911 and
+// siblings), running the snapshot loop on the GPU through libtsvd_gb300.
+//
+//   tree_svd <u_nc|d_nc|u_lp|d_lp> queryname EBpath alpha pass rmax NUMTHREAD \
+//            nParts hierarchy_n N dynamic_ppr_start_iter lazy_update_start_iter delta \
+//            [--compat] [--device K]
+//
+// Same positional arguments (Tree_u_NC.cpp:301-322; NUMTHREAD is accepted and
+// ignored), same inputs (DY_Dataset/<queryname>/config.txt: line 0 the subset
+// file, then one edge file per snapshot, :338-372) and the same output file
+// name and CSV layout (:877-909): ((T-1)*|S|) x 128 values, ", " separated,
+// six significant digits. --compat reproduces the reference's reader (last
+// pair of a file repeated when whitespace follows it) and its integer-division
+// refresh; without it the exact refresh is used.
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <iostream>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "tsvd.h"
+
+static int die(const char *what, tsvd_status st) {
+  std::fprintf(stderr, "tree_svd: %s: %s (%s)\n", what, tsvd_status_string(st), tsvd_last_error());
+  return 1;
+}
+
+int main(int argc, char **argv) {
+  if (argc < 14) {
+    std::fprintf(stderr,
+                 "usage: %s <u_nc|d_nc|u_lp|d_lp> queryname EBpath alpha pass rmax NUMTHREAD "
+                 "nParts hierarchy_n N dynamic_ppr_start_iter lazy_update_start_iter delta "
+                 "[--compat] [--device K]\n",
+                 argv[0]);
+    return 2;
+  }
+  const std::string mode = argv[1];
+  const bool directed = mode[0] == 'd';
+  const bool lp = mode.size() >= 4 && mode.substr(2) == "lp";
+  const std::string queryname = argv[2], ebpath = argv[3];
+  char *endp;
+  const double alpha = std::strtod(argv[4], &endp);
+  const int pass = (int)std::strtod(argv[5], &endp);
+  const double rmax = std::strtod(argv[6], &endp);
+  const int nparts = (int)std::strtod(argv[8], &endp);
+  const int hn = (int)std::strtod(argv[9], &endp);
+  const int nv = (int)std::strtod(argv[10], &endp);
+  const int dyn = (int)std::strtod(argv[11], &endp);
+  const int lazy = (int)std::strtod(argv[12], &endp);
+  const double delta = std::strtod(argv[13], &endp);
+  bool compat = false;
+  int device = 0;
+  for (int i = 14; i < argc; ++i) {
+    if (!std::strcmp(argv[i], "--compat")) compat = true;
+    else if (!std::strcmp(argv[i], "--device") && i + 1 < argc) device = std::atoi(argv[++i]);
+  }
+  std::vector<std::string> shots;
+  {
+    std::ifstream cfg(("DY_Dataset/" + queryname + "/config.txt").c_str());
+    if (!cfg) {
+      std::fprintf(stderr, "tree_svd: cannot read DY_Dataset/%s/config.txt\n", queryname.c_str());
+      return 1;
+    }
+    std::string line;
+    while (std::getline(cfg, line)) shots.push_back(line);
+  }
+  if (shots.size() < 2) {
+    std::fprintf(stderr, "tree_svd: config.txt needs a subset file and at least one snapshot\n");
+    return 1;
+  }
+  std::vector<int32_t> sources;
+  {
+    std::ifstream sf(shots[0].c_str());
+    int v;
+    while (sf >> v) sources.push_back(v);
+  }
+  const int d = 128;
+  tsvd_config c;
+  tsvd_config_default(&c);
+  c.n_vertices = nv;
+  c.directed = directed;
+  c.n_sources = (int32_t)sources.size();
+  c.sources = sources.data();
+  c.alpha = alpha;
+  c.rmax = rmax;
+  c.n_parts = nparts;
+  c.hierarchy_n = hn;
+  c.rank_d = d;
+  c.passes_q = pass;
+  c.dynamic_ppr_start_iter = dyn;
+  c.lazy_update_start_iter = lazy;
+  c.delta = delta;
+  c.transform = lp ? TSVD_TRANSFORM_LOG10_LP : TSVD_TRANSFORM_LOG10_NC;
+  c.root_scaling = lp ? TSVD_ROOT_U : TSVD_ROOT_SQRT_SIGMA;
+  c.refresh_mode = compat ? TSVD_REFRESH_INTDIV : TSVD_REFRESH_EXACT;
+  c.device = device;
+  tsvd_session *s = nullptr;
+  tsvd_status st = tsvd_session_create(&c, &s);
+  if (st != TSVD_OK) return die("session", st);
+  const size_t S = sources.size();
+  const int T = (int)shots.size();
+  std::vector<double> all((size_t)(T - 1) * S * d, 0.0), emb(S * d, 0.0);
+  bool have = false;
+  for (int it = 1; it < T; ++it) {
+    int32_t *edges = nullptr;
+    int64_t m = 0;
+    st = tsvd_read_edge_file(shots[it].c_str(), compat ? 1 : 0, &edges, &m);
+    if (st != TSVD_OK) return die(shots[it].c_str(), st);
+    st = tsvd_session_step(s, edges, m);
+    tsvd_free(edges);
+    if (st != TSVD_OK) return die("step", st);
+    tsvd_step_stats ss;
+    tsvd_session_last_stats(s, &ss);
+    std::printf("Iter = %d, edges %lld, pushes %lld, dirty %d, time = %.3f ms\n", it,
+                (long long)ss.edges_inserted, (long long)ss.pushes, ss.dirty_blocks, ss.ms_total);
+    if (tsvd_session_embedding(s, emb.data()) == TSVD_OK) have = true;
+    if (have) std::copy(emb.begin(), emb.end(), all.begin() + (size_t)(it - 1) * S * d);
+  }
+  tsvd_session_destroy(s);
+  // Tree_u_NC.cpp:877-896
+  int residue_order = 0;
+  if (rmax * 10000 == 1) residue_order = 5;
+  else if (rmax * 100000 == 1) residue_order = 6;
+  else if (rmax * 1000000 == 1) residue_order = 7;
+  else if (rmax * 10000000 == 1) residue_order = 8;
+  else if (rmax * 1000000000 == 1) residue_order = 10;
+  const std::string out = ebpath + queryname + std::to_string(delta) + "_" +
+                          std::to_string(residue_order) + "_" + std::to_string(nparts) + "_" +
+                          std::to_string(hn) + "_" + "De_svd_" + (directed ? "d" : "u") +
+                          "_Dppr_parallel_bound_nodegree_U.csv";
+  std::ofstream os(out.c_str());
+  if (!os) {
+    std::fprintf(stderr, "tree_svd: cannot write %s\n", out.c_str());
+    return 1;
+  }
+  const size_t rows = (size_t)(T - 1) * S;
+  for (size_t r = 0; r < rows; ++r) {
+    for (int j = 0; j < d; ++j) {
+      if (j) os << ", ";
+      os << all[r * d + j];
+    }
+    if (r + 1 < rows) os << "\n";
+  }
+  std::printf("wrote %s\n", out.c_str());
+  return 0;
+}

@@ -28,11 +28,11 @@ namespace {
 constexpr int kHeavy = 1024;  // neighbours per warp work unit for hub vertices
 constexpr unsigned kFull = 0xffffffffu;
 
+// Sets the touched bit of (u, chunk c). The result is unused, so this is a
+// fire-and-forget reduction (RED.OR): no round trip on the issuing warp.
 __device__ __forceinline__ void mark_touched(uint32_t *tflag, int32_t u, int32_t c, int32_t C) {
   int64_t idx = (int64_t)u * C + c;
-  uint32_t bit = 1u << (idx & 31);
-  uint32_t *w = tflag + (idx >> 5);
-  if (!(__ldcg(w) & bit)) atomicOr(w, bit);
+  atomicOr(tflag + (idx >> 5), 1u << (idx & 31));
 }
 
 struct StatAcc {
@@ -70,8 +70,9 @@ __device__ __forceinline__ void scatter_range(const PushArgs &a, int32_t v, int3
     for (int32_t t = 0; t < jn; ++t) {
       int32_t u = __shfl_sync(kFull, mine, t);
       if (act) atomicAdd(a.r + (int64_t)u * a.sp + s, w);
-      if (lane == 0) mark_touched(a.tflag, u, c, a.chunks);
     }
+    // each lane marks the neighbour it loaded: 32 independent reductions
+    if (lane < jn) mark_touched(a.tflag, mine, c, a.chunks);
   }
 }
 
