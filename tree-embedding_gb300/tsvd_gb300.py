@@ -77,6 +77,9 @@ _SIGS = {
     "tsvd_frpca": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.c_int64, _i64p, _i32p,
                                   _f64p, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
                                   ctypes.c_uint64, _f64p, _f64p, _f64p]),
+    "tsvd_frpca_noalloc": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.c_int64, _i64p,
+                                          _i32p, _f64p, ctypes.c_int32, ctypes.c_int32,
+                                          ctypes.c_int32, ctypes.c_uint64, _f64p, _f64p, _f64p]),
     "tsvd_config_default": (None, [ctypes.POINTER(Config)]),
     "tsvd_session_create": (ctypes.c_int, [ctypes.POINTER(Config), ctypes.POINTER(_vp)]),
     "tsvd_session_destroy": (ctypes.c_int, [_vp]),
@@ -181,8 +184,10 @@ def launch_count():
     return lib().tsvd_launch_count()
 
 
-def frpca(csr_indptr, csr_indices, csr_data, shape, k, q, seed=20231, index_base=0):
-    """Randomized SVD of a CSR matrix; returns U (m x k), S (k, descending), V (n x k)."""
+def frpca(csr_indptr, csr_indices, csr_data, shape, k, q, seed=20231, index_base=0,
+          noalloc=False):
+    """Randomized SVD of a CSR matrix; returns U (m x k), S (k, descending), V (n x k).
+    noalloc=True calls tsvd_frpca_noalloc (no allocation, bounded sizes)."""
     m, n = shape
     rp = np.ascontiguousarray(csr_indptr, dtype=np.int64)
     ci = np.ascontiguousarray(csr_indices, dtype=np.int32)
@@ -190,8 +195,9 @@ def frpca(csr_indptr, csr_indices, csr_data, shape, k, q, seed=20231, index_base
     U = np.zeros((k, m), np.float64)
     S = np.zeros(k, np.float64)
     V = np.zeros((k, n), np.float64)
-    _check(lib().tsvd_frpca(m, n, len(va), _p(rp, _i64p), _p(ci, _i32p), _p(va, _f64p),
-                            index_base, k, q, seed, _p(U, _f64p), _p(S, _f64p), _p(V, _f64p)))
+    fn = lib().tsvd_frpca_noalloc if noalloc else lib().tsvd_frpca
+    _check(fn(m, n, len(va), _p(rp, _i64p), _p(ci, _i32p), _p(va, _f64p), index_base, k, q,
+              seed, _p(U, _f64p), _p(S, _f64p), _p(V, _f64p)))
     return U.T.copy(), S, V.T.copy()
 
 
