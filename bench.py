@@ -267,11 +267,11 @@ def run_reference(args):
     cfg, snaps, sources = workload(args)
     vals = []
     info = None
-    for _ in range(args.warmup):
-        pass  # the CPU sample has no device warm-up
     t0 = time.perf_counter()
+    # each step is one bounded CPU sample of a dynamic snapshot, scaled to the
+    # full workload; the run stops after two minutes of samples
     for k in range(max(1, args.steps)):
-        info = cpu_sample(cfg, snaps[k % max(1, len(snaps) - 1):] if False else snaps, sources)
+        info = cpu_sample(cfg, snaps, sources)
         vals.append(info["edges"] / info["seconds_per_snapshot"])
         if time.perf_counter() - t0 > 120:
             break
@@ -288,6 +288,40 @@ def run_reference(args):
             "e2e": {"value": v, "unit": "edge updates/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
+
+
+# Per-launch DRAM traffic of the push scatter kernels measured by ncu on the
+# scaled case (profiles/push_kernel_rmat-d.md), per pushed item-neighbour, used to
+# scale `traffic` to a full launch; None until such a capture exists.
+PUSH_TRAFFIC_BYTES_PER_ITEM_EDGE = None
+
+
+def push_roofline(stages):
+    """Roofline of the dominant kernels (push_kernel + push_heavy_kernel) over
+    the timed steps. Algorithmic bytes: per lane push 16 (residue exchange +
+    reserve read-modify-write, fp32), per lane edge update 8 (fp32 atomic
+    read-modify-write of r[u][s]), per item-neighbour 4 (neighbour id), per
+    item 20 (frontier entry, row start, degree); duration from CUDA events
+    around every launch on the session stream."""
+    pk, _ = peaks()
+    peak = float(pk.get("hbm_gbs", 6800.0))
+    pushes = sum(s["pushes"] for s in stages)
+    upd = sum(s["push_edge_updates"] for s in stages)
+    items = sum(s["push_items"] for s in stages)
+    iedges = sum(s["push_item_edges"] for s in stages)
+    ms = sum(s["ms_push_kernels"] for s in stages)
+    launches = sum(2 * s["push_rounds"] for s in stages)
+    byts = 16.0 * pushes + 8.0 * upd + 4.0 * iedges + 20.0 * items
+    achieved = byts / (ms / 1e3) / 1e9 if ms > 0 else 0.0
+    traffic = None
+    if PUSH_TRAFFIC_BYTES_PER_ITEM_EDGE is not None and launches:
+        traffic = PUSH_TRAFFIC_BYTES_PER_ITEM_EDGE * iedges / launches
+    return {"kernel": "push_kernel+push_heavy_kernel", "bound": "hbm", "achieved": achieved,
+            "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
+            "algorithmic_bytes_per_launch": byts / max(1, launches),
+            "launches": launches, "kernel_ms": ms,
+            "lanes_per_item": pushes / max(1, items),
+            "peak_source": "MEASURED_PEAKS.json hbm_gbs (copy bandwidth)"}
 
 
 def aggregate(ms, edges, device=None):
@@ -341,7 +375,11 @@ def main():
             "stage_ms_mean": {k: float(np.mean([s[k] for s in res["stages"]]))
                               for k in ("ms_insert", "ms_push", "ms_log", "ms_frpca", "ms_merge")},
             "push_rounds_mean": float(np.mean([s["push_rounds"] for s in res["stages"]])),
+            "pushes_mean": float(np.mean([s["pushes"] for s in res["stages"]])),
+            "push_edge_updates_mean": float(np.mean([s["push_edge_updates"] for s in res["stages"]])),
+            "ms_materialize_kernel_mean": float(np.mean([s["ms_materialize_kernel"] for s in res["stages"]])),
             "dirty_blocks_mean": float(np.mean([s["dirty_blocks"] for s in res["stages"]]))}
+    line["roofline"] = push_roofline(res["stages"])
     if "e2e_ms" in res:
         line["e2e"] = {"value": edges_all / (res["e2e_ms"] / 1e3), "unit": "edge updates/s",
                        "h2d_bytes_per_step": res["h2d"], "d2h_bytes_per_step": res["d2h"],

@@ -167,6 +167,9 @@ typedef struct tsvd_config {
   uint64_t seed;            /* Gaussian test matrices                                */
   int32_t device;           /* CUDA device ordinal                                   */
   int32_t max_push_rounds;  /* bound on frontier rounds per push (0 = default)       */
+  int32_t push_levels;      /* threshold schedule: push r > rmax*ratio^k, k = L-1..0  */
+  double push_ratio;        /* (1 level = the plain rmax test)                      */
+  double push_cofrac;       /* co-push residues > rmax*cofrac on lines being pushed  */
 } tsvd_config;
 
 /* Fills the reference's defaults (Tree_u_NC, run.sh: alpha .5, q 12, ...). */
@@ -204,6 +207,10 @@ typedef struct tsvd_step_stats {
   int32_t factorized_blocks;
   int32_t merged_nodes;
   double ms_insert, ms_refresh, ms_push, ms_log, ms_frpca, ms_merge, ms_total;
+  int64_t push_items;       /* (vertex, 32-source chunk) items pushed             */
+  double ms_push_kernels;   /* device time of the push scatter kernels            */
+  double ms_materialize_kernel; /* device time of the block materialization      */
+  int64_t push_item_edges;  /* sum of deg(v) over pushed items (neighbour-list reads) */
 } tsvd_step_stats;
 tsvd_status tsvd_session_last_stats(tsvd_session *s, tsvd_step_stats *out);
 

@@ -17,6 +17,7 @@
 // The loop ends when a frontier is empty: every eligible residue <= rmax,
 // the same invariant the FIFO leaves behind.
 #include <algorithm>
+#include <cmath>
 
 #include "internal.h"
 #include "ppr.h"
@@ -36,25 +37,31 @@ __device__ __forceinline__ void mark_touched(uint32_t *tflag, int32_t u, int32_t
 }
 
 struct StatAcc {
-  unsigned long long pushes = 0, upd = 0;
+  unsigned long long pushes = 0, upd = 0, items = 0, iedges = 0;
 };
 
 __device__ void flush_stats(StatAcc acc, unsigned long long *gstats) {
-  __shared__ unsigned long long sp[32], su[32];
+  __shared__ unsigned long long sp[32], su[32], si[32], se[32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  unsigned long long a = acc.pushes, b = acc.upd;
+  unsigned long long a = acc.pushes, b = acc.upd, c = acc.items, e = acc.iedges;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
     a += __shfl_down_sync(kFull, a, o);
     b += __shfl_down_sync(kFull, b, o);
+    c += __shfl_down_sync(kFull, c, o);
+    e += __shfl_down_sync(kFull, e, o);
   }
-  if (lane == 0) { sp[warp] = a; su[warp] = b; }
+  if (lane == 0) { sp[warp] = a; su[warp] = b; si[warp] = c; se[warp] = e; }
   __syncthreads();
   if (threadIdx.x == 0) {
-    unsigned long long ta = 0, tb = 0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) { ta += sp[w]; tb += su[w]; }
+    unsigned long long ta = 0, tb = 0, tc = 0, te = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+      ta += sp[w]; tb += su[w]; tc += si[w]; te += se[w];
+    }
     if (ta) atomicAdd(&gstats[0], ta);
     if (tb) atomicAdd(&gstats[1], tb);
+    if (tc) atomicAdd(&gstats[2], tc);
+    if (te) atomicAdd(&gstats[3], te);
   }
 }
 
@@ -89,8 +96,22 @@ __global__ void __launch_bounds__(256) push_kernel(PushArgs a) {
     const int32_t s = c * 32 + lane;
     float *rp = a.r + (int64_t)v * a.sp + s;
     float x = __ldcg(rp);
-    bool act = s < a.nsrc && x > a.rmax_f;
+    // push above the current level of the threshold schedule; lanes between
+    // rmax and that level are parked in the pending set for a later level
+    bool act = s < a.nsrc && x > a.theta_f;
     unsigned mask = __ballot_sync(kFull, act);
+    // Co-push: once the line is pushed for some source, the other sources of
+    // the chunk with a residue above co_f ride along. The 128-byte atomic per
+    // neighbour is paid either way; pushing a residue below rmax is a valid
+    // push step (the push identity holds) that the FIFO would do later or not
+    // at all, so it only tightens the error bound.
+    if (mask && a.co_f < a.theta_f) {
+      act = s < a.nsrc && x > a.co_f;
+      mask = __ballot_sync(kFull, act);
+    }
+    if (a.theta_f > a.rmax_f && d > 0 &&
+        __ballot_sync(kFull, s < a.nsrc && !act && x > a.rmax_f) && lane == 0)
+      mark_touched(a.pend, v, c, a.chunks);
     if (!mask) continue;
     if (d == 0) {
       // Isolated source of an undirected graph: the reference assigns
@@ -110,6 +131,8 @@ __global__ void __launch_bounds__(256) push_kernel(PushArgs a) {
       if (a.vmark[v] == 0) a.vmark[v] = 1;
       acc.pushes += __popc(mask);
       acc.upd += (unsigned long long)__popc(mask) * (unsigned long long)d;
+      acc.items += 1;
+      acc.iedges += (unsigned long long)d;
     }
     if (d > kHeavy) {
       // Hub vertex: park the lane weights and split the neighbour list into
@@ -185,11 +208,13 @@ __global__ void __launch_bounds__(256) collect_kernel(CollectArgs a) {
         if (a.deg[u] == 0) continue;
         int32_t s = c * 32 + lane;
         float x = s < a.nsrc ? __ldcg(a.r + (int64_t)u * a.sp + s) : 0.0f;
-        if (__ballot_sync(kFull, x > a.rmax_f)) {
+        if (__ballot_sync(kFull, x > a.theta_f)) {
           if (lane == 0) {
             int32_t pos = atomicAdd(&nbuf, 1);
             buf[pos] = make_int2(u, c);
           }
+        } else if (a.theta_f > a.rmax_f && __ballot_sync(kFull, x > a.rmax_f)) {
+          if (lane == 0) mark_touched(a.pend, u, c, a.chunks);  // for a lower level
         }
       }
     }
@@ -251,6 +276,19 @@ __global__ void __launch_bounds__(256) refresh_kernel(RefreshArgs a) {
   }
 }
 
+// Lowering the threshold: parked (vertex, chunk) pairs become touched again.
+__global__ void unpark_kernel(uint32_t *__restrict__ tflag, uint32_t *__restrict__ pend,
+                              int64_t nwords) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nwords;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    uint32_t b = pend[i];
+    if (b) {
+      tflag[i] |= b;
+      pend[i] = 0;
+    }
+  }
+}
+
 __global__ void list_updated_kernel(const int32_t *__restrict__ deg,
                                     const int32_t *__restrict__ former, int32_t n,
                                     int32_t *__restrict__ out, int32_t *__restrict__ count) {
@@ -301,6 +339,8 @@ tsvd_status ppr_alloc(PprState &P, int32_t n, int32_t nsrc, int32_t sp) {
   P.nwords = ceil_div((int64_t)n * P.chunks, 32);
   TSVD_CUDA(cudaMalloc(&P.tflag, P.nwords * sizeof(uint32_t)));
   TSVD_CUDA(cudaMemset(P.tflag, 0, P.nwords * sizeof(uint32_t)));
+  TSVD_CUDA(cudaMalloc(&P.pend, P.nwords * sizeof(uint32_t)));
+  TSVD_CUDA(cudaMemset(P.pend, 0, P.nwords * sizeof(uint32_t)));
   P.cap = (int64_t)n * P.chunks;
   for (int i = 0; i < 2; ++i) TSVD_CUDA(cudaMalloc(&P.front[i], P.cap * sizeof(int2)));
   P.heavy_cap = 1 << 20;
@@ -314,15 +354,18 @@ tsvd_status ppr_alloc(PprState &P, int32_t n, int32_t nsrc, int32_t sp) {
   TSVD_CUDA(cudaMemset(P.counters, 0, 16 * sizeof(int32_t)));
   TSVD_CUDA(cudaMalloc(&P.stats, 4 * sizeof(unsigned long long)));
   TSVD_CUDA(cudaMallocHost(&P.host_counters, 16 * sizeof(int32_t)));
+  for (auto &e : P.kev) TSVD_CUDA(cudaEventCreate(&e));
   return TSVD_OK;
 }
 
 void ppr_free(PprState &P) {
-  cudaFree(P.r); cudaFree(P.p); cudaFree(P.tflag);
+  cudaFree(P.r); cudaFree(P.p); cudaFree(P.tflag); cudaFree(P.pend);
   cudaFree(P.front[0]); cudaFree(P.front[1]);
   cudaFree(P.heavy_w); cudaFree(P.heavy_item); cudaFree(P.heavy_mask); cudaFree(P.units);
   cudaFree(P.upd); cudaFree(P.counters); cudaFree(P.stats);
   cudaFreeHost(P.host_counters);
+  for (auto &e : P.kev)
+    if (e) cudaEventDestroy(e);
   P = PprState();
 }
 
@@ -336,6 +379,7 @@ tsvd_status ppr_refresh(PprState &P, const Adjacency &A, const int32_t *sources_
     TSVD_CUDA(cudaMemsetAsync(P.r, 0, (size_t)P.n * P.sp * sizeof(float), st));
     TSVD_CUDA(cudaMemsetAsync(P.p, 0, (size_t)P.n * P.sp * sizeof(float), st));
     TSVD_CUDA(cudaMemsetAsync(P.tflag, 0, P.nwords * sizeof(uint32_t), st));
+    TSVD_CUDA(cudaMemsetAsync(P.pend, 0, P.nwords * sizeof(uint32_t), st));
     P.cur = 0;
     init_sources_kernel<<<grid_for(P.nsrc, 256), 256, 0, st>>>(sources_dev, P.nsrc, P.r, P.sp,
                                                                   P.front[0], P.counters + 0);
@@ -362,6 +406,7 @@ tsvd_status ppr_refresh(PprState &P, const Adjacency &A, const int32_t *sources_
   CollectArgs ca;
   ca.tflag = P.tflag; ca.nwords = P.nwords; ca.chunks = P.chunks; ca.nsrc = P.nsrc;
   ca.sp = P.sp; ca.r = P.r; ca.deg = A.deg; ca.rmax_f = largest_float_not_above(prm.rmax);
+  ca.theta_f = ca.rmax_f; ca.pend = P.pend;
   ca.next = P.front[0]; ca.next_count = P.counters + 0; ca.cap = P.cap;
   ca.overflow = P.counters + 4;
   collect_kernel<<<grid_for(ceil_div(P.nwords, 64) * 256, 256, 8), 256, 0, st>>>(ca);
@@ -373,58 +418,88 @@ tsvd_status ppr_refresh(PprState &P, const Adjacency &A, const int32_t *sources_
 tsvd_status ppr_push(PprState &P, const Adjacency &A, const PprParams &prm, uint8_t *vmark,
                      cudaStream_t st, PushStats *out) {
   if (!P.seeded) return fail(TSVD_ERR_STATE, "push before refresh");
-  TSVD_CUDA(cudaMemsetAsync(P.stats, 0, 2 * sizeof(unsigned long long), st));
+  TSVD_CUDA(cudaMemsetAsync(P.stats, 0, 4 * sizeof(unsigned long long), st));
   TSVD_CUDA(cudaMemsetAsync(P.counters + 4, 0, sizeof(int32_t), st));
   const float rmax_f = largest_float_not_above(prm.rmax);
   PushArgs pa;
   pa.r = P.r; pa.p = P.p; pa.off = A.off; pa.deg = A.deg; pa.nbr = A.nbr;
-  pa.sp = P.sp; pa.nsrc = P.nsrc; pa.chunks = P.chunks; pa.tflag = P.tflag;
+  pa.sp = P.sp; pa.nsrc = P.nsrc; pa.chunks = P.chunks; pa.tflag = P.tflag; pa.pend = P.pend;
   pa.alpha_f = (float)prm.alpha; pa.one_minus_alpha_f = (float)(1.0 - prm.alpha);
   pa.rmax_f = rmax_f; pa.undirected = prm.undirected; pa.vmark = vmark;
+  pa.co_f = prm.cofrac >= 1.0 ? rmax_f : (float)(prm.rmax * std::max(prm.cofrac, 0.0));
   pa.heavy_w = P.heavy_w; pa.heavy_item = P.heavy_item; pa.heavy_mask = P.heavy_mask;
   pa.heavy_count = P.counters + 2; pa.heavy_cap = P.heavy_cap;
   pa.units = P.units; pa.unit_count = P.counters + 3; pa.unit_cap = P.unit_cap;
   pa.overflow = P.counters + 4; pa.stats = P.stats;
   CollectArgs ca;
-  ca.tflag = P.tflag; ca.nwords = P.nwords; ca.chunks = P.chunks; ca.nsrc = P.nsrc;
-  ca.sp = P.sp; ca.r = P.r; ca.deg = A.deg; ca.rmax_f = rmax_f; ca.cap = P.cap;
-  ca.overflow = P.counters + 4;
+  ca.tflag = P.tflag; ca.pend = P.pend; ca.nwords = P.nwords; ca.chunks = P.chunks;
+  ca.nsrc = P.nsrc; ca.sp = P.sp; ca.r = P.r; ca.deg = A.deg; ca.rmax_f = rmax_f;
+  ca.cap = P.cap; ca.overflow = P.counters + 4;
   const int gpush = grid_for((int64_t)1 << 30, 256, 8);
   const int gcol = grid_for(ceil_div(P.nwords, 64) * 256, 256, 8);
-  const int check_every = prm.check_every > 0 ? prm.check_every : 4;
+  const int check_every = std::min(8, prm.check_every > 0 ? prm.check_every : 4);
+  double kernel_ms = 0;
+  const int levels = std::max(1, prm.levels);
   int64_t rounds = 0;
-  for (;;) {
-    for (int k = 0; k < check_every; ++k) {
-      int cur = P.cur, nxt = 1 - P.cur;
-      pa.front = P.front[cur];
-      pa.front_count = P.counters + cur;
-      TSVD_CUDA(cudaMemsetAsync(P.counters + 2, 0, 2 * sizeof(int32_t), st));
-      TSVD_CUDA(cudaMemsetAsync(P.counters + nxt, 0, sizeof(int32_t), st));
-      push_kernel<<<gpush, 256, 0, st>>>(pa);
+  // Threshold schedule: residues above rmax * ratio^k are pushed first, k
+  // descending to 0. Lower residues wait in the pending set, so a vertex
+  // collects more before it is pushed; the last level is the plain rmax test
+  // and leaves the same invariant (every eligible residue <= rmax).
+  for (int level = levels - 1; level >= 0; --level) {
+    const float theta = largest_float_not_above(prm.rmax * std::pow(prm.ratio, (double)level));
+    pa.theta_f = ca.theta_f = std::max(theta, rmax_f);
+    if (level < levels - 1) {
+      // the frontier of the previous level is empty: re-examine parked pairs
+      unpark_kernel<<<grid_for(P.nwords, 256, 8), 256, 0, st>>>(P.tflag, P.pend, P.nwords);
       TSVD_LAUNCH_CHECK();
-      push_heavy_kernel<<<gpush, 256, 0, st>>>(pa);
-      TSVD_LAUNCH_CHECK();
-      ca.next = P.front[nxt];
-      ca.next_count = P.counters + nxt;
+      TSVD_CUDA(cudaMemsetAsync(P.counters + P.cur, 0, sizeof(int32_t), st));
+      ca.next = P.front[P.cur];
+      ca.next_count = P.counters + P.cur;
       collect_kernel<<<gcol, 256, 0, st>>>(ca);
       TSVD_LAUNCH_CHECK();
-      P.cur = nxt;
-      ++rounds;
     }
-    TSVD_CUDA(cudaMemcpyAsync(P.host_counters, P.counters, 8 * sizeof(int32_t),
-                              cudaMemcpyDeviceToHost, st));
-    TSVD_CUDA(cudaStreamSynchronize(st));
-    if (P.host_counters[4]) return fail(TSVD_ERR_STATE, "push: frontier buffer overflow");
-    if (P.host_counters[P.cur] == 0) break;
-    if (rounds >= prm.max_rounds)
-      return fail(TSVD_ERR_TIMEOUT, "push: %lld rounds without convergence", (long long)rounds);
+    for (;;) {
+      for (int k = 0; k < check_every; ++k) {
+        int cur = P.cur, nxt = 1 - P.cur;
+        pa.front = P.front[cur];
+        pa.front_count = P.counters + cur;
+        TSVD_CUDA(cudaMemsetAsync(P.counters + 2, 0, 2 * sizeof(int32_t), st));
+        TSVD_CUDA(cudaMemsetAsync(P.counters + nxt, 0, sizeof(int32_t), st));
+        TSVD_CUDA(cudaEventRecord(P.kev[2 * k], st));
+        push_kernel<<<gpush, 256, 0, st>>>(pa);
+        TSVD_LAUNCH_CHECK();
+        push_heavy_kernel<<<gpush, 256, 0, st>>>(pa);
+        TSVD_LAUNCH_CHECK();
+        TSVD_CUDA(cudaEventRecord(P.kev[2 * k + 1], st));
+        ca.next = P.front[nxt];
+        ca.next_count = P.counters + nxt;
+        collect_kernel<<<gcol, 256, 0, st>>>(ca);
+        TSVD_LAUNCH_CHECK();
+        P.cur = nxt;
+        ++rounds;
+      }
+      TSVD_CUDA(cudaMemcpyAsync(P.host_counters, P.counters, 8 * sizeof(int32_t),
+                                cudaMemcpyDeviceToHost, st));
+      TSVD_CUDA(cudaStreamSynchronize(st));
+      for (int k = 0; k < check_every; ++k) {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, P.kev[2 * k], P.kev[2 * k + 1]) == cudaSuccess) kernel_ms += ms;
+      }
+      if (P.host_counters[4]) return fail(TSVD_ERR_STATE, "push: frontier buffer overflow");
+      if (P.host_counters[P.cur] == 0) break;
+      if (rounds >= prm.max_rounds)
+        return fail(TSVD_ERR_TIMEOUT, "push: %lld rounds without convergence", (long long)rounds);
+    }
   }
-  unsigned long long hs[2];
+  unsigned long long hs[4];
   TSVD_CUDA(cudaMemcpy(hs, P.stats, sizeof hs, cudaMemcpyDeviceToHost));
   if (out) {
     out->rounds = rounds;
     out->pushes = (int64_t)hs[0];
     out->edge_updates = (int64_t)hs[1];
+    out->items = (int64_t)hs[2];
+    out->item_edges = (int64_t)hs[3];
+    out->kernel_ms = kernel_ms;
   }
   P.seeded = false;
   return TSVD_OK;

@@ -8,6 +8,7 @@ struct PprState {
   int32_t n = 0, nsrc = 0, sp = 0, chunks = 0;
   float *r = nullptr, *p = nullptr;  // [n][sp]
   uint32_t *tflag = nullptr;         // touched (vertex, chunk) bitset
+  uint32_t *pend = nullptr;          // parked below the current threshold level
   int64_t nwords = 0;
   int2 *front[2] = {nullptr, nullptr};
   int64_t cap = 0;
@@ -22,6 +23,7 @@ struct PprState {
   int32_t *counters = nullptr;
   int32_t *host_counters = nullptr;
   unsigned long long *stats = nullptr;
+  cudaEvent_t kev[16] = {};  // scatter-kernel timing, two per round of a check interval
 };
 
 struct PprParams {
@@ -30,10 +32,15 @@ struct PprParams {
   int undirected = 1;
   int check_every = 4;
   int64_t max_rounds = 100000;
+  int levels = 1;       // threshold schedule: rmax * ratio^(levels-1) ... rmax
+  double ratio = 8.0;
+  double cofrac = 1.0;  // co-push residues above rmax * cofrac on pushed lines
 };
 
 struct PushStats {
-  int64_t rounds = 0, pushes = 0, edge_updates = 0;
+  int64_t rounds = 0, pushes = 0, edge_updates = 0, items = 0;
+  double kernel_ms = 0;  // push_kernel + push_heavy_kernel device time
+  int64_t item_edges = 0;  // sum of deg(v) over pushed (vertex, chunk) items
 };
 
 struct PushArgs {
@@ -43,8 +50,8 @@ struct PushArgs {
   const int64_t *off;
   const int32_t *deg, *nbr;
   int32_t sp, nsrc, chunks;
-  uint32_t *tflag;
-  float alpha_f, one_minus_alpha_f, rmax_f;
+  uint32_t *tflag, *pend;
+  float alpha_f, one_minus_alpha_f, rmax_f, theta_f, co_f;
   int undirected;
   uint8_t *vmark;
   float *heavy_w;
@@ -60,7 +67,8 @@ struct PushArgs {
 };
 
 struct CollectArgs {
-  uint32_t *tflag;
+  uint32_t *tflag, *pend;
+  float theta_f;
   int64_t nwords;
   int32_t chunks, nsrc, sp;
   const float *r;

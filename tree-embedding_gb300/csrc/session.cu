@@ -155,6 +155,9 @@ extern "C" void tsvd_config_default(tsvd_config *c) {
   c->seed = 20231;
   c->device = 0;
   c->max_push_rounds = 0;
+  c->push_levels = 1;
+  c->push_ratio = 8.0;
+  c->push_cofrac = 1.0;
 }
 
 static tsvd_status session_alloc(tsvd_session *s) {
@@ -315,6 +318,9 @@ static PprParams ppr_params(const tsvd_session *s) {
   p.intdiv = s->cfg.refresh_mode == TSVD_REFRESH_INTDIV;
   p.undirected = !s->directed;
   p.max_rounds = s->cfg.max_push_rounds > 0 ? s->cfg.max_push_rounds : 1000000;
+  p.levels = std::max(1, s->cfg.push_levels);
+  p.ratio = s->cfg.push_ratio > 1.0 ? s->cfg.push_ratio : 8.0;
+  p.cofrac = s->cfg.push_cofrac;
   return p;
 }
 
@@ -384,13 +390,16 @@ static tsvd_status stage_materialize(tsvd_session *s, int iter) {
   a.stored = s->stored_dev;
   int32_t max_nc = 0;
   for (int32_t x : s->ncols_h) max_nc = std::max(max_nc, x);
+  TSVD_CUDA(cudaEventRecord(s->ev[6], s->st));
   TSVD_TRY(materialize_blocks(a, P, max_nc, s->st));
+  TSVD_CUDA(cudaEventRecord(s->ev[7], s->st));
   std::vector<unsigned long long> nn(P), ss(P);
   TSVD_CUDA(cudaMemcpyAsync(s->norm2_h.data(), s->norm2_dev, sizeof(double) * P, cudaMemcpyDeviceToHost, s->st));
   TSVD_CUDA(cudaMemcpyAsync(s->diff2_h.data(), s->diff2_dev, sizeof(double) * P, cudaMemcpyDeviceToHost, s->st));
   TSVD_CUDA(cudaMemcpyAsync(nn.data(), s->nnz_dev, sizeof(unsigned long long) * P, cudaMemcpyDeviceToHost, s->st));
   TSVD_CUDA(cudaMemcpyAsync(ss.data(), s->stored_dev, sizeof(unsigned long long) * P, cudaMemcpyDeviceToHost, s->st));
   TSVD_CUDA(cudaStreamSynchronize(s->st));
+  s->last.ms_materialize_kernel = ms_between(s->ev[6], s->ev[7]);
   // Lazy-update decision (ppr:2700-2729) or unconditional refresh (Tree_u_NC.cpp:642-668).
   const bool with_norm = iter >= s->cfg.lazy_update_start_iter;
   s->factor_now.clear();
@@ -509,6 +518,9 @@ static tsvd_status stage_ppr(tsvd_session *s, int iter, int dir) {
   s->last.push_rounds += ps.rounds;
   s->last.pushes += ps.pushes;
   s->last.push_edge_updates += ps.edge_updates;
+  s->last.push_items += ps.items;
+  s->last.ms_push_kernels += ps.kernel_ms;
+  s->last.push_item_edges += ps.item_edges;
   return TSVD_OK;
 }
 

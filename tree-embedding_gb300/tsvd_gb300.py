@@ -40,6 +40,8 @@ class Config(ctypes.Structure):
         ("dirty_frac", ctypes.c_double), ("root_scaling", ctypes.c_int32),
         ("refresh_mode", ctypes.c_int32), ("seed", ctypes.c_uint64),
         ("device", ctypes.c_int32), ("max_push_rounds", ctypes.c_int32),
+        ("push_levels", ctypes.c_int32), ("push_ratio", ctypes.c_double),
+        ("push_cofrac", ctypes.c_double),
     ]
 
 
@@ -53,7 +55,9 @@ class StepStats(ctypes.Structure):
         ("ms_insert", ctypes.c_double), ("ms_refresh", ctypes.c_double),
         ("ms_push", ctypes.c_double), ("ms_log", ctypes.c_double),
         ("ms_frpca", ctypes.c_double), ("ms_merge", ctypes.c_double),
-        ("ms_total", ctypes.c_double),
+        ("ms_total", ctypes.c_double), ("push_items", ctypes.c_int64),
+        ("ms_push_kernels", ctypes.c_double), ("ms_materialize_kernel", ctypes.c_double),
+        ("push_item_edges", ctypes.c_int64),
     ]
 
     def as_dict(self):
@@ -210,7 +214,7 @@ class Session:
                  dynamic_ppr_start_iter=100, lazy_update_start_iter=100, delta=0.3,
                  transform=TRANSFORM_LOG10_NC, dirty_rule=DIRTY_REFERENCE, dirty_frac=0.01,
                  root_scaling=ROOT_SQRT_SIGMA, refresh_mode=REFRESH_EXACT, seed=20231, device=0,
-                 max_push_rounds=0):
+                 max_push_rounds=0, push_levels=1, push_ratio=8.0, push_cofrac=1.0):
         self.sources = np.ascontiguousarray(sources, dtype=np.int32)
         c = Config()
         lib().tsvd_config_default(ctypes.byref(c))
@@ -226,6 +230,8 @@ class Session:
         c.transform, c.dirty_rule, c.dirty_frac = int(transform), int(dirty_rule), float(dirty_frac)
         c.root_scaling, c.refresh_mode = int(root_scaling), int(refresh_mode)
         c.seed, c.device, c.max_push_rounds = int(seed), int(device), int(max_push_rounds)
+        c.push_levels, c.push_ratio = int(push_levels), float(push_ratio)
+        c.push_cofrac = float(push_cofrac)
         self.cfg = c
         self.n, self.S, self.d = c.n_vertices, c.n_sources, c.rank_d
         self.n_parts, self.h, self.directed = c.n_parts, c.hierarchy_n, bool(directed)
