@@ -31,8 +31,12 @@ constexpr unsigned kFull = 0xffffffffu;
 
 // Sets the touched bit of (u, chunk c). The result is unused, so this is a
 // fire-and-forget reduction (RED.OR): no round trip on the issuing warp.
-__device__ __forceinline__ void mark_touched(uint32_t *tflag, int32_t u, int32_t c, int32_t C) {
-  int64_t idx = (int64_t)u * C + c;
+// The bitset is chunk-major (bit c * n + u): the next frontier comes out
+// grouped by chunk, so the residual lines a stretch of a push round hits lie
+// in one chunk's n * 128 bytes instead of the whole n * Sp * 4 byte state,
+// and repeated hits on a line are served by L2.
+__device__ __forceinline__ void mark_touched(uint32_t *tflag, int32_t u, int32_t c, int32_t n) {
+  int64_t idx = (int64_t)c * n + u;
   atomicOr(tflag + (idx >> 5), 1u << (idx & 31));
 }
 
@@ -79,7 +83,7 @@ __device__ __forceinline__ void scatter_range(const PushArgs &a, int32_t v, int3
       if (act) atomicAdd(a.r + (int64_t)u * a.sp + s, w);
     }
     // each lane marks the neighbour it loaded: 32 independent reductions
-    if (lane < jn) mark_touched(a.tflag, mine, c, a.chunks);
+    if (lane < jn) mark_touched(a.tflag, mine, c, a.n);
   }
 }
 
@@ -111,7 +115,7 @@ __global__ void __launch_bounds__(256) push_kernel(PushArgs a) {
     }
     if (a.theta_f > a.rmax_f && d > 0 &&
         __ballot_sync(kFull, s < a.nsrc && !act && x > a.rmax_f) && lane == 0)
-      mark_touched(a.pend, v, c, a.chunks);
+      mark_touched(a.pend, v, c, a.n);
     if (!mask) continue;
     if (d == 0) {
       // Isolated source of an undirected graph: the reference assigns
@@ -204,7 +208,7 @@ __global__ void __launch_bounds__(256) collect_kernel(CollectArgs a) {
         int b = __ffs(bits) - 1;
         bits &= bits - 1;
         int64_t idx = wi * 32 + b;
-        int32_t u = (int32_t)(idx / a.chunks), c = (int32_t)(idx % a.chunks);
+        int32_t u = (int32_t)(idx % a.n), c = (int32_t)(idx / a.n);
         if (a.deg[u] == 0) continue;
         int32_t s = c * 32 + lane;
         float x = s < a.nsrc ? __ldcg(a.r + (int64_t)u * a.sp + s) : 0.0f;
@@ -214,7 +218,7 @@ __global__ void __launch_bounds__(256) collect_kernel(CollectArgs a) {
             buf[pos] = make_int2(u, c);
           }
         } else if (a.theta_f > a.rmax_f && __ballot_sync(kFull, x > a.rmax_f)) {
-          if (lane == 0) mark_touched(a.pend, u, c, a.chunks);  // for a lower level
+          if (lane == 0) mark_touched(a.pend, u, c, a.n);  // for a lower level
         }
       }
     }
@@ -260,7 +264,7 @@ __global__ void __launch_bounds__(256) refresh_kernel(RefreshArgs a) {
       const float q = pf / jp1;                 // p_u / (j+1)
       rdelta -= q * a.inv_alpha_f;
       if (valid) atomicAdd(a.r + (int64_t)w * a.sp + s, q * a.oma_over_alpha_f);
-      if (lane == 0) mark_touched(a.tflag, w, c, a.chunks);
+      if (lane == 0) mark_touched(a.tflag, w, c, a.n);
     }
     if (any) {
       if (valid) {
@@ -272,7 +276,7 @@ __global__ void __launch_bounds__(256) refresh_kernel(RefreshArgs a) {
     // push; in exact mode it is re-examined like any touched vertex. The
     // reference's dense path skips slot 0 entirely (ppr:2086-2093).
     if ((any || (!a.intdiv && j0 == 0 && j1 > 0)) && lane == 0)
-      mark_touched(a.tflag, u, c, a.chunks);
+      mark_touched(a.tflag, u, c, a.n);
   }
 }
 
@@ -393,7 +397,7 @@ tsvd_status ppr_refresh(PprState &P, const Adjacency &A, const int32_t *sources_
                                                             P.counters + 5);
   TSVD_LAUNCH_CHECK();
   RefreshArgs ra;
-  ra.upd = P.upd; ra.nupd = P.counters + 5; ra.chunks = P.chunks; ra.nsrc = P.nsrc;
+  ra.upd = P.upd; ra.nupd = P.counters + 5; ra.n = P.n; ra.chunks = P.chunks; ra.nsrc = P.nsrc;
   ra.sp = P.sp; ra.off = A.off; ra.deg = A.deg; ra.former = A.former; ra.nbr = A.nbr;
   ra.r = P.r; ra.p = P.p; ra.tflag = P.tflag; ra.intdiv = prm.intdiv;
   ra.inv_alpha_f = (float)(1.0 / prm.alpha);
@@ -404,7 +408,7 @@ tsvd_status ppr_refresh(PprState &P, const Adjacency &A, const int32_t *sources_
   P.cur = 0;
   TSVD_CUDA(cudaMemsetAsync(P.counters + 0, 0, sizeof(int32_t), st));
   CollectArgs ca;
-  ca.tflag = P.tflag; ca.nwords = P.nwords; ca.chunks = P.chunks; ca.nsrc = P.nsrc;
+  ca.tflag = P.tflag; ca.nwords = P.nwords; ca.n = P.n; ca.chunks = P.chunks; ca.nsrc = P.nsrc;
   ca.sp = P.sp; ca.r = P.r; ca.deg = A.deg; ca.rmax_f = largest_float_not_above(prm.rmax);
   ca.theta_f = ca.rmax_f; ca.pend = P.pend;
   ca.next = P.front[0]; ca.next_count = P.counters + 0; ca.cap = P.cap;
@@ -423,7 +427,7 @@ tsvd_status ppr_push(PprState &P, const Adjacency &A, const PprParams &prm, uint
   const float rmax_f = largest_float_not_above(prm.rmax);
   PushArgs pa;
   pa.r = P.r; pa.p = P.p; pa.off = A.off; pa.deg = A.deg; pa.nbr = A.nbr;
-  pa.sp = P.sp; pa.nsrc = P.nsrc; pa.chunks = P.chunks; pa.tflag = P.tflag; pa.pend = P.pend;
+  pa.n = P.n; pa.sp = P.sp; pa.nsrc = P.nsrc; pa.chunks = P.chunks; pa.tflag = P.tflag; pa.pend = P.pend;
   pa.alpha_f = (float)prm.alpha; pa.one_minus_alpha_f = (float)(1.0 - prm.alpha);
   pa.rmax_f = rmax_f; pa.undirected = prm.undirected; pa.vmark = vmark;
   pa.co_f = prm.cofrac >= 1.0 ? rmax_f : (float)(prm.rmax * std::max(prm.cofrac, 0.0));
@@ -432,7 +436,7 @@ tsvd_status ppr_push(PprState &P, const Adjacency &A, const PprParams &prm, uint
   pa.units = P.units; pa.unit_count = P.counters + 3; pa.unit_cap = P.unit_cap;
   pa.overflow = P.counters + 4; pa.stats = P.stats;
   CollectArgs ca;
-  ca.tflag = P.tflag; ca.pend = P.pend; ca.nwords = P.nwords; ca.chunks = P.chunks;
+  ca.tflag = P.tflag; ca.pend = P.pend; ca.nwords = P.nwords; ca.n = P.n; ca.chunks = P.chunks;
   ca.nsrc = P.nsrc; ca.sp = P.sp; ca.r = P.r; ca.deg = A.deg; ca.rmax_f = rmax_f;
   ca.cap = P.cap; ca.overflow = P.counters + 4;
   const int gpush = grid_for((int64_t)1 << 30, 256, 8);

@@ -49,7 +49,7 @@ struct PushArgs {
   float *r, *p;
   const int64_t *off;
   const int32_t *deg, *nbr;
-  int32_t sp, nsrc, chunks;
+  int32_t n, sp, nsrc, chunks;
   uint32_t *tflag, *pend;
   float alpha_f, one_minus_alpha_f, rmax_f, theta_f, co_f;
   int undirected;
@@ -70,7 +70,7 @@ struct CollectArgs {
   uint32_t *tflag, *pend;
   float theta_f;
   int64_t nwords;
-  int32_t chunks, nsrc, sp;
+  int32_t n, chunks, nsrc, sp;
   const float *r;
   const int32_t *deg;
   float rmax_f;
@@ -83,7 +83,7 @@ struct CollectArgs {
 struct RefreshArgs {
   const int32_t *upd;
   const int32_t *nupd;
-  int32_t chunks, nsrc, sp;
+  int32_t n, chunks, nsrc, sp;
   const int64_t *off;
   const int32_t *deg, *former, *nbr;
   float *r, *p;
