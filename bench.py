@@ -298,11 +298,19 @@ PUSH_TRAFFIC_BYTES_PER_ITEM_EDGE = None
 
 def push_roofline(stages):
     """Roofline of the dominant kernels (push_kernel + push_heavy_kernel) over
-    the timed steps. Algorithmic bytes: per lane push 16 (residue exchange +
-    reserve read-modify-write, fp32), per lane edge update 8 (fp32 atomic
-    read-modify-write of r[u][s]), per item-neighbour 4 (neighbour id), per
-    item 20 (frontier entry, row start, degree); duration from CUDA events
-    around every launch on the session stream."""
+    the timed steps, duration from CUDA events around every launch on the
+    session stream.
+
+    Algorithmic bytes (`achieved`) follow the per-push work of the reference's
+    FIFO push: per executed push of (v, s) 8 (r_v read) + 8 (r_v write) + 16
+    (p_v read-modify-write) + 8 (row offsets), and per edge update 4
+    (neighbour id) + 16 (r_u atomic read-modify-write).
+
+    `achieved_min` counts the bytes this design has to move at least: per lane
+    push 16 (fp32 residue exchange + reserve update), per lane edge update 8
+    (fp32 atomic read-modify-write), per item-neighbour 4 (the neighbour id is
+    read once for 32 sources), per item 20 (frontier entry, row start,
+    degree)."""
     pk, _ = peaks()
     peak = float(pk.get("hbm_gbs", 6800.0))
     pushes = sum(s["pushes"] for s in stages)
@@ -311,17 +319,22 @@ def push_roofline(stages):
     iedges = sum(s["push_item_edges"] for s in stages)
     ms = sum(s["ms_push_kernels"] for s in stages)
     launches = sum(2 * s["push_rounds"] for s in stages)
-    byts = 16.0 * pushes + 8.0 * upd + 4.0 * iedges + 20.0 * items
-    achieved = byts / (ms / 1e3) / 1e9 if ms > 0 else 0.0
+    byts = 40.0 * pushes + 20.0 * upd
+    byts_min = 16.0 * pushes + 8.0 * upd + 4.0 * iedges + 20.0 * items
+    sec = ms / 1e3
+    achieved = byts / sec / 1e9 if ms > 0 else 0.0
+    achieved_min = byts_min / sec / 1e9 if ms > 0 else 0.0
     traffic = None
     if PUSH_TRAFFIC_BYTES_PER_ITEM_EDGE is not None and launches:
         traffic = PUSH_TRAFFIC_BYTES_PER_ITEM_EDGE * iedges / launches
     return {"kernel": "push_kernel+push_heavy_kernel", "bound": "hbm", "achieved": achieved,
             "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
             "algorithmic_bytes_per_launch": byts / max(1, launches),
+            "achieved_min": achieved_min, "frac_min": achieved_min / peak,
+            "min_bytes_per_launch": byts_min / max(1, launches),
             "launches": launches, "kernel_ms": ms,
             "lanes_per_item": pushes / max(1, items),
-            "peak_source": "MEASURED_PEAKS.json hbm_gbs (copy bandwidth)"}
+            "peak_source": "MEASURED_PEAKS.json hbm_gbs (copy bandwidth), of measured"}
 
 
 def aggregate(ms, edges, device=None):

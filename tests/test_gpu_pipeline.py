@@ -2,6 +2,7 @@
 against the CPU oracle on the same seeded inputs."""
 import numpy as np
 import pytest
+import scipy.sparse as sp
 
 import tsvd_gb300 as T
 import workloads as W
@@ -176,6 +177,24 @@ def test_frpca_abi_matches_oracle():
     R = (U * S) @ V.T
     Ro = (Uo * So) @ Vo[:, ::-1].T
     assert np.linalg.norm(R - Ro) / np.linalg.norm(Ro) < 1e-3
+
+
+def test_frpca_abi_repeated_and_zero_singular_values():
+    """Rank 6 < k with a triple and a double singular value: the eigensolver's
+    clustered path (equal eigenvalues, and the zero eigenvalues of the rank
+    deficient Gram) must still return an orthonormal U and the exact spectrum."""
+    rng = np.random.default_rng(5)
+    m, n, k, q = 300, 400, 10, 4
+    U0, _ = np.linalg.qr(rng.standard_normal((m, 6)))
+    V0, _ = np.linalg.qr(rng.standard_normal((n, 6)))
+    s0 = np.array([5.0, 5.0, 5.0, 2.0, 1.0, 1.0])
+    A = sp.csr_matrix((U0 * s0) @ V0.T)
+    U, S, V = T.frpca(A.indptr, A.indices, A.data, A.shape, k, q, seed=11)
+    assert np.allclose(S[:6], s0, rtol=2e-3)
+    assert np.all(S[6:] < 1e-2)
+    assert np.abs(U.T @ U - np.eye(k)).max() < 1e-3
+    assert max_principal_sine(U[:, :3], U0[:, :3]) < 1e-2
+    assert max_principal_sine(U[:, :6], U0) < 1e-2
 
 
 @pytest.mark.parametrize("directed", [False, True])

@@ -12,6 +12,7 @@
 // Columns (vertices) whose reserve has never been non-zero are left out of
 // A^T; the set only grows, so a column keeps its slot across snapshots.
 #include "blocks.h"
+#include "ppr.h"
 
 namespace tsvd {
 
@@ -90,15 +91,14 @@ __global__ void __launch_bounds__(256) materialize_kernel(MaterializeArgs a) {
   unsigned long long nnz = 0, stored = 0;
   for (int32_t c = blockIdx.x * 8 + warp; c < nc; c += gridDim.x * 8) {
     const int32_t v = a.colmap[cbase + c];
-    const float *p1 = a.p1 + (int64_t)v * a.sp;
-    const float *p2 = a.p2 ? a.p2 + (int64_t)v * a.sp : nullptr;
     const __half *orow = old + (int64_t)c * a.sp;
     __half *nrow = out + (int64_t)c * a.sp;
     const bool has_old = c < nc_old;
     for (int32_t s0 = lane * 4; s0 < a.sp; s0 += 128) {
-      float4 x = __ldcs(reinterpret_cast<const float4 *>(p1 + s0));
-      if (p2) {
-        float4 y = __ldcs(reinterpret_cast<const float4 *>(p2 + s0));
+      const int64_t cell = ppr_cell(v, s0, a.n);
+      float4 x = __ldcs(reinterpret_cast<const float4 *>(a.p1 + cell));
+      if (a.p2) {
+        float4 y = __ldcs(reinterpret_cast<const float4 *>(a.p2 + cell));
         x.x += y.x; x.y += y.y; x.z += y.z; x.w += y.w;
       }
       float xs[4] = {x.x, x.y, x.z, x.w};

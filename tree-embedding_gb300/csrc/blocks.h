@@ -7,14 +7,14 @@
 namespace tsvd {
 
 struct MaterializeArgs {
-  const float *p1;        // reserve [n][sp] (forward / undirected)
+  const float *p1;        // reserve, chunk-major (ppr_cell) (forward / undirected)
   const float *p2;        // reserve of the reverse push (directed) or null
   const int32_t *colmap;  // compacted vertex ids, block b at [b*col_dim, ...)
   const int32_t *ncols;   // current column counts
   const int32_t *ncols_old;
   const __half *const *at_old;  // accepted A^T of each block
   __half *const *at_new;        // output A^T of each block
-  int32_t sp, nsrc, col_dim;
+  int32_t n, sp, nsrc, col_dim;
   int transform;
   float rmin_f, inv_rmin_f, n_f;
   double *norm2, *diff2;

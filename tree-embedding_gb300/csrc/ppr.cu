@@ -1,19 +1,18 @@
-// Dynamic forward-push PPR for all sources at once, vertex-major state.
+// Dynamic forward-push PPR for all sources at once.
 //
-// State: r[v][s], p[v][s] (float, v-major, |S| padded to Sp) so that one warp
-// holds 32 consecutive sources of one vertex: a push of vertex v for a chunk
-// of sources is one 128-byte atomic add per neighbour.
+// State: r and p (float, |S| padded to Sp = 32 * chunks), chunk-major: cell
+// (v, s) is ((s / 32) * n + v) * 32 + s % 32. One warp holds the 32 sources of
+// one chunk of one vertex, so a push of vertex v for a chunk is one 128-byte
+// atomic add per neighbour, and the lines of one chunk are contiguous.
 //
 // Reference: the per-source FIFO push of Code/ppr_computation_store_dynamic.h
 // (nodegree_DenseDynamicForwardPush :1394-1498, nodegree_DenseDirected...
 // :2945-3030, ...Transpose :3356-3437) and its dynamic refresh (:2035-2121,
 // :3811-3898, :4133-4228). The FIFO becomes frontier-synchronous rounds:
-//   push round : every (v, chunk) in the frontier exchanges r[v][s] > rmax to
-//                zero, adds alpha*r to p[v][s] and scatters (1-alpha)*r/deg(v)
-//                to every neighbour, marking (u, chunk) as touched;
-//   collect    : every touched (u, chunk) whose residue exceeds rmax for some
-//                lane and whose degree is non-zero joins the next frontier.
-// Kernel boundaries order the two phases, so no flag/residue race exists.
+// every (v, chunk) in the frontier exchanges r[v][s] > rmax to zero, adds
+// alpha*r to p[v][s] and scatters (1-alpha)*r/deg(v) to every neighbour. The
+// next frontier is every touched (u, chunk) with some residue above rmax and
+// a non-zero degree (collect_kernel over the touched bitset).
 // The loop ends when a frontier is empty: every eligible residue <= rmax,
 // the same invariant the FIFO leaves behind.
 #include <algorithm>
@@ -69,18 +68,20 @@ __device__ void flush_stats(StatAcc acc, unsigned long long *gstats) {
   }
 }
 
-// Scatter w (per lane) of vertex v's chunk c to neighbours [j0, j1).
+// Scatter w (per lane) of vertex v's chunk c to neighbours [j0, j1):
+// fire-and-forget atomic adds (RED), and every neighbour's (u, chunk) is
+// marked in the touched bitset for collect_kernel.
 __device__ __forceinline__ void scatter_range(const PushArgs &a, int32_t v, int32_t c,
                                               bool act, float w, int32_t j0, int32_t j1) {
   const int lane = threadIdx.x & 31;
-  const int32_t s = c * 32 + lane;
+  float *rc = a.r + (int64_t)c * a.n * 32 + lane;  // r cell of (u, c * 32 + lane) = rc + 32 u
   const int32_t *nb = a.nbr + a.off[v];
   for (int32_t jb = j0; jb < j1; jb += 32) {
-    int32_t jn = min(32, j1 - jb);
-    int32_t mine = lane < jn ? __ldg(nb + jb + lane) : 0;
+    const int32_t jn = min(32, j1 - jb);
+    const int32_t mine = lane < jn ? __ldg(nb + jb + lane) : 0;
     for (int32_t t = 0; t < jn; ++t) {
-      int32_t u = __shfl_sync(kFull, mine, t);
-      if (act) atomicAdd(a.r + (int64_t)u * a.sp + s, w);
+      const int32_t u = __shfl_sync(kFull, mine, t);
+      if (act) atomicAdd(rc + (int64_t)u * 32, w);
     }
     // each lane marks the neighbour it loaded: 32 independent reductions
     if (lane < jn) mark_touched(a.tflag, mine, c, a.n);
@@ -98,7 +99,7 @@ __global__ void __launch_bounds__(256) push_kernel(PushArgs a) {
     const int32_t v = it.x, c = it.y;
     const int32_t d = a.deg[v];
     const int32_t s = c * 32 + lane;
-    float *rp = a.r + (int64_t)v * a.sp + s;
+    float *rp = a.r + ppr_cell(v, s, a.n);
     float x = __ldcg(rp);
     // push above the current level of the threshold schedule; lanes between
     // rmax and that level are parked in the pending set for a later level
@@ -121,14 +122,14 @@ __global__ void __launch_bounds__(256) push_kernel(PushArgs a) {
       // Isolated source of an undirected graph: the reference assigns
       // pi = alpha * r and keeps r (ppr:1433-1441); directed dangling
       // vertices are skipped (ppr:2971-2976).
-      if (a.undirected && act) a.p[(int64_t)v * a.sp + s] = a.alpha_f * x;
+      if (a.undirected && act) a.p[ppr_cell(v, s, a.n)] = a.alpha_f * x;
       if (a.undirected && lane == 0 && a.vmark[v] == 0) a.vmark[v] = 1;
       continue;
     }
     if (act) x = atomicExch(rp, 0.0f);
     const float w = act ? x * (a.one_minus_alpha_f / (float)d) : 0.0f;
     if (act) {
-      float *pp = a.p + (int64_t)v * a.sp + s;
+      float *pp = a.p + ppr_cell(v, s, a.n);
       *pp = fmaf(a.alpha_f, x, *pp);
     }
     if (lane == 0) {
@@ -211,7 +212,7 @@ __global__ void __launch_bounds__(256) collect_kernel(CollectArgs a) {
         int32_t u = (int32_t)(idx % a.n), c = (int32_t)(idx / a.n);
         if (a.deg[u] == 0) continue;
         int32_t s = c * 32 + lane;
-        float x = s < a.nsrc ? __ldcg(a.r + (int64_t)u * a.sp + s) : 0.0f;
+        float x = s < a.nsrc ? __ldcg(a.r + ppr_cell(u, s, a.n)) : 0.0f;
         if (__ballot_sync(kFull, x > a.theta_f)) {
           if (lane == 0) {
             int32_t pos = atomicAdd(&nbuf, 1);
@@ -249,7 +250,7 @@ __global__ void __launch_bounds__(256) refresh_kernel(RefreshArgs a) {
     const bool valid = s < a.nsrc;
     const int32_t j0 = a.former[u], j1 = a.deg[u];
     const int32_t *nb = a.nbr + a.off[u];
-    float pf = valid ? a.p[(int64_t)u * a.sp + s] : 0.0f;
+    float pf = valid ? a.p[ppr_cell(u, s, a.n)] : 0.0f;
     float rdelta = 0.0f;
     bool any = false;
     for (int32_t j = max(j0, 1); j < j1; ++j) {
@@ -263,13 +264,13 @@ __global__ void __launch_bounds__(256) refresh_kernel(RefreshArgs a) {
       }
       const float q = pf / jp1;                 // p_u / (j+1)
       rdelta -= q * a.inv_alpha_f;
-      if (valid) atomicAdd(a.r + (int64_t)w * a.sp + s, q * a.oma_over_alpha_f);
+      if (valid) atomicAdd(a.r + ppr_cell(w, s, a.n), q * a.oma_over_alpha_f);
       if (lane == 0) mark_touched(a.tflag, w, c, a.n);
     }
     if (any) {
       if (valid) {
-        a.p[(int64_t)u * a.sp + s] = pf;
-        atomicAdd(a.r + (int64_t)u * a.sp + s, rdelta);
+        a.p[ppr_cell(u, s, a.n)] = pf;
+        atomicAdd(a.r + ppr_cell(u, s, a.n), rdelta);
       }
     }
     // A formerly dangling vertex (j0 == 0) may hold residue it could not
@@ -311,12 +312,12 @@ __global__ void list_updated_kernel(const int32_t *__restrict__ deg,
 }
 
 __global__ void init_sources_kernel(const int32_t *__restrict__ sources, int32_t nsrc,
-                                    float *__restrict__ r, int32_t sp,
+                                    float *__restrict__ r, int32_t n,
                                     int2 *__restrict__ front, int32_t *__restrict__ count) {
   for (int32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < nsrc;
        k += gridDim.x * blockDim.x) {
     int32_t v = sources[k];
-    r[(int64_t)v * sp + k] = 1.0f;
+    r[ppr_cell(v, k, n)] = 1.0f;
     front[k] = make_int2(v, k / 32);
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) *count = nsrc;
@@ -385,7 +386,7 @@ tsvd_status ppr_refresh(PprState &P, const Adjacency &A, const int32_t *sources_
     TSVD_CUDA(cudaMemsetAsync(P.tflag, 0, P.nwords * sizeof(uint32_t), st));
     TSVD_CUDA(cudaMemsetAsync(P.pend, 0, P.nwords * sizeof(uint32_t), st));
     P.cur = 0;
-    init_sources_kernel<<<grid_for(P.nsrc, 256), 256, 0, st>>>(sources_dev, P.nsrc, P.r, P.sp,
+    init_sources_kernel<<<grid_for(P.nsrc, 256), 256, 0, st>>>(sources_dev, P.nsrc, P.r, P.n,
                                                                   P.front[0], P.counters + 0);
     TSVD_LAUNCH_CHECK();
     P.seeded = true;

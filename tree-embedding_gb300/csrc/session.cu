@@ -377,6 +377,7 @@ static tsvd_status stage_materialize(tsvd_session *s, int iter) {
   a.ncols_old = s->ncols_old_dev;
   a.at_old = s->at_ptrs_dev;
   a.at_new = s->at_ptrs_dev + P;
+  a.n = s->n;
   a.sp = s->sp;
   a.nsrc = s->S;
   a.col_dim = s->col_dim;
@@ -716,7 +717,7 @@ extern "C" tsvd_status tsvd_ppr_state(tsvd_session *s, int32_t transpose, int32_
   TSVD_CUDA(cudaMemcpy(tmp.data(), which ? P.p : P.r, sizeof(float) * tmp.size(),
                        cudaMemcpyDeviceToHost));
   for (int v = 0; v < s->n; ++v)
-    for (int k = 0; k < s->S; ++k) out[(size_t)k * s->n + v] = tmp[(size_t)v * s->sp + k];
+    for (int k = 0; k < s->S; ++k) out[(size_t)k * s->n + v] = tmp[ppr_cell(v, k, s->n)];
   return TSVD_OK;
 }
 
