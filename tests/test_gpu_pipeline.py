@@ -179,21 +179,40 @@ def test_frpca_abi_matches_oracle():
     assert np.linalg.norm(R - Ro) / np.linalg.norm(Ro) < 1e-3
 
 
-def test_frpca_abi_repeated_and_zero_singular_values():
-    """Rank 6 < k with a triple and a double singular value: the eigensolver's
-    clustered path (equal eigenvalues, and the zero eigenvalues of the rank
-    deficient Gram) must still return an orthonormal U and the exact spectrum."""
-    rng = np.random.default_rng(5)
+def _lowrank_exact(m, n, s, seed):
+    rng = np.random.default_rng(seed)
+    U0, _ = np.linalg.qr(rng.standard_normal((m, len(s))))
+    V0, _ = np.linalg.qr(rng.standard_normal((n, len(s))))
+    return sp.csr_matrix((U0 * s) @ V0.T), U0
+
+
+def test_frpca_abi_repeated_singular_values():
+    """A triple and a double singular value at the top of a full-rank
+    spectrum: equal eigenvalues of the Gram form a cluster, whose vectors
+    must still come out orthonormal and span the right subspaces."""
     m, n, k, q = 300, 400, 10, 4
-    U0, _ = np.linalg.qr(rng.standard_normal((m, 6)))
-    V0, _ = np.linalg.qr(rng.standard_normal((n, 6)))
-    s0 = np.array([5.0, 5.0, 5.0, 2.0, 1.0, 1.0])
-    A = sp.csr_matrix((U0 * s0) @ V0.T)
+    s = np.concatenate([[5.0, 5.0, 5.0, 2.0, 1.0, 1.0], 0.5 * 0.9 ** np.arange(40)])
+    A, U0 = _lowrank_exact(m, n, s, seed=5)
     U, S, V = T.frpca(A.indptr, A.indices, A.data, A.shape, k, q, seed=11)
-    assert np.allclose(S[:6], s0, rtol=2e-3)
-    assert np.all(S[6:] < 1e-2)
+    assert np.allclose(S[:6], s[:6], rtol=2e-3)
     assert np.abs(U.T @ U - np.eye(k)).max() < 1e-3
     assert max_principal_sine(U[:, :3], U0[:, :3]) < 1e-2
+    assert max_principal_sine(U[:, :6], U0[:, :6]) < 1e-2
+
+
+def test_frpca_abi_rank_deficient():
+    """Rank 6 < k: the leading 6 singular triplets are exact and orthonormal,
+    the rest are (numerically) zero; nothing is NaN. The directions of the
+    zero singular values are arbitrary (the reference's eigSVD divides by
+    them), so only their singular values are checked."""
+    m, n, k, q = 300, 400, 10, 4
+    s = np.array([5.0, 5.0, 5.0, 2.0, 1.0, 1.0])
+    A, U0 = _lowrank_exact(m, n, s, seed=6)
+    U, S, V = T.frpca(A.indptr, A.indices, A.data, A.shape, k, q, seed=11)
+    assert np.isfinite(U).all() and np.isfinite(S).all() and np.isfinite(V).all()
+    assert np.allclose(S[:6], s, rtol=2e-3)
+    assert np.all(S[6:] < 1e-2)
+    assert np.abs(U[:, :6].T @ U[:, :6] - np.eye(6)).max() < 1e-3
     assert max_principal_sine(U[:, :6], U0) < 1e-2
 
 

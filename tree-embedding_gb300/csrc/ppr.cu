@@ -28,44 +28,29 @@ namespace {
 constexpr int kHeavy = 1024;  // neighbours per warp work unit for hub vertices
 constexpr unsigned kFull = 0xffffffffu;
 
-// Sets the touched bit of (u, chunk c). The result is unused, so this is a
-// fire-and-forget reduction (RED.OR): no round trip on the issuing warp.
-// The bitset is chunk-major (bit c * n + u): the next frontier comes out
-// grouped by chunk, so the residual lines a stretch of a push round hits lie
-// in one chunk's n * 128 bytes instead of the whole n * Sp * 4 byte state,
-// and repeated hits on a line are served by L2.
-__device__ __forceinline__ void mark_touched(uint32_t *tflag, int32_t u, int32_t c, int32_t n) {
-  int64_t idx = (int64_t)c * n + u;
-  atomicOr(tflag + (idx >> 5), 1u << (idx & 31));
+// Sets the bit of (u, chunk c) in a chunk-major bitset (bit c * n + u). The
+// result is unused, so this is a fire-and-forget reduction (RED.OR). The
+// touched set of a whole round (n * chunks bits) stays in L2, and chunk-major
+// order makes the next frontier come out grouped by chunk, so the residual
+// lines a stretch of a push round hits lie in one chunk's n * 128 bytes.
+__device__ __forceinline__ void mark_pair(uint32_t *bits, int32_t u, int32_t c, int32_t n) {
+  const int64_t idx = (int64_t)c * n + u;
+  atomicOr(bits + (idx >> 5), 1u << (idx & 31));
 }
 
 struct StatAcc {
   unsigned long long pushes = 0, upd = 0, items = 0, iedges = 0;
 };
 
-__device__ void flush_stats(StatAcc acc, unsigned long long *gstats) {
-  __shared__ unsigned long long sp[32], su[32], si[32], se[32];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  unsigned long long a = acc.pushes, b = acc.upd, c = acc.items, e = acc.iedges;
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    a += __shfl_down_sync(kFull, a, o);
-    b += __shfl_down_sync(kFull, b, o);
-    c += __shfl_down_sync(kFull, c, o);
-    e += __shfl_down_sync(kFull, e, o);
-  }
-  if (lane == 0) { sp[warp] = a; su[warp] = b; si[warp] = c; se[warp] = e; }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    unsigned long long ta = 0, tb = 0, tc = 0, te = 0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
-      ta += sp[w]; tb += su[w]; tc += si[w]; te += se[w];
-    }
-    if (ta) atomicAdd(&gstats[0], ta);
-    if (tb) atomicAdd(&gstats[1], tb);
-    if (tc) atomicAdd(&gstats[2], tc);
-    if (te) atomicAdd(&gstats[3], te);
-  }
+// Only lane 0 of a warp counts; it adds its counts to one of kStatSlots
+// slots (no block barrier, so a warp that runs out of items leaves at once).
+__device__ __forceinline__ void flush_stats(const StatAcc &acc, unsigned long long *gstats) {
+  if ((threadIdx.x & 31) != 0) return;
+  unsigned long long *slot = gstats + (blockIdx.x % kStatSlots) * 4;
+  if (acc.pushes) atomicAdd(slot + 0, acc.pushes);
+  if (acc.upd) atomicAdd(slot + 1, acc.upd);
+  if (acc.items) atomicAdd(slot + 2, acc.items);
+  if (acc.iedges) atomicAdd(slot + 3, acc.iedges);
 }
 
 // Scatter w (per lane) of vertex v's chunk c to neighbours [j0, j1):
@@ -84,7 +69,7 @@ __device__ __forceinline__ void scatter_range(const PushArgs &a, int32_t v, int3
       if (act) atomicAdd(rc + (int64_t)u * 32, w);
     }
     // each lane marks the neighbour it loaded: 32 independent reductions
-    if (lane < jn) mark_touched(a.tflag, mine, c, a.n);
+    if (lane < jn) mark_pair(a.tflag, mine, c, a.n);
   }
 }
 
@@ -94,9 +79,11 @@ __global__ void __launch_bounds__(256) push_kernel(PushArgs a) {
   const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
   const int32_t nitems = *a.front_count;
   StatAcc acc;
+  int2 it = gw < nitems ? __ldg(a.front + gw) : make_int2(0, 0);
   for (int64_t i = gw; i < nitems; i += nw) {
-    int2 it = a.front[i];
     const int32_t v = it.x, c = it.y;
+    // the warp's next item is loaded while this one is pushed
+    it = i + nw < nitems ? __ldg(a.front + i + nw) : make_int2(0, 0);
     const int32_t d = a.deg[v];
     const int32_t s = c * 32 + lane;
     float *rp = a.r + ppr_cell(v, s, a.n);
@@ -116,7 +103,7 @@ __global__ void __launch_bounds__(256) push_kernel(PushArgs a) {
     }
     if (a.theta_f > a.rmax_f && d > 0 &&
         __ballot_sync(kFull, s < a.nsrc && !act && x > a.rmax_f) && lane == 0)
-      mark_touched(a.pend, v, c, a.n);
+      mark_pair(a.pend, v, c, a.n);
     if (!mask) continue;
     if (d == 0) {
       // Isolated source of an undirected graph: the reference assigns
@@ -189,7 +176,7 @@ __global__ void __launch_bounds__(256) push_heavy_kernel(PushArgs a) {
 }
 
 // Scan the touched bitset; for each touched (u, chunk) with some residue
-// above rmax and deg(u) > 0, append it to the next frontier. Clears the bits.
+// above theta and deg(u) > 0, append it to the next frontier. Clears the bits.
 __global__ void __launch_bounds__(256) collect_kernel(CollectArgs a) {
   __shared__ int2 buf[2048];
   __shared__ int32_t nbuf, gbase;
@@ -200,26 +187,23 @@ __global__ void __launch_bounds__(256) collect_kernel(CollectArgs a) {
     if (threadIdx.x == 0) nbuf = 0;
     __syncthreads();
     for (int k = 0; k < 8; ++k) {
-      int64_t wi = w0 + warp * 8 + k;
+      const int64_t wi = w0 + warp * 8 + k;
       if (wi >= a.nwords) break;
       uint32_t bits = __ldcg(a.tflag + wi);
       if (!bits) continue;
       if (lane == 0) a.tflag[wi] = 0;
       while (bits) {
-        int b = __ffs(bits) - 1;
+        const int b = __ffs(bits) - 1;
         bits &= bits - 1;
-        int64_t idx = wi * 32 + b;
-        int32_t u = (int32_t)(idx % a.n), c = (int32_t)(idx / a.n);
+        const int64_t idx = wi * 32 + b;
+        const int32_t u = (int32_t)(idx % a.n), c = (int32_t)(idx / a.n);
         if (a.deg[u] == 0) continue;
-        int32_t s = c * 32 + lane;
-        float x = s < a.nsrc ? __ldcg(a.r + ppr_cell(u, s, a.n)) : 0.0f;
+        const int32_t s = c * 32 + lane;
+        const float x = s < a.nsrc ? __ldcg(a.r + ppr_cell(u, s, a.n)) : 0.0f;
         if (__ballot_sync(kFull, x > a.theta_f)) {
-          if (lane == 0) {
-            int32_t pos = atomicAdd(&nbuf, 1);
-            buf[pos] = make_int2(u, c);
-          }
+          if (lane == 0) buf[atomicAdd(&nbuf, 1)] = make_int2(u, c);
         } else if (a.theta_f > a.rmax_f && __ballot_sync(kFull, x > a.rmax_f)) {
-          if (lane == 0) mark_touched(a.pend, u, c, a.n);  // for a lower level
+          if (lane == 0) mark_pair(a.pend, u, c, a.n);  // for a lower level
         }
       }
     }
@@ -227,7 +211,7 @@ __global__ void __launch_bounds__(256) collect_kernel(CollectArgs a) {
     if (threadIdx.x == 0) gbase = nbuf ? atomicAdd(a.next_count, nbuf) : 0;
     __syncthreads();
     for (int i = threadIdx.x; i < nbuf; i += blockDim.x) {
-      int64_t dst = (int64_t)gbase + i;
+      const int64_t dst = (int64_t)gbase + i;
       if (dst < a.cap) a.next[dst] = buf[i];
       else atomicExch(a.overflow, 1);
     }
@@ -265,7 +249,7 @@ __global__ void __launch_bounds__(256) refresh_kernel(RefreshArgs a) {
       const float q = pf / jp1;                 // p_u / (j+1)
       rdelta -= q * a.inv_alpha_f;
       if (valid) atomicAdd(a.r + ppr_cell(w, s, a.n), q * a.oma_over_alpha_f);
-      if (lane == 0) mark_touched(a.tflag, w, c, a.n);
+      if (lane == 0) mark_pair(a.tflag, w, c, a.n);
     }
     if (any) {
       if (valid) {
@@ -277,7 +261,7 @@ __global__ void __launch_bounds__(256) refresh_kernel(RefreshArgs a) {
     // push; in exact mode it is re-examined like any touched vertex. The
     // reference's dense path skips slot 0 entirely (ppr:2086-2093).
     if ((any || (!a.intdiv && j0 == 0 && j1 > 0)) && lane == 0)
-      mark_touched(a.tflag, u, c, a.n);
+      mark_pair(a.tflag, u, c, a.n);
   }
 }
 
@@ -286,7 +270,7 @@ __global__ void unpark_kernel(uint32_t *__restrict__ tflag, uint32_t *__restrict
                               int64_t nwords) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nwords;
        i += (int64_t)gridDim.x * blockDim.x) {
-    uint32_t b = pend[i];
+    const uint32_t b = pend[i];
     if (b) {
       tflag[i] |= b;
       pend[i] = 0;
@@ -357,7 +341,7 @@ tsvd_status ppr_alloc(PprState &P, int32_t n, int32_t nsrc, int32_t sp) {
   TSVD_CUDA(cudaMalloc(&P.upd, (size_t)n * sizeof(int32_t)));
   TSVD_CUDA(cudaMalloc(&P.counters, 16 * sizeof(int32_t)));
   TSVD_CUDA(cudaMemset(P.counters, 0, 16 * sizeof(int32_t)));
-  TSVD_CUDA(cudaMalloc(&P.stats, 4 * sizeof(unsigned long long)));
+  TSVD_CUDA(cudaMalloc(&P.stats, kStatSlots * 4 * sizeof(unsigned long long)));
   TSVD_CUDA(cudaMallocHost(&P.host_counters, 16 * sizeof(int32_t)));
   for (auto &e : P.kev) TSVD_CUDA(cudaEventCreate(&e));
   return TSVD_OK;
@@ -423,7 +407,7 @@ tsvd_status ppr_refresh(PprState &P, const Adjacency &A, const int32_t *sources_
 tsvd_status ppr_push(PprState &P, const Adjacency &A, const PprParams &prm, uint8_t *vmark,
                      cudaStream_t st, PushStats *out) {
   if (!P.seeded) return fail(TSVD_ERR_STATE, "push before refresh");
-  TSVD_CUDA(cudaMemsetAsync(P.stats, 0, 4 * sizeof(unsigned long long), st));
+  TSVD_CUDA(cudaMemsetAsync(P.stats, 0, kStatSlots * 4 * sizeof(unsigned long long), st));
   TSVD_CUDA(cudaMemsetAsync(P.counters + 4, 0, sizeof(int32_t), st));
   const float rmax_f = largest_float_not_above(prm.rmax);
   PushArgs pa;
@@ -496,8 +480,9 @@ tsvd_status ppr_push(PprState &P, const Adjacency &A, const PprParams &prm, uint
         return fail(TSVD_ERR_TIMEOUT, "push: %lld rounds without convergence", (long long)rounds);
     }
   }
-  unsigned long long hs[4];
-  TSVD_CUDA(cudaMemcpy(hs, P.stats, sizeof hs, cudaMemcpyDeviceToHost));
+  unsigned long long slots[kStatSlots * 4], hs[4] = {0, 0, 0, 0};
+  TSVD_CUDA(cudaMemcpy(slots, P.stats, sizeof slots, cudaMemcpyDeviceToHost));
+  for (int k = 0; k < kStatSlots * 4; ++k) hs[k % 4] += slots[k];
   if (out) {
     out->rounds = rounds;
     out->pushes = (int64_t)hs[0];

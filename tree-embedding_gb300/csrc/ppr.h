@@ -11,12 +11,14 @@ __host__ __device__ __forceinline__ int64_t ppr_cell(int32_t v, int32_t s, int32
   return ((int64_t)(s >> 5) * n + v) * 32 + (s & 31);
 }
 
+constexpr int kStatSlots = 64;  // push counters are spread over this many slots
+
 struct PprState {
   int32_t n = 0, nsrc = 0, sp = 0, chunks = 0;
   float *r = nullptr, *p = nullptr;  // [chunks][n][32], see ppr_cell
-  uint32_t *tflag = nullptr;         // touched (vertex, chunk) bitset
+  uint32_t *tflag = nullptr;         // touched (vertex, chunk) bitset, chunk-major
   uint32_t *pend = nullptr;          // parked below the current threshold level
-  int64_t nwords = 0;
+  int64_t nwords = 0;                // words of either bitset
   int2 *front[2] = {nullptr, nullptr};
   int64_t cap = 0;
   int cur = 0;
@@ -29,7 +31,7 @@ struct PprState {
   int32_t *upd = nullptr;
   int32_t *counters = nullptr;
   int32_t *host_counters = nullptr;
-  unsigned long long *stats = nullptr;
+  unsigned long long *stats = nullptr;  // [kStatSlots][4]
   cudaEvent_t kev[16] = {};  // scatter-kernel timing, two per round of a check interval
 };
 
