@@ -290,10 +290,13 @@ def run_reference(args):
     print(json.dumps(line))
 
 
-# Per-launch DRAM traffic of the push scatter kernels measured by ncu on the
-# scaled case (profiles/push_kernel_rmat-d.md), per pushed item-neighbour, used to
-# scale `traffic` to a full launch; None until such a capture exists.
-PUSH_TRAFFIC_BYTES_PER_ITEM_EDGE = None
+# DRAM bytes (read + write) of push_kernel + push_heavy_kernel per pushed
+# item-neighbour (one 128-byte residual-line atomic), from one ncu capture of
+# every push launch of a timed rmat-d-2.7m snapshot (dram__bytes_read.sum +
+# dram__bytes_write.sum, one pass): 2310.7 GB over 1.474e10 item-neighbours
+# (profiles/push_kernel_rmat-d-2.7m.md). `traffic` scales it to the launches
+# of the run being reported.
+PUSH_TRAFFIC_BYTES_PER_ITEM_EDGE = 156.8
 
 
 def push_roofline(stages):
@@ -390,6 +393,8 @@ def main():
             "push_rounds_mean": float(np.mean([s["push_rounds"] for s in res["stages"]])),
             "pushes_mean": float(np.mean([s["pushes"] for s in res["stages"]])),
             "push_edge_updates_mean": float(np.mean([s["push_edge_updates"] for s in res["stages"]])),
+            "push_items_mean": float(np.mean([s["push_items"] for s in res["stages"]])),
+            "push_item_edges_mean": float(np.mean([s["push_item_edges"] for s in res["stages"]])),
             "ms_materialize_kernel_mean": float(np.mean([s["ms_materialize_kernel"] for s in res["stages"]])),
             "dirty_blocks_mean": float(np.mean([s["dirty_blocks"] for s in res["stages"]]))}
     line["roofline"] = push_roofline(res["stages"])
