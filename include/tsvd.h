@@ -170,6 +170,8 @@ typedef struct tsvd_config {
   int32_t push_levels;      /* threshold schedule: push r > rmax*ratio^k, k = L-1..0  */
   double push_ratio;        /* (1 level = the plain rmax test)                      */
   double push_cofrac;       /* co-push residues > rmax*cofrac on lines being pushed  */
+  int32_t lp_right_factor;  /* 1: after every snapshot, V_b = A_b^T U for each block  */
+                            /* refreshed in it (LP drivers; needs TSVD_ROOT_U)        */
 } tsvd_config;
 
 /* Fills the reference's defaults (Tree_u_NC, run.sh: alpha .5, q 12, ...). */
@@ -211,8 +213,31 @@ typedef struct tsvd_step_stats {
   double ms_push_kernels;   /* device time of the push scatter kernels            */
   double ms_materialize_kernel; /* device time of the block materialization      */
   int64_t push_item_edges;  /* sum of deg(v) over pushed items (neighbour-list reads) */
+  double ms_lp;             /* LP right factor of the refreshed blocks            */
 } tsvd_step_stats;
 tsvd_status tsvd_session_last_stats(tsvd_session *s, tsvd_step_stats *out);
+
+/* ---- link prediction (LP drivers) ---------------------------------------
+ * Replaces mkl_right_matrix_multiplication_without_norm
+ * (Code/Tree_u_LP.cpp:291-407; Tree_d_LP.cpp) and the scoring loop of the LP
+ * drivers (Tree_u_LP.cpp:1046-1122; degree-scaled variant
+ * ppr_computation_store_dynamic.h:7600-7779). With cfg.lp_right_factor, every
+ * snapshot computes V_b = A_b^T U for each block refreshed in it, with U the
+ * root factor of that snapshot, and keeps that U beside V_b; blocks that are
+ * not refreshed keep both (the reference's left_matrix_U_cache). */
+
+/* V: n_vertices x rank_d row-major (host). Rows of vertices whose block was
+ * never refreshed, or whose column never held a non-zero, are zero. */
+tsvd_status tsvd_lp_right_factor(tsvd_session *s, float *v_out);
+/* score[k] = U_b[row(i)] . V[j] for the pair (i, j) = (pairs[2k], pairs[2k+1]),
+ * i a source, b the block of j, U_b the root factor V_b was computed with;
+ * times outdeg(i) * indeg(j) (deg(i) * deg(j) undirected) if degree_scaled. */
+tsvd_status tsvd_lp_scores(tsvd_session *s, const int32_t *pairs, int64_t m,
+                           int32_t degree_scaled, double *scores);
+/* Fraction of positives among the k highest scores (ties: lower index first);
+ * Tree_u_LP.cpp:1104-1122 with k = sample_m. */
+tsvd_status tsvd_lp_precision(const double *scores, const uint8_t *positive, int64_t m,
+                              int64_t k, double *precision);
 
 /* ---- granular PPR-store interface (the reference's thread entry points) --- */
 /* a1: append edges to the device adjacency (both directions for undirected,

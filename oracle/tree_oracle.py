@@ -11,6 +11,10 @@ module, as the checker. It restates the reference's algorithm literally:
                          eigSVD (:99-136), in float64 (numpy/scipy LAPACK)
   block factor/residual  Code/Tree_u_NC.cpp:139-204 (dense residual, as there)
   merge ................ Code/Tree_u_NC.cpp:723-850 (LAPACK gesvd via numpy)
+  LP right factor ...... Code/Tree_u_LP.cpp:291-407 (V_b = A_b^T U per updated
+                         block), U cache per block :1002-1038, scores and
+                         precision :1046-1122, degree-scaled scores
+                         Code/ppr_computation_store_dynamic.h:7704-7755
 
 The reference seeds its Gaussian test matrix from time(NULL)
 (Code/matrix_vector_functions_intel_mkl.c:495); the oracle and the GPU both
@@ -107,7 +111,7 @@ class OracleTreeSVD:
                  hierarchy_n=2, rank_d=128, oversample=5, passes_q=12,
                  dynamic_ppr_start_iter=100, lazy_update_start_iter=100, delta=0.3,
                  transform=TRANSFORM_LOG10_NC, dirty_rule=DIRTY_REFERENCE, dirty_frac=0.01,
-                 root_scaling=0, refresh_mode=0, seed=20231, threads=1):
+                 root_scaling=0, refresh_mode=0, seed=20231, threads=1, lp_right_factor=False):
         self.n, self.directed = int(n), bool(directed)
         self.sources = np.ascontiguousarray(sources, dtype=np.int32)
         self.S = len(self.sources)
@@ -140,6 +144,9 @@ class OracleTreeSVD:
         self.iter = 0
         self.push_counts = (0, 0)
         self.last_factorized = []
+        self.lp = bool(lp_right_factor)
+        self.lp_V = np.zeros((n, rank_d))       # V_matrix (zero where never computed)
+        self.lp_U = [None] * n_parts            # left_matrix_U_cache per block
 
     def block_cols(self, b):
         c0 = b * self.col_dim
@@ -237,4 +244,41 @@ class OracleTreeSVD:
         self.last_factorized = todo
         if todo:
             self.merge_stage(todo)
+        if self.lp and todo and self.embedding is not None:
+            self.lp_stage()
         return self.embedding
+
+    def lp_stage(self):
+        """Right factor of every block updated in this snapshot with this
+        snapshot's root U (Tree_u_LP.cpp:1040-1044 -> :291-407)."""
+        for b in range(self.P):
+            if not self.dirty[b]:
+                continue
+            c0, c1 = self.block_cols(b)
+            self.lp_V[c0:c1] = self.accepted[b].T @ self.embedding
+            self.lp_U[b] = self.embedding.copy()
+
+
+def lp_scores(lp_U, lp_V, sources, col_dim, n_parts, pairs, degree_scaled=False,
+              deg_i=None, deg_j=None):
+    """score(i, j) = U_b[row(i)] . V[j] with U_b the root factor block b(j)'s
+    V rows were computed with (Tree_u_LP.cpp:1051-1070); times
+    outdeg(i) * indeg(j) when degree_scaled (ppr:7725, 7749)."""
+    row = {int(v): k for k, v in enumerate(sources)}
+    out = np.zeros(len(pairs))
+    for k, (i, j) in enumerate(np.asarray(pairs).reshape(-1, 2)):
+        b = min(int(j) // col_dim, n_parts - 1)
+        U = lp_U[b]
+        sc = 0.0 if U is None else float(np.dot(U[row[int(i)]], lp_V[int(j)]))
+        if degree_scaled:
+            sc *= float(deg_i[i]) * float(deg_j[j])
+        out[k] = sc
+    return out
+
+
+def lp_precision(scores, positive, k):
+    """Positives among the k highest scores over k (Tree_u_LP.cpp:1104-1122);
+    ties go to the lower index."""
+    scores = np.asarray(scores, dtype=np.float64)
+    order = np.lexsort((np.arange(len(scores)), -scores))
+    return float(np.count_nonzero(np.asarray(positive)[order[:k]])) / k

@@ -115,3 +115,16 @@ def test_gaussian_is_standard_normal_and_matches_oracle():
     assert np.array_equal(g, g.astype(np.float16).astype(np.float64))
     for (r, c) in [(0, 0), (0, 1), (17, 132), (1999, 64)]:
         assert T.gaussian(20231, 5, r, c) == g[r, c]
+
+
+def test_lp_precision_matches_oracle_including_ties():
+    from oracle.tree_oracle import lp_precision
+    rng = np.random.default_rng(3)
+    for m, k in [(10, 3), (1000, 100), (257, 257)]:
+        scores = np.round(rng.standard_normal(m), 1)  # many ties
+        pos = (rng.random(m) < 0.3).astype(np.uint8)
+        assert T.lp_precision(scores, pos, k) == pytest.approx(lp_precision(scores, pos, k))
+    with pytest.raises(T.TsvdError):
+        T.lp_precision(np.zeros(3), np.zeros(3, np.uint8), 4)
+    with pytest.raises(T.TsvdError):
+        T.lp_precision(np.zeros(3), np.zeros(3, np.uint8), 0)

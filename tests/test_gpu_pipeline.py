@@ -7,7 +7,8 @@ import scipy.sparse as sp
 import tsvd_gb300 as T
 import workloads as W
 from oracle import native
-from oracle.tree_oracle import OracleTreeSVD, frpca as oracle_frpca, gaussian_matrix, log_transform
+from oracle.tree_oracle import (OracleTreeSVD, frpca as oracle_frpca, gaussian_matrix,
+                                log_transform, lp_scores)
 
 from helpers import (gap_index, gram_rel_err, max_principal_sine, push_identity_residual,
                      residual_error_bound, transition)
@@ -257,3 +258,51 @@ def test_session_matches_oracle_pipeline(directed):
             _, sig = s.tree_factor(0)
             assert np.allclose(sig[:16], o.sigma[0][:16], rtol=1e-3)
             assert gram_rel_err(emb, emb_o) < 5e-3
+
+
+@pytest.mark.parametrize("directed", [False, True])
+def test_lp_right_factor_and_scores(directed):
+    """LP drivers: V_b = A_b^T U for the blocks refreshed in a snapshot (U that
+    snapshot's root factor, kept beside V_b), untouched for the others; pair
+    scores U_b[row(i)] . V[j], plain and degree-scaled, against the oracle's
+    restatement on the GPU's own blocks and factors."""
+    cfg = small_cfg(directed, n=6000, m=40000, sources=64, n_parts=4, rank_d=32, snapshots=4)
+    _, snaps, src = W.build(cfg, seed=31)
+    kw = W.session_kwargs(cfg, dynamic_start=2, lazy_start=2)
+    kw.update(transform=T.TRANSFORM_LOG10_LP, root_scaling=T.ROOT_U,
+              dirty_rule=T.DIRTY_FROBENIUS, dirty_frac=0.3 if directed else 0.15,
+              lp_right_factor=True)
+    P, cd = cfg["n_parts"], cfg["n"] // cfg["n_parts"]
+    rng = np.random.default_rng(7)
+    lp_U = [None] * P
+    V_prev = None
+    clean_seen = False
+    with T.Session(cfg["n"], src, **kw) as s:
+        for e in snaps:
+            s.step(e)
+            U = s.embedding()
+            assert np.abs(U.T @ U - np.eye(cfg["rank_d"])).max() < 5e-3  # root U (fp32 M V S^-1)
+            V = s.lp_right_factor().astype(np.float64)
+            dirty = s.block_info()["dirty"]
+            for b in range(P):
+                c0 = b * cd
+                c1 = cfg["n"] if b == P - 1 else c0 + cd
+                if dirty[b]:
+                    ref = s.block_dense(b).astype(np.float64).T @ U
+                    assert np.abs(V[c0:c1] - ref).max() <= 1e-4 * max(np.abs(ref).max(), 1e-30)
+                    lp_U[b] = U.copy()
+                else:
+                    clean_seen = True
+                    assert np.array_equal(V[c0:c1], V_prev[c0:c1])
+            V_prev = V
+            pairs = np.stack([rng.choice(src, 500), rng.integers(0, cfg["n"], 500)], 1)
+            deg_i, _ = s.degrees(0)
+            deg_j, _ = s.degrees(1 if directed else 0)
+            for scaled in (False, True):
+                got = s.lp_scores(pairs, degree_scaled=scaled)
+                ref = lp_scores(lp_U, V, src, cd, P, pairs, scaled, deg_i, deg_j)
+                assert np.allclose(got, ref, rtol=1e-9, atol=1e-12 * max(np.abs(ref).max(), 1.0))
+        not_a_source = int(np.setdiff1d(np.arange(cfg["n"]), src)[0])
+        with pytest.raises(T.TsvdError):
+            s.lp_scores(np.array([[not_a_source, 0]]))
+    assert clean_seen  # the lazy rule kept some block's V and U across a snapshot

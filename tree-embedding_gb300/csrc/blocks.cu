@@ -20,9 +20,11 @@ namespace {
 
 constexpr unsigned kFull = 0xffffffffu;
 
-// Append the block's newly non-zero vertices (vmark == 1) in vertex order.
+// Append the block's newly non-zero vertices (vmark == 1) in vertex order;
+// colpos (optional) receives each appended vertex's compacted column.
 __global__ void __launch_bounds__(1024) colmap_update_kernel(uint8_t *__restrict__ vmark,
                                                              int32_t *__restrict__ colmap,
+                                                             int32_t *__restrict__ colpos,
                                                              int32_t *__restrict__ ncols,
                                                              int32_t n, int32_t col_dim,
                                                              int32_t nparts) {
@@ -46,7 +48,9 @@ __global__ void __launch_bounds__(1024) colmap_update_kernel(uint8_t *__restrict
       total += warp_sums[w];
     }
     if (f) {
-      colmap[v0 + base + before + __popc(m & ((1u << lane) - 1u))] = v;
+      const int32_t c = base + before + __popc(m & ((1u << lane) - 1u));
+      colmap[v0 + c] = v;
+      if (colpos) colpos[v] = c;
       vmark[v] = 2;
     }
     __syncthreads();
@@ -155,9 +159,9 @@ __global__ void __launch_bounds__(256) materialize_kernel(MaterializeArgs a) {
 
 }  // namespace
 
-tsvd_status colmap_update(uint8_t *vmark, int32_t *colmap, int32_t *ncols, int32_t n,
-                          int32_t col_dim, int32_t nparts, cudaStream_t st) {
-  colmap_update_kernel<<<nparts, 1024, 0, st>>>(vmark, colmap, ncols, n, col_dim, nparts);
+tsvd_status colmap_update(uint8_t *vmark, int32_t *colmap, int32_t *colpos, int32_t *ncols,
+                          int32_t n, int32_t col_dim, int32_t nparts, cudaStream_t st) {
+  colmap_update_kernel<<<nparts, 1024, 0, st>>>(vmark, colmap, colpos, ncols, n, col_dim, nparts);
   TSVD_LAUNCH_CHECK();
   return TSVD_OK;
 }

@@ -21,8 +21,8 @@ struct MaterializeArgs {
   unsigned long long *nnz, *stored;
 };
 
-tsvd_status colmap_update(uint8_t *vmark, int32_t *colmap, int32_t *ncols, int32_t n,
-                          int32_t col_dim, int32_t nparts, cudaStream_t st);
+tsvd_status colmap_update(uint8_t *vmark, int32_t *colmap, int32_t *colpos, int32_t *ncols,
+                          int32_t n, int32_t col_dim, int32_t nparts, cudaStream_t st);
 tsvd_status materialize_blocks(const MaterializeArgs &a, int nparts, int32_t max_nc,
                                cudaStream_t st);
 

@@ -13,6 +13,14 @@
 // six significant digits. --compat reproduces the reference's reader (last
 // pair of a file repeated when whitespace follows it) and its integer-division
 // refresh; without it the exact refresh is used.
+//
+// The LP modes follow Tree_u_LP.cpp / Tree_d_LP.cpp instead: inputs from
+// DY_LP_Dataset/<queryname>/ (config.txt and the <queryname>-Pos_LP_Test.txt /
+// -Neg_LP_Test.txt pairs, :473, :617-638), the LOG10_LP transform, the root
+// factor U, and after every snapshot the right factor of the refreshed blocks
+// and "link prediction precision: P", the share of positive pairs among the
+// sample_m best-scored test pairs (:1040-1122); no embedding file is written.
+#include <algorithm>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -58,11 +66,12 @@ int main(int argc, char **argv) {
     if (!std::strcmp(argv[i], "--compat")) compat = true;
     else if (!std::strcmp(argv[i], "--device") && i + 1 < argc) device = std::atoi(argv[++i]);
   }
+  const std::string dataset = std::string(lp ? "DY_LP_Dataset/" : "DY_Dataset/") + queryname + "/";
   std::vector<std::string> shots;
   {
-    std::ifstream cfg(("DY_Dataset/" + queryname + "/config.txt").c_str());
+    std::ifstream cfg((dataset + "config.txt").c_str());
     if (!cfg) {
-      std::fprintf(stderr, "tree_svd: cannot read DY_Dataset/%s/config.txt\n", queryname.c_str());
+      std::fprintf(stderr, "tree_svd: cannot read %sconfig.txt\n", dataset.c_str());
       return 1;
     }
     std::string line;
@@ -98,6 +107,35 @@ int main(int argc, char **argv) {
   c.root_scaling = lp ? TSVD_ROOT_U : TSVD_ROOT_SQRT_SIGMA;
   c.refresh_mode = compat ? TSVD_REFRESH_INTDIV : TSVD_REFRESH_EXACT;
   c.device = device;
+  c.lp_right_factor = lp ? 1 : 0;
+  // LP test pairs: both files as sets, positives first (Tree_u_LP.cpp:617-638);
+  // sample_m counts every read of the positive file, including the repeated
+  // last pair of the reference's reader under --compat.
+  std::vector<int32_t> test_pairs;
+  std::vector<uint8_t> test_pos;
+  int64_t sample_m = 0;
+  if (lp) {
+    std::vector<std::pair<int32_t, int32_t>> pos, neg;
+    for (int f = 0; f < 2; ++f) {
+      const std::string path = dataset + queryname + (f ? "-Neg_LP_Test.txt" : "-Pos_LP_Test.txt");
+      int32_t *e = nullptr;
+      int64_t m = 0;
+      tsvd_status rs = tsvd_read_edge_file(path.c_str(), compat ? 1 : 0, &e, &m);
+      if (rs != TSVD_OK) return die(path.c_str(), rs);
+      auto &dst = f ? neg : pos;
+      for (int64_t i = 0; i < m; ++i) dst.emplace_back(e[2 * i], e[2 * i + 1]);
+      if (!f) sample_m = m;
+      tsvd_free(e);
+      std::sort(dst.begin(), dst.end());
+      dst.erase(std::unique(dst.begin(), dst.end()), dst.end());
+    }
+    for (int f = 0; f < 2; ++f)
+      for (auto &p : f ? neg : pos) {
+        test_pairs.push_back(p.first);
+        test_pairs.push_back(p.second);
+        test_pos.push_back(f == 0 || std::binary_search(pos.begin(), pos.end(), p) ? 1 : 0);
+      }
+  }
   tsvd_session *s = nullptr;
   tsvd_status st = tsvd_session_create(&c, &s);
   if (st != TSVD_OK) return die("session", st);
@@ -119,8 +157,19 @@ int main(int argc, char **argv) {
                 (long long)ss.edges_inserted, (long long)ss.pushes, ss.dirty_blocks, ss.ms_total);
     if (tsvd_session_embedding(s, emb.data()) == TSVD_OK) have = true;
     if (have) std::copy(emb.begin(), emb.end(), all.begin() + (size_t)(it - 1) * S * d);
+    const int64_t np = (int64_t)test_pos.size();
+    if (lp && have && np > 0) {
+      std::vector<double> score(np);
+      st = tsvd_lp_scores(s, test_pairs.data(), np, 0, score.data());
+      if (st != TSVD_OK) return die("lp scores", st);
+      double prec = 0;
+      st = tsvd_lp_precision(score.data(), test_pos.data(), np, std::min(sample_m, np), &prec);
+      if (st != TSVD_OK) return die("lp precision", st);
+      std::printf("link prediction precision: %g\n", prec);
+    }
   }
   tsvd_session_destroy(s);
+  if (lp) return 0;
   // Tree_u_NC.cpp:877-896
   int residue_order = 0;
   if (rmax * 10000 == 1) residue_order = 5;

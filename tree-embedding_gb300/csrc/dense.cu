@@ -580,9 +580,13 @@ __device__ __forceinline__ int packed(int i, int j) {  // i <= j
 }
 __device__ __forceinline__ int pk(int i, int j) { return i <= j ? packed(i, j) : packed(j, i); }
 
-// Player at circle position `pos` in round `t` of a round-robin over np players.
+// Player at circle position `pos` (<= np-1) in round `t` (< np-1) of a
+// round-robin over np players.
 __device__ __forceinline__ int circle_player(int pos, int t, int np) {
-  return pos == 0 ? 0 : ((pos - 1 + t) % (np - 1)) + 1;
+  if (pos == 0) return 0;
+  int x = pos - 1 + t;
+  if (x >= np - 1) x -= np - 1;
+  return x + 1;
 }
 
 struct JacobiArgs {
@@ -698,39 +702,68 @@ __global__ void __launch_bounds__(JAC_THREADS) jacobi_kernel(JacobiArgs a) {
 }
 
 // V = product of the logged rotations, rows processed independently;
-// column c of the product lands in column rank[c] of the output.
+// column c of the product lands in column rank[c] of the output. The log is
+// streamed into shared memory REPLAY_CHUNK rounds at a time with cp.async,
+// double buffered, so a round waits on its barrier only, not on L2.
 constexpr int REPLAY_ROWS = 16;
+constexpr int REPLAY_CHUNK = 16;
+
+__device__ __forceinline__ void cp_async8(void *smem, const void *gmem) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(smem_u32(smem)), "l"(gmem));
+}
+
 __global__ void __launch_bounds__(256) jacobi_replay_kernel(JacobiArgs a, float *const *vout) {
-  extern __shared__ __align__(16) float sv[];  // [REPLAY_ROWS][n]
+  extern __shared__ __align__(16) float sv[];  // [REPLAY_ROWS][n], then [2][REPLAY_CHUNK][P] float2
   const int n = a.n, np = n + (n & 1), P = np / 2;
   const int prob = blockIdx.y;
   const int r0 = blockIdx.x * REPLAY_ROWS;
   const int nr = min(REPLAY_ROWS, n - r0);
   if (nr <= 0) return;
+  float2 *lb = reinterpret_cast<float2 *>(sv + ((REPLAY_ROWS * n + 1) & ~1));
   for (int i = threadIdx.x; i < REPLAY_ROWS * n; i += blockDim.x) {
     int rr = i / n, cc = i % n;
     sv[i] = (rr < nr && r0 + rr == cc) ? 1.f : 0.f;
   }
   const float2 *log = a.log + (int64_t)prob * JAC_MAX_SWEEPS * (np - 1) * P;
-  const int sweeps = a.sweeps[prob];
-  __syncthreads();
-  for (int sw = 0; sw < sweeps; ++sw)
-    for (int t = 0; t < np - 1; ++t) {
-      const float2 *lg = log + ((int64_t)sw * (np - 1) + t) * P;
-      for (int w = threadIdx.x; w < P * REPLAY_ROWS; w += blockDim.x) {
-        const int k = w % P, rr = w / P;
-        if (rr >= nr) continue;
-        float2 cs = lg[k];
-        if (cs.y == 0.f) continue;
-        int x = circle_player(k, t, np), y = circle_player(np - 1 - k, t, np);
-        int p = min(x, y), q = max(x, y);
-        if (q >= n) continue;
-        float vp = sv[rr * n + p], vq = sv[rr * n + q];
-        sv[rr * n + p] = cs.x * vp - cs.y * vq;
-        sv[rr * n + q] = cs.y * vp + cs.x * vq;
+  const int rounds = a.sweeps[prob] * (np - 1);
+  const int nchunks = (rounds + REPLAY_CHUNK - 1) / REPLAY_CHUNK;
+  const int G = max(1, (int)blockDim.x / P);                // row groups (P <= 128)
+  const int g = (int)threadIdx.x / P, k = (int)threadIdx.x % P;
+  auto issue = [&](int c) {
+    const int first = c * REPLAY_CHUNK, cnt = min(REPLAY_CHUNK, rounds - first);
+    const float2 *src = log + (int64_t)first * P;
+    float2 *dst = lb + (c & 1) * REPLAY_CHUNK * P;
+    for (int i = threadIdx.x; i < cnt * P; i += blockDim.x) cp_async8(dst + i, src + i);
+    cp_async_commit();
+  };
+  if (nchunks > 0) issue(0);
+  for (int c = 0; c < nchunks; ++c) {
+    if (c + 1 < nchunks) {
+      issue(c + 1);
+      cp_async_wait<1>();
+    } else {
+      cp_async_wait<0>();
+    }
+    __syncthreads();  // chunk c visible to every thread; sv initialized
+    const float2 *buf = lb + (c & 1) * REPLAY_CHUNK * P;
+    const int first = c * REPLAY_CHUNK, cnt = min(REPLAY_CHUNK, rounds - first);
+    for (int q = 0; q < cnt; ++q) {
+      const int t = (first + q) % (np - 1);
+      // thread (group g, pair k): one rotation, applied to rows g, g+G, ...
+      if (g < G) {
+        const float2 cs = buf[q * P + k];
+        const int x = circle_player(k, t, np), y = circle_player(np - 1 - k, t, np);
+        const int p = min(x, y), qq = max(x, y);
+        if (cs.y != 0.f && qq < n)
+          for (int rr = g; rr < nr; rr += G) {
+            const float vp = sv[rr * n + p], vq = sv[rr * n + qq];
+            sv[rr * n + p] = cs.x * vp - cs.y * vq;
+            sv[rr * n + qq] = cs.y * vp + cs.x * vq;
+          }
       }
       __syncthreads();
     }
+  }
   float *V = vout[prob];
   const int32_t *rank = a.rank + prob * n;
   for (int i = threadIdx.x; i < nr * n; i += blockDim.x) {
@@ -916,7 +949,13 @@ tsvd_status jacobi_eig_batched(double *const *g, int n, float *const *lambda, fl
   }
   jacobi_kernel<<<nprob, JAC_THREADS, smem, st>>>(a);
   TSVD_LAUNCH_CHECK();
-  size_t rsmem = (size_t)REPLAY_ROWS * n * sizeof(float);
+  const size_t rsmem = (size_t)((REPLAY_ROWS * n + 1) & ~1) * sizeof(float) +
+                       (size_t)2 * REPLAY_CHUNK * P * sizeof(float2);
+  static size_t rcur = 0;
+  if (rsmem > 48 * 1024 && rsmem > rcur) {
+    TSVD_TRY(set_smem((const void *)jacobi_replay_kernel, rsmem));
+    rcur = rsmem;
+  }
   jacobi_replay_kernel<<<dim3((unsigned)ceil_div(n, REPLAY_ROWS), nprob), 256, rsmem, st>>>(a, v);
   TSVD_LAUNCH_CHECK();
   if (sweeps_out) {

@@ -158,6 +158,20 @@ tsvd_status cholqr2(FrpcaWork &W, float *const *x, const int32_t *rows, int max_
   return TSVD_OK;
 }
 
+// U (nsrc x d fp32, ld d; orthonormal columns, |u| <= 1) -> hi + lo halves of
+// U * scale in the [sp][kLp] layout of the skinny GEMM operand, zero padded.
+__global__ void lp_split_kernel(const float *__restrict__ u, int nsrc, int d, int sp,
+                                __half *__restrict__ hi, __half *__restrict__ lo, float scale) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < (int64_t)sp * kLp;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int r = (int)(i / kLp), c = (int)(i % kLp);
+    const float x = (r < nsrc && c < d) ? u[(int64_t)r * d + c] * scale : 0.f;
+    const __half h = __float2half_rn(x);
+    hi[i] = h;
+    lo[i] = __float2half_rn(x - __half2float(h));
+  }
+}
+
 }  // namespace
 
 tsvd_status frpca_work_alloc(FrpcaWork &W, int nmax, int64_t rows_max, int sp, int l, int d) {
@@ -366,6 +380,37 @@ tsvd_status merge_batch(FrpcaWork &W, const MergeProblem *probs, int nprob, int 
                                (const float *const *)d_v, n, n, d, (const float *const *)d_cs,
                                d_out, d, nullptr, nullptr, 1.f, nprob, st));
   return TSVD_OK;
+}
+
+tsvd_status lp_right_batch(FrpcaWork &W, const LpProblem *probs, int nprob, const float *u,
+                           int nsrc, int d, cudaStream_t st) {
+  if (nprob == 0) return TSVD_OK;
+  if (nprob > W.nmax) return fail(TSVD_ERR_INVALID, "lp: too many blocks");
+  if (d > kLp || nsrc > W.sp) return fail(TSVD_ERR_INVALID, "lp: d = %d, |S| = %d", d, nsrc);
+  TSVD_CUDA(cudaStreamSynchronize(st));  // the pointer staging area is reused
+  // one split of U, shared by every block
+  lp_split_kernel<<<grid_for((int64_t)W.sp * kLp, 256, 4), 256, 0, st>>>(u, nsrc, d, W.sp, W.qhi,
+                                                                         W.qlo, kSplitScale);
+  TSVD_LAUNCH_CHECK();
+  std::vector<const __half *> at(nprob), yhi(nprob, W.qhi), ylo(nprob, W.qlo);
+  std::vector<float *> z(nprob);
+  std::vector<int32_t> nc(nprob);
+  int max_nc = 0;
+  for (int i = 0; i < nprob; ++i) {
+    at[i] = probs[i].at;
+    z[i] = probs[i].v_out;
+    nc[i] = probs[i].ncols;
+    max_nc = std::max(max_nc, (int)probs[i].ncols);
+  }
+  if (max_nc == 0) return TSVD_OK;
+  PtrPack pk(W);
+  auto d_at = pk.add(at);
+  auto d_yhi = pk.add(yhi), d_ylo = pk.add(ylo);
+  auto d_z = pk.add(z);
+  const int32_t *d_nc = pk.add_int(nc);
+  TSVD_TRY(pk.upload(st));
+  GemmBatch gb{d_at, d_nc, W.sp, nprob};
+  return gemm_bwd(gb, d_yhi, d_ylo, d_z, W.sp, max_nc, 1.f / kSplitScale, st);
 }
 
 }  // namespace tsvd

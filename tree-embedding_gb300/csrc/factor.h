@@ -61,4 +61,17 @@ struct MergeProblem {
 tsvd_status merge_batch(FrpcaWork &W, const MergeProblem *probs, int nprob, int h, int nsrc,
                         int root_mode, cudaStream_t st);
 
+struct LpProblem {
+  const __half *at;  // A^T of the block, [ncols][sp]
+  int32_t ncols;
+  float *v_out;      // [ncols][kLp]: row c = A[:, c]^T U (columns >= d are zero)
+};
+
+// LP right factor of every listed block: V_b = A_b^T U with U the |S| x d root
+// factor (orthonormal columns), on the tensor cores (the transposed product of
+// the frPCA passes). Tree_u_LP.cpp:291-407 (csr_matrix_transpose_matrix_mult
+// per updated block).
+tsvd_status lp_right_batch(FrpcaWork &W, const LpProblem *probs, int nprob, const float *u,
+                           int nsrc, int d, cudaStream_t st);
+
 }  // namespace tsvd

@@ -404,13 +404,30 @@ tsvd_status ppr_refresh(PprState &P, const Adjacency &A, const int32_t *sources_
   return TSVD_OK;
 }
 
-tsvd_status ppr_push(PprState &P, const Adjacency &A, const PprParams &prm, uint8_t *vmark,
-                     cudaStream_t st, PushStats *out) {
+namespace {
+
+// One push (one PPR state), advanced check_every rounds at a time.
+struct PushJob {
+  PprState *P = nullptr;
+  cudaStream_t st = nullptr;
+  PushArgs pa{};
+  CollectArgs ca{};
+  int gpush = 0, gcol = 0;
+  int level = 0;
+  bool done = false;
+  int64_t rounds = 0;
+  double kernel_ms = 0;
+};
+
+tsvd_status job_begin(PushJob &J, PprState &P, const Adjacency &A, const PprParams &prm,
+                      uint8_t *vmark, cudaStream_t st) {
   if (!P.seeded) return fail(TSVD_ERR_STATE, "push before refresh");
+  J.P = &P;
+  J.st = st;
   TSVD_CUDA(cudaMemsetAsync(P.stats, 0, kStatSlots * 4 * sizeof(unsigned long long), st));
   TSVD_CUDA(cudaMemsetAsync(P.counters + 4, 0, sizeof(int32_t), st));
   const float rmax_f = largest_float_not_above(prm.rmax);
-  PushArgs pa;
+  PushArgs &pa = J.pa;
   pa.r = P.r; pa.p = P.p; pa.off = A.off; pa.deg = A.deg; pa.nbr = A.nbr;
   pa.n = P.n; pa.sp = P.sp; pa.nsrc = P.nsrc; pa.chunks = P.chunks; pa.tflag = P.tflag; pa.pend = P.pend;
   pa.alpha_f = (float)prm.alpha; pa.one_minus_alpha_f = (float)(1.0 - prm.alpha);
@@ -420,79 +437,119 @@ tsvd_status ppr_push(PprState &P, const Adjacency &A, const PprParams &prm, uint
   pa.heavy_count = P.counters + 2; pa.heavy_cap = P.heavy_cap;
   pa.units = P.units; pa.unit_count = P.counters + 3; pa.unit_cap = P.unit_cap;
   pa.overflow = P.counters + 4; pa.stats = P.stats;
-  CollectArgs ca;
+  CollectArgs &ca = J.ca;
   ca.tflag = P.tflag; ca.pend = P.pend; ca.nwords = P.nwords; ca.n = P.n; ca.chunks = P.chunks;
   ca.nsrc = P.nsrc; ca.sp = P.sp; ca.r = P.r; ca.deg = A.deg; ca.rmax_f = rmax_f;
   ca.cap = P.cap; ca.overflow = P.counters + 4;
-  const int gpush = grid_for((int64_t)1 << 30, 256, 8);
-  const int gcol = grid_for(ceil_div(P.nwords, 64) * 256, 256, 8);
-  const int check_every = std::min(8, prm.check_every > 0 ? prm.check_every : 4);
-  double kernel_ms = 0;
-  const int levels = std::max(1, prm.levels);
-  int64_t rounds = 0;
-  // Threshold schedule: residues above rmax * ratio^k are pushed first, k
-  // descending to 0. Lower residues wait in the pending set, so a vertex
-  // collects more before it is pushed; the last level is the plain rmax test
-  // and leaves the same invariant (every eligible residue <= rmax).
-  for (int level = levels - 1; level >= 0; --level) {
-    const float theta = largest_float_not_above(prm.rmax * std::pow(prm.ratio, (double)level));
-    pa.theta_f = ca.theta_f = std::max(theta, rmax_f);
-    if (level < levels - 1) {
-      // the frontier of the previous level is empty: re-examine parked pairs
-      unpark_kernel<<<grid_for(P.nwords, 256, 8), 256, 0, st>>>(P.tflag, P.pend, P.nwords);
-      TSVD_LAUNCH_CHECK();
-      TSVD_CUDA(cudaMemsetAsync(P.counters + P.cur, 0, sizeof(int32_t), st));
-      ca.next = P.front[P.cur];
-      ca.next_count = P.counters + P.cur;
-      collect_kernel<<<gcol, 256, 0, st>>>(ca);
-      TSVD_LAUNCH_CHECK();
-    }
-    for (;;) {
-      for (int k = 0; k < check_every; ++k) {
-        int cur = P.cur, nxt = 1 - P.cur;
-        pa.front = P.front[cur];
-        pa.front_count = P.counters + cur;
-        TSVD_CUDA(cudaMemsetAsync(P.counters + 2, 0, 2 * sizeof(int32_t), st));
-        TSVD_CUDA(cudaMemsetAsync(P.counters + nxt, 0, sizeof(int32_t), st));
-        TSVD_CUDA(cudaEventRecord(P.kev[2 * k], st));
-        push_kernel<<<gpush, 256, 0, st>>>(pa);
-        TSVD_LAUNCH_CHECK();
-        push_heavy_kernel<<<gpush, 256, 0, st>>>(pa);
-        TSVD_LAUNCH_CHECK();
-        TSVD_CUDA(cudaEventRecord(P.kev[2 * k + 1], st));
-        ca.next = P.front[nxt];
-        ca.next_count = P.counters + nxt;
-        collect_kernel<<<gcol, 256, 0, st>>>(ca);
-        TSVD_LAUNCH_CHECK();
-        P.cur = nxt;
-        ++rounds;
-      }
-      TSVD_CUDA(cudaMemcpyAsync(P.host_counters, P.counters, 8 * sizeof(int32_t),
-                                cudaMemcpyDeviceToHost, st));
-      TSVD_CUDA(cudaStreamSynchronize(st));
-      for (int k = 0; k < check_every; ++k) {
-        float ms = 0.f;
-        if (cudaEventElapsedTime(&ms, P.kev[2 * k], P.kev[2 * k + 1]) == cudaSuccess) kernel_ms += ms;
-      }
-      if (P.host_counters[4]) return fail(TSVD_ERR_STATE, "push: frontier buffer overflow");
-      if (P.host_counters[P.cur] == 0) break;
-      if (rounds >= prm.max_rounds)
-        return fail(TSVD_ERR_TIMEOUT, "push: %lld rounds without convergence", (long long)rounds);
-    }
+  J.gpush = grid_for((int64_t)1 << 30, 256, 8);
+  J.gcol = grid_for(ceil_div(P.nwords, 64) * 256, 256, 8);
+  J.level = std::max(1, prm.levels) - 1;
+  J.done = false;
+  J.rounds = 0;
+  J.kernel_ms = 0;
+  return TSVD_OK;
+}
+
+// Threshold schedule: residues above rmax * ratio^k are pushed first, k
+// descending to 0. Lower residues wait in the pending set, so a vertex
+// collects more before it is pushed; the last level is the plain rmax test
+// and leaves the same invariant (every eligible residue <= rmax).
+float level_theta(const PprParams &prm, int level, float rmax_f) {
+  const float theta = largest_float_not_above(prm.rmax * std::pow(prm.ratio, (double)level));
+  return std::max(theta, rmax_f);
+}
+
+// Launches `count` rounds on the job's stream (asynchronous).
+tsvd_status job_rounds(PushJob &J, int count) {
+  PprState &P = *J.P;
+  cudaStream_t st = J.st;
+  for (int k = 0; k < count; ++k) {
+    const int cur = P.cur, nxt = 1 - P.cur;
+    J.pa.front = P.front[cur];
+    J.pa.front_count = P.counters + cur;
+    TSVD_CUDA(cudaMemsetAsync(P.counters + 2, 0, 2 * sizeof(int32_t), st));
+    TSVD_CUDA(cudaMemsetAsync(P.counters + nxt, 0, sizeof(int32_t), st));
+    TSVD_CUDA(cudaEventRecord(P.kev[2 * k], st));
+    push_kernel<<<J.gpush, 256, 0, st>>>(J.pa);
+    TSVD_LAUNCH_CHECK();
+    push_heavy_kernel<<<J.gpush, 256, 0, st>>>(J.pa);
+    TSVD_LAUNCH_CHECK();
+    TSVD_CUDA(cudaEventRecord(P.kev[2 * k + 1], st));
+    J.ca.next = P.front[nxt];
+    J.ca.next_count = P.counters + nxt;
+    collect_kernel<<<J.gcol, 256, 0, st>>>(J.ca);
+    TSVD_LAUNCH_CHECK();
+    P.cur = nxt;
+    ++J.rounds;
   }
+  TSVD_CUDA(cudaMemcpyAsync(P.host_counters, P.counters, 8 * sizeof(int32_t),
+                            cudaMemcpyDeviceToHost, st));
+  return TSVD_OK;
+}
+
+// Waits for the job's launched rounds; ends the level when its frontier is
+// empty, starting the next level (or finishing) as the schedule says.
+tsvd_status job_poll(PushJob &J, int count, const PprParams &prm) {
+  PprState &P = *J.P;
+  TSVD_CUDA(cudaStreamSynchronize(J.st));
+  for (int k = 0; k < count; ++k) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, P.kev[2 * k], P.kev[2 * k + 1]) == cudaSuccess) J.kernel_ms += ms;
+  }
+  if (P.host_counters[4]) return fail(TSVD_ERR_STATE, "push: frontier buffer overflow");
+  if (P.host_counters[P.cur] != 0) {
+    if (J.rounds >= prm.max_rounds)
+      return fail(TSVD_ERR_TIMEOUT, "push: %lld rounds without convergence", (long long)J.rounds);
+    return TSVD_OK;
+  }
+  if (J.level == 0) {
+    J.done = true;
+    return TSVD_OK;
+  }
+  // the frontier of this level is empty: re-examine parked pairs at the next
+  --J.level;
+  J.pa.theta_f = J.ca.theta_f = level_theta(prm, J.level, J.pa.rmax_f);
+  unpark_kernel<<<grid_for(P.nwords, 256, 8), 256, 0, J.st>>>(P.tflag, P.pend, P.nwords);
+  TSVD_LAUNCH_CHECK();
+  TSVD_CUDA(cudaMemsetAsync(P.counters + P.cur, 0, sizeof(int32_t), J.st));
+  J.ca.next = P.front[P.cur];
+  J.ca.next_count = P.counters + P.cur;
+  collect_kernel<<<J.gcol, 256, 0, J.st>>>(J.ca);
+  TSVD_LAUNCH_CHECK();
+  return TSVD_OK;
+}
+
+tsvd_status job_finish(PushJob &J, PushStats *out) {
+  PprState &P = *J.P;
   unsigned long long slots[kStatSlots * 4], hs[4] = {0, 0, 0, 0};
-  TSVD_CUDA(cudaMemcpy(slots, P.stats, sizeof slots, cudaMemcpyDeviceToHost));
+  TSVD_CUDA(cudaMemcpyAsync(slots, P.stats, sizeof slots, cudaMemcpyDeviceToHost, J.st));
+  TSVD_CUDA(cudaStreamSynchronize(J.st));
   for (int k = 0; k < kStatSlots * 4; ++k) hs[k % 4] += slots[k];
   if (out) {
-    out->rounds = rounds;
+    out->rounds = J.rounds;
     out->pushes = (int64_t)hs[0];
     out->edge_updates = (int64_t)hs[1];
     out->items = (int64_t)hs[2];
     out->item_edges = (int64_t)hs[3];
-    out->kernel_ms = kernel_ms;
+    out->kernel_ms = J.kernel_ms;
   }
   P.seeded = false;
   return TSVD_OK;
+}
+
+}  // namespace
+
+tsvd_status ppr_push(PprState &P, const Adjacency &A, const PprParams &prm, uint8_t *vmark,
+                     cudaStream_t st, PushStats *out) {
+  PushJob J;
+  TSVD_TRY(job_begin(J, P, A, prm, vmark, st));
+  J.pa.theta_f = J.ca.theta_f = level_theta(prm, J.level, J.pa.rmax_f);
+  const int check_every = std::min(8, prm.check_every > 0 ? prm.check_every : 4);
+  while (!J.done) {
+    TSVD_TRY(job_rounds(J, check_every));
+    TSVD_TRY(job_poll(J, check_every, prm));
+  }
+  return job_finish(J, out);
 }
 
 }  // namespace tsvd

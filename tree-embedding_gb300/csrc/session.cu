@@ -84,6 +84,16 @@ struct tsvd_session {
   int iter = 0;
   tsvd_step_stats last{};
   cudaEvent_t ev[8]{};
+  // LP right factor (cfg.lp_right_factor)
+  float *lp_v = nullptr;          // [n][kLp]: row b*col_dim + c = V of block b's column c
+  float *lp_u = nullptr;          // [nparts][S][d]: the root factor each V_b was made with
+  std::vector<int> lp_iter;       // snapshot of each block's V_b (-1: never)
+  int32_t *lp_valid_dev = nullptr;
+  int32_t *colpos = nullptr;      // [n]: compacted column of a vertex in its block (-1: none)
+  int32_t *src_row = nullptr;     // [n]: row of a source vertex in U (-1: not a source)
+  int32_t *pairs_dev = nullptr;
+  double *scores_dev = nullptr;
+  int64_t pairs_cap = 0;
 
   size_t node_elems() const { return (size_t)S * d; }
   float *node_b(int i) { return tree_b + (size_t)i * node_elems(); }
@@ -119,6 +129,44 @@ __global__ void f32_to_f64_kernel(const float *in, double *out, int64_t n) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x)
     out[i] = (double)in[i];
+}
+
+// One warp per (source i, vertex j) pair: U_b[row(i)] . V[j] in fp64, times
+// the degree product when asked; invalid pairs set *bad.
+__global__ void lp_score_kernel(const int32_t *__restrict__ pairs, int64_t m,
+                                const int32_t *__restrict__ src_row,
+                                const int32_t *__restrict__ colpos, int32_t n, int32_t col_dim,
+                                int32_t nparts, const float *__restrict__ lp_v,
+                                const float *__restrict__ lp_u, const int32_t *__restrict__ valid,
+                                int d, int S, const int32_t *__restrict__ deg_i,
+                                const int32_t *__restrict__ deg_j, int degree_scaled,
+                                double *__restrict__ scores, int32_t *__restrict__ bad) {
+  const int lane = threadIdx.x & 31;
+  const int64_t gw = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t k = gw; k < m; k += nw) {
+    const int32_t i = pairs[2 * k], j = pairs[2 * k + 1];
+    const int32_t row = (i >= 0 && i < n) ? src_row[i] : -1;
+    if (row < 0 || j < 0 || j >= n) {
+      if (lane == 0) {
+        scores[k] = 0.0;
+        *bad = 1;
+      }
+      continue;
+    }
+    const int32_t b = min(j / col_dim, nparts - 1);
+    const int32_t c = colpos[j];
+    double acc = 0.0;
+    if (valid[b] && c >= 0) {
+      const float *u = lp_u + ((size_t)b * S + row) * d;
+      const float *v = lp_v + ((size_t)b * col_dim + c) * kLp;
+      for (int t = lane; t < d; t += 32) acc += (double)u[t] * (double)v[t];
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (degree_scaled) acc *= (double)deg_i[i] * (double)deg_j[j];
+    if (lane == 0) scores[k] = acc;
+  }
 }
 
 bool is_power_of(int n, int h) {
@@ -221,6 +269,21 @@ static tsvd_status session_alloc(tsvd_session *s) {
   TSVD_CUDA(cudaMalloc(&s->embedding, sizeof(float) * s->node_elems()));
   TSVD_CUDA(cudaMemset(s->embedding, 0, sizeof(float) * s->node_elems()));
   TSVD_CUDA(cudaMalloc(&s->bad_dev, sizeof(int32_t)));
+  if (c.lp_right_factor) {
+    TSVD_CUDA(cudaMalloc(&s->lp_v, sizeof(float) * s->n * kLp));
+    TSVD_CUDA(cudaMemset(s->lp_v, 0, sizeof(float) * s->n * kLp));
+    TSVD_CUDA(cudaMalloc(&s->lp_u, sizeof(float) * s->node_elems() * s->nparts));
+    TSVD_CUDA(cudaMemset(s->lp_u, 0, sizeof(float) * s->node_elems() * s->nparts));
+    TSVD_CUDA(cudaMalloc(&s->lp_valid_dev, sizeof(int32_t) * s->nparts));
+    TSVD_CUDA(cudaMemset(s->lp_valid_dev, 0, sizeof(int32_t) * s->nparts));
+    s->lp_iter.assign(s->nparts, -1);
+    TSVD_CUDA(cudaMalloc(&s->colpos, sizeof(int32_t) * s->n));
+    TSVD_CUDA(cudaMemset(s->colpos, 0xFF, sizeof(int32_t) * s->n));
+    std::vector<int32_t> rows(s->n, -1);
+    for (int k = 0; k < s->S; ++k) rows[s->sources[k]] = k;
+    TSVD_CUDA(cudaMalloc(&s->src_row, sizeof(int32_t) * s->n));
+    TSVD_CUDA(cudaMemcpy(s->src_row, rows.data(), sizeof(int32_t) * s->n, cudaMemcpyHostToDevice));
+  }
   const int last_w = s->n - (s->nparts - 1) * s->col_dim;
   TSVD_TRY(frpca_work_alloc(s->fw, s->nparts, std::max(last_w, s->col_dim), s->sp, s->l, s->d));
   return TSVD_OK;
@@ -241,6 +304,8 @@ static void session_release(tsvd_session *s) {
   cudaFree(s->norm2_dev); cudaFree(s->diff2_dev); cudaFree(s->nnz_dev); cudaFree(s->stored_dev);
   cudaFree(s->tree_b); cudaFree(s->tree_sigma); cudaFree(s->embedding);
   cudaFree(s->edges_dev); cudaFree(s->keys); cudaFree(s->vals); cudaFree(s->bad_dev);
+  cudaFree(s->lp_v); cudaFree(s->lp_u); cudaFree(s->lp_valid_dev); cudaFree(s->colpos);
+  cudaFree(s->src_row); cudaFree(s->pairs_dev); cudaFree(s->scores_dev);
   frpca_work_free(s->fw);
   for (auto &e : s->ev)
     if (e) cudaEventDestroy(e);
@@ -268,6 +333,8 @@ extern "C" tsvd_status tsvd_session_create(const tsvd_config *cfg, tsvd_session 
   if (c.passes_q < 1) return fail(TSVD_ERR_INVALID, "passes_q must be >= 1");
   if (c.transform < 0 || c.transform > 2 || c.dirty_rule < 0 || c.dirty_rule > 2)
     return fail(TSVD_ERR_INVALID, "bad transform or dirty rule");
+  if (c.lp_right_factor && c.root_scaling != TSVD_ROOT_U)
+    return fail(TSVD_ERR_INVALID, "lp_right_factor needs root_scaling TSVD_ROOT_U (LP drivers)");
   std::vector<int32_t> src(c.sources, c.sources + c.n_sources);
   {
     std::vector<int32_t> chk = src;
@@ -358,7 +425,7 @@ static tsvd_status insert_device(tsvd_session *s, const int32_t *edges_dev, int6
 
 static tsvd_status stage_materialize(tsvd_session *s, int iter) {
   const int P = s->nparts;
-  TSVD_TRY(colmap_update(s->vmark, s->colmap, s->ncols_dev, s->n, s->col_dim, P, s->st));
+  TSVD_TRY(colmap_update(s->vmark, s->colmap, s->colpos, s->ncols_dev, s->n, s->col_dim, P, s->st));
   TSVD_CUDA(cudaMemcpyAsync(s->ncols_h.data(), s->ncols_dev, sizeof(int32_t) * P,
                             cudaMemcpyDeviceToHost, s->st));
   TSVD_CUDA(cudaStreamSynchronize(s->st));
@@ -510,6 +577,40 @@ static tsvd_status stage_merge(tsvd_session *s) {
   return TSVD_OK;
 }
 
+// LP right factor of the blocks refreshed in this snapshot (Tree_u_LP.cpp:
+// 1024-1044: the blocks whose update record is this iteration), with this
+// snapshot's root factor U, which is kept beside them for scoring.
+static tsvd_status stage_lp(tsvd_session *s, int iter) {
+  if (!s->cfg.lp_right_factor || !s->has_embedding) return TSVD_OK;
+  std::vector<LpProblem> probs;
+  std::vector<int> blocks;
+  for (int b = 0; b < s->nparts; ++b) {
+    if (!s->dirty_h[b]) continue;
+    LpProblem p;
+    p.at = s->at_block(s->atcur[b], b);
+    p.ncols = s->ncols_h[b];
+    p.v_out = s->lp_v + (size_t)b * s->col_dim * kLp;
+    probs.push_back(p);
+    blocks.push_back(b);
+  }
+  if (probs.empty()) return TSVD_OK;
+  TSVD_TRY(lp_right_batch(s->fw, probs.data(), (int)probs.size(), s->embedding, s->S, s->d, s->st));
+  std::vector<int32_t> valid(s->nparts);
+  for (int b : blocks) {
+    TSVD_CUDA(cudaMemcpyAsync(s->lp_u + (size_t)b * s->node_elems(), s->embedding,
+                              sizeof(float) * s->node_elems(), cudaMemcpyDeviceToDevice, s->st));
+    s->lp_iter[b] = iter;
+  }
+  for (int b = 0; b < s->nparts; ++b) valid[b] = s->lp_iter[b] >= 0;
+  TSVD_CUDA(cudaMemcpyAsync(s->lp_valid_dev, valid.data(), sizeof(int32_t) * s->nparts,
+                            cudaMemcpyHostToDevice, s->st));
+  TSVD_CUDA(cudaStreamSynchronize(s->st));
+  return TSVD_OK;
+}
+
+// Refresh + push of one PPR state (the reverse one of a directed graph with
+// dir = 1). Running the two directions on two streams, round-interleaved, was
+// measured no faster: both are DRAM-bound through most of their rounds.
 static tsvd_status stage_ppr(tsvd_session *s, int iter, int dir) {
   const bool scratch = iter < s->cfg.dynamic_ppr_start_iter;
   PprParams prm = ppr_params(s);
@@ -551,12 +652,18 @@ static tsvd_status step_device(tsvd_session *s, const int32_t *edges_dev, int64_
   TSVD_TRY(stage_merge(s));
   TSVD_CUDA(cudaEventRecord(ev[5], s->st));
   TSVD_CUDA(cudaEventSynchronize(ev[5]));
+  if (s->cfg.lp_right_factor) {
+    TSVD_TRY(stage_lp(s, iter));
+    TSVD_CUDA(cudaEventRecord(ev[6], s->st));
+    TSVD_CUDA(cudaEventSynchronize(ev[6]));
+    s->last.ms_lp = ms_between(ev[5], ev[6]);
+  }
   s->last.ms_insert = ms_between(ev[0], ev[1]);
   s->last.ms_push = ms_between(ev[1], ev[2]);
   s->last.ms_log = ms_between(ev[2], ev[3]);
   s->last.ms_frpca = ms_between(ev[3], ev[4]);
   s->last.ms_merge = ms_between(ev[4], ev[5]);
-  s->last.ms_total = ms_between(ev[0], ev[5]);
+  s->last.ms_total = ms_between(ev[0], ev[5]) + s->last.ms_lp;
   return TSVD_OK;
 }
 
@@ -772,5 +879,79 @@ extern "C" tsvd_status tsvd_block_dense(tsvd_session *s, int32_t b, float *out) 
     for (int k = 0; k < s->S; ++k)
       out[(size_t)k * nb + col] = __half2float(at[(size_t)c * s->sp + k]);
   }
+  return TSVD_OK;
+}
+
+// ------------------------------------------------------------------ link prediction
+extern "C" tsvd_status tsvd_lp_right_factor(tsvd_session *s, float *v_out) {
+  if (!s || !v_out) return fail(TSVD_ERR_INVALID, "null argument");
+  if (!s->cfg.lp_right_factor) return fail(TSVD_ERR_STATE, "session built without lp_right_factor");
+  TSVD_CUDA(cudaSetDevice(s->cfg.device));
+  TSVD_CUDA(cudaStreamSynchronize(s->st));
+  std::memset(v_out, 0, sizeof(float) * (size_t)s->n * s->d);
+  std::vector<float> v;
+  std::vector<int32_t> cm;
+  for (int b = 0; b < s->nparts; ++b) {
+    const int nc = s->ncols_h[b];
+    if (s->lp_iter[b] < 0 || nc == 0) continue;
+    v.resize((size_t)nc * kLp);
+    cm.resize(nc);
+    TSVD_CUDA(cudaMemcpy(v.data(), s->lp_v + (size_t)b * s->col_dim * kLp,
+                         sizeof(float) * v.size(), cudaMemcpyDeviceToHost));
+    TSVD_CUDA(cudaMemcpy(cm.data(), s->colmap + (size_t)b * s->col_dim, sizeof(int32_t) * nc,
+                         cudaMemcpyDeviceToHost));
+    for (int c = 0; c < nc; ++c)
+      std::memcpy(v_out + (size_t)cm[c] * s->d, v.data() + (size_t)c * kLp, sizeof(float) * s->d);
+  }
+  return TSVD_OK;
+}
+
+extern "C" tsvd_status tsvd_lp_scores(tsvd_session *s, const int32_t *pairs, int64_t m,
+                                      int32_t degree_scaled, double *scores) {
+  if (!s || (m > 0 && (!pairs || !scores)) || m < 0) return fail(TSVD_ERR_INVALID, "bad arguments");
+  if (!s->cfg.lp_right_factor) return fail(TSVD_ERR_STATE, "session built without lp_right_factor");
+  if (m == 0) return TSVD_OK;
+  TSVD_CUDA(cudaSetDevice(s->cfg.device));
+  if (m > s->pairs_cap) {
+    cudaFree(s->pairs_dev);
+    cudaFree(s->scores_dev);
+    s->pairs_dev = nullptr;
+    s->scores_dev = nullptr;
+    s->pairs_cap = 0;
+    TSVD_CUDA(cudaMalloc(&s->pairs_dev, sizeof(int32_t) * 2 * m));
+    TSVD_CUDA(cudaMalloc(&s->scores_dev, sizeof(double) * m));
+    s->pairs_cap = m;
+  }
+  TSVD_CUDA(cudaMemcpyAsync(s->pairs_dev, pairs, sizeof(int32_t) * 2 * m, cudaMemcpyHostToDevice,
+                            s->st));
+  TSVD_CUDA(cudaMemsetAsync(s->bad_dev, 0, sizeof(int32_t), s->st));
+  const int32_t *deg_i = s->adj[0].deg;
+  const int32_t *deg_j = s->directed ? s->adj[1].deg : s->adj[0].deg;
+  lp_score_kernel<<<grid_for(m * 32, 256, 8), 256, 0, s->st>>>(
+      s->pairs_dev, m, s->src_row, s->colpos, s->n, s->col_dim, s->nparts, s->lp_v, s->lp_u,
+      s->lp_valid_dev, s->d, s->S, deg_i, deg_j, degree_scaled, s->scores_dev, s->bad_dev);
+  TSVD_LAUNCH_CHECK();
+  int32_t bad = 0;
+  TSVD_CUDA(cudaMemcpyAsync(scores, s->scores_dev, sizeof(double) * m, cudaMemcpyDeviceToHost,
+                            s->st));
+  TSVD_CUDA(cudaMemcpyAsync(&bad, s->bad_dev, sizeof(int32_t), cudaMemcpyDeviceToHost, s->st));
+  TSVD_CUDA(cudaStreamSynchronize(s->st));
+  if (bad) return fail(TSVD_ERR_INVALID, "a pair's first vertex is not a source or a vertex is out of range");
+  return TSVD_OK;
+}
+
+extern "C" tsvd_status tsvd_lp_precision(const double *scores, const uint8_t *positive, int64_t m,
+                                         int64_t k, double *precision) {
+  if (!precision || m < 0 || k < 1 || k > m || (m > 0 && (!scores || !positive)))
+    return fail(TSVD_ERR_INVALID, "need 1 <= k <= m");
+  std::vector<int64_t> idx(m);
+  for (int64_t i = 0; i < m; ++i) idx[i] = i;
+  auto before = [&](int64_t a, int64_t b) {
+    return scores[a] > scores[b] || (scores[a] == scores[b] && a < b);
+  };
+  std::nth_element(idx.begin(), idx.begin() + (k - 1), idx.end(), before);
+  int64_t hit = 0;
+  for (int64_t i = 0; i < k; ++i) hit += positive[idx[i]] ? 1 : 0;
+  *precision = (double)hit / (double)k;
   return TSVD_OK;
 }

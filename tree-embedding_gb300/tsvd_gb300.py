@@ -41,7 +41,7 @@ class Config(ctypes.Structure):
         ("refresh_mode", ctypes.c_int32), ("seed", ctypes.c_uint64),
         ("device", ctypes.c_int32), ("max_push_rounds", ctypes.c_int32),
         ("push_levels", ctypes.c_int32), ("push_ratio", ctypes.c_double),
-        ("push_cofrac", ctypes.c_double),
+        ("push_cofrac", ctypes.c_double), ("lp_right_factor", ctypes.c_int32),
     ]
 
 
@@ -57,7 +57,7 @@ class StepStats(ctypes.Structure):
         ("ms_frpca", ctypes.c_double), ("ms_merge", ctypes.c_double),
         ("ms_total", ctypes.c_double), ("push_items", ctypes.c_int64),
         ("ms_push_kernels", ctypes.c_double), ("ms_materialize_kernel", ctypes.c_double),
-        ("push_item_edges", ctypes.c_int64),
+        ("push_item_edges", ctypes.c_int64), ("ms_lp", ctypes.c_double),
     ]
 
     def as_dict(self):
@@ -116,6 +116,9 @@ _SIGS = {
     "tsvd_gaussian": (ctypes.c_float, [ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32,
                                        ctypes.c_uint32]),
     "frPCA": (None, [_vp, _vp, _vp, _vp, ctypes.c_int, ctypes.c_int]),
+    "tsvd_lp_right_factor": (ctypes.c_int, [_vp, _f32p]),
+    "tsvd_lp_scores": (ctypes.c_int, [_vp, _i32p, ctypes.c_int64, ctypes.c_int32, _f64p]),
+    "tsvd_lp_precision": (ctypes.c_int, [_f64p, _u8p, ctypes.c_int64, ctypes.c_int64, _f64p]),
 }
 
 EXPORTS = sorted(_SIGS)
@@ -183,6 +186,15 @@ def gaussian(seed, stream, row, col):
     return lib().tsvd_gaussian(seed, stream, row, col)
 
 
+def lp_precision(scores, positive, k):
+    sc = np.ascontiguousarray(scores, dtype=np.float64)
+    pos = np.ascontiguousarray(positive, dtype=np.uint8)
+    out = ctypes.c_double()
+    _check(lib().tsvd_lp_precision(_p(sc, _f64p), _p(pos, _u8p), len(sc), int(k),
+                                   ctypes.byref(out)))
+    return out.value
+
+
 def launch_count():
     """Kernels launched by the library so far in this process."""
     return lib().tsvd_launch_count()
@@ -214,7 +226,8 @@ class Session:
                  dynamic_ppr_start_iter=100, lazy_update_start_iter=100, delta=0.3,
                  transform=TRANSFORM_LOG10_NC, dirty_rule=DIRTY_REFERENCE, dirty_frac=0.01,
                  root_scaling=ROOT_SQRT_SIGMA, refresh_mode=REFRESH_EXACT, seed=20231, device=0,
-                 max_push_rounds=0, push_levels=1, push_ratio=8.0, push_cofrac=1.0):
+                 max_push_rounds=0, push_levels=1, push_ratio=8.0, push_cofrac=1.0,
+                 lp_right_factor=False):
         self.sources = np.ascontiguousarray(sources, dtype=np.int32)
         c = Config()
         lib().tsvd_config_default(ctypes.byref(c))
@@ -232,6 +245,7 @@ class Session:
         c.seed, c.device, c.max_push_rounds = int(seed), int(device), int(max_push_rounds)
         c.push_levels, c.push_ratio = int(push_levels), float(push_ratio)
         c.push_cofrac = float(push_cofrac)
+        c.lp_right_factor = int(bool(lp_right_factor))
         self.cfg = c
         self.n, self.S, self.d = c.n_vertices, c.n_sources, c.rank_d
         self.n_parts, self.h, self.directed = c.n_parts, c.hierarchy_n, bool(directed)
@@ -340,6 +354,19 @@ class Session:
         sig = np.zeros(self.d, np.float64)
         _check(lib().tsvd_tree_factor(self._h, int(node), _p(out, _f64p), _p(sig, _f64p)))
         return out, sig
+
+    # link prediction
+    def lp_right_factor(self):
+        out = np.zeros((self.n, self.d), np.float32)
+        _check(lib().tsvd_lp_right_factor(self._h, _p(out, _f32p)))
+        return out
+
+    def lp_scores(self, pairs, degree_scaled=False):
+        pr = np.ascontiguousarray(pairs, dtype=np.int32).reshape(-1, 2)
+        out = np.zeros(pr.shape[0], np.float64)
+        _check(lib().tsvd_lp_scores(self._h, _p(pr, _i32p), pr.shape[0], int(degree_scaled),
+                                    _p(out, _f64p)))
+        return out
 
     def block_dense(self, b):
         cd = self.n // self.n_parts
