@@ -293,10 +293,10 @@ def run_reference(args):
 # DRAM bytes (read + write) of push_kernel + push_heavy_kernel per pushed
 # item-neighbour (one 128-byte residual-line atomic), from one ncu capture of
 # every push launch of a timed rmat-d-2.7m snapshot (dram__bytes_read.sum +
-# dram__bytes_write.sum, one pass): 2310.7 GB over 1.474e10 item-neighbours
+# dram__bytes_write.sum, one pass): 2310.0 GB over 1.323e10 item-neighbours
 # (profiles/push_kernel_rmat-d-2.7m.md). `traffic` scales it to the launches
 # of the run being reported.
-PUSH_TRAFFIC_BYTES_PER_ITEM_EDGE = 156.8
+PUSH_TRAFFIC_BYTES_PER_ITEM_EDGE = 174.6
 
 
 def push_roofline(stages):

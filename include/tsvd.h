@@ -170,6 +170,7 @@ typedef struct tsvd_config {
   int32_t push_levels;      /* threshold schedule: push r > rmax*ratio^k, k = L-1..0  */
   double push_ratio;        /* (1 level = the plain rmax test)                      */
   double push_cofrac;       /* co-push residues > rmax*cofrac on lines being pushed  */
+                            /* (default 0.5; 1 = plain rmax test only)               */
   int32_t lp_right_factor;  /* 1: after every snapshot, V_b = A_b^T U for each block  */
                             /* refreshed in it (LP drivers; needs TSVD_ROOT_U)        */
 } tsvd_config;
@@ -297,10 +298,14 @@ tsvd_status tsvd_sample_sources(int32_t n, const int32_t *edges, int64_t m,
                                 int32_t k, uint64_t seed, int32_t *out);
 /* Parse a "u v" per line edge file. compat_dup_last = 1 reproduces the
  * reference reader's repeat of the last pair when the file ends in
- * whitespace (Graph_dynamic.h:127-130, 539-542). *edges is malloc'ed; free
- * with tsvd_free. */
+ * whitespace (Graph_dynamic.h:127-130, 539-542). A path ending in ".bin" is
+ * read as raw int32 (from, to) pairs in host byte order instead (no
+ * counterpart in the reference: fast ingestion of large deltas). *edges is
+ * malloc'ed; free with tsvd_free. */
 tsvd_status tsvd_read_edge_file(const char *path, int32_t compat_dup_last,
                                 int32_t **edges, int64_t *m);
+/* Writes m pairs as a ".bin" edge file (no counterpart in the reference). */
+tsvd_status tsvd_write_edge_file_binary(const char *path, const int32_t *edges, int64_t m);
 void tsvd_free(void *p);
 
 /* Gaussian test-matrix entry used by frPCA (Philox4x32-10 + Box-Muller in

@@ -128,3 +128,40 @@ def test_lp_precision_matches_oracle_including_ties():
         T.lp_precision(np.zeros(3), np.zeros(3, np.uint8), 4)
     with pytest.raises(T.TsvdError):
         T.lp_precision(np.zeros(3), np.zeros(3, np.uint8), 0)
+
+
+def test_binary_edge_file_round_trip(tmp_path):
+    e = np.random.default_rng(1).integers(0, 1 << 30, (1000, 2)).astype(np.int32)
+    p = str(tmp_path / "delta.bin")
+    T.write_edge_file_binary(p, e)
+    assert np.array_equal(T.read_edge_file(p), e)
+    (tmp_path / "bad.bin").write_bytes(b"\x00" * 12)  # not whole pairs
+    with pytest.raises(T.TsvdError):
+        T.read_edge_file(str(tmp_path / "bad.bin"))
+
+
+def test_cli_split_matches_reference_batch_splitter(tmp_path):
+    """tree_svd split: Code/split_edges_NC.cpp semantics (keep the first
+    round_index config lines, re-cut the following edges into batches)."""
+    cli = os.path.join(os.path.dirname(os.path.abspath(T.__file__)), "tree_svd")
+    d = tmp_path / "DY_Dataset" / "q"
+    d.mkdir(parents=True)
+    rng = np.random.default_rng(2)
+    files = [str(d / "subset.txt")]
+    (d / "subset.txt").write_text("1\n2\n")
+    snaps = [rng.integers(0, 500, (n, 2)) for n in (300, 170, 260)]
+    for k, e in enumerate(snaps):
+        files.append(str(d / ("s%d.txt" % k)))
+        np.savetxt(files[-1], e, fmt="%d %d")
+    (d / "config.txt").write_text("\n".join(files) + "\n")
+    r = subprocess.run([cli, "split", "nc", "q", "2", "--batch", "100", "--count", "3"],
+                       cwd=str(tmp_path), capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    lines = (tmp_path / "DY_Dataset" / "q_batch" / "config.txt").read_text().split()
+    assert lines[:2] == files[:2]
+    assert len(lines) == 5
+    rest = np.concatenate(snaps[1:])
+    for k, path in enumerate(lines[2:]):
+        assert path.endswith("q_batch-Train-2-%d.txt" % (k + 1))
+        got = np.loadtxt(tmp_path / path, dtype=np.int64).reshape(-1, 2)
+        assert np.array_equal(got, rest[100 * k:100 * (k + 1)])

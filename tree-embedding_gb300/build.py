@@ -53,7 +53,7 @@ def build(verbose=False):
     if os.path.exists(cli_src) and (not os.path.exists(CLI) or
                                     os.path.getmtime(CLI) < max(os.path.getmtime(LIB),
                                                                 os.path.getmtime(cli_src))):
-        cmd = ["g++", "-O2", "-std=c++17", "-I" + INCLUDE, cli_src, "-o", CLI, "-L" + HERE,
+        cmd = ["g++", "-O2", "-std=c++17", "-pthread", "-I" + INCLUDE, cli_src, "-o", CLI, "-L" + HERE,
                "-ltsvd_gb300", "-Wl,-rpath,$ORIGIN"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:

@@ -4,7 +4,15 @@
 //
 //   tree_svd <u_nc|d_nc|u_lp|d_lp> queryname EBpath alpha pass rmax NUMTHREAD \
 //            nParts hierarchy_n N dynamic_ppr_start_iter lazy_update_start_iter delta \
-//            [--compat] [--device K]
+//            [--compat] [--device K] [--npy]
+//   tree_svd split <nc|lp> queryname round_index [--batch B] [--count C] [--compat]
+//
+// While the GPU runs a snapshot, the next snapshot's file is read and parsed
+// on a host thread. --npy also writes the embeddings as <output>.npy
+// (float64, ((T-1)*|S|) x 128). `split` is the batch splitter of
+// Code/split_edges_NC.cpp / split_edges_LP.cpp: snapshots before round_index
+// are kept, the edges from round_index on are re-cut into files of B edges
+// (10,000), at most C of them (100), under DY_[LP_]Dataset/<queryname>_batch/.
 //
 // Same positional arguments (Tree_u_NC.cpp:301-322; NUMTHREAD is accepted and
 // ignored), same inputs (DY_Dataset/<queryname>/config.txt: line 0 the subset
@@ -20,6 +28,8 @@
 // factor U, and after every snapshot the right factor of the refreshed blocks
 // and "link prediction precision: P", the share of positive pairs among the
 // sample_m best-scored test pairs (:1040-1122); no embedding file is written.
+#include <sys/stat.h>
+
 #include <algorithm>
 #include <cstdio>
 #include <cstdlib>
@@ -28,6 +38,7 @@
 #include <iostream>
 #include <sstream>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "tsvd.h"
@@ -37,7 +48,85 @@ static int die(const char *what, tsvd_status st) {
   return 1;
 }
 
+// Code/split_edges_NC.cpp:21-131 (and the LP twin with DY_LP_Dataset).
+static int split_main(int argc, char **argv) {
+  if (argc < 5) {
+    std::fprintf(stderr, "usage: %s split <nc|lp> queryname round_index [--batch B] [--count C] "
+                         "[--compat]\n", argv[0]);
+    return 2;
+  }
+  const bool lp = std::string(argv[2]) == "lp";
+  const std::string root = lp ? "DY_LP_Dataset/" : "DY_Dataset/";
+  const std::string q = argv[3], bq = q + "_batch";
+  const int round_index = std::atoi(argv[4]);
+  int64_t per = 10000, count = 100;
+  bool compat = false;
+  for (int i = 5; i < argc; ++i) {
+    if (!std::strcmp(argv[i], "--batch") && i + 1 < argc) per = std::atoll(argv[++i]);
+    else if (!std::strcmp(argv[i], "--count") && i + 1 < argc) count = std::atoll(argv[++i]);
+    else if (!std::strcmp(argv[i], "--compat")) compat = true;
+  }
+  std::vector<std::string> shots;
+  {
+    std::ifstream cfg((root + q + "/config.txt").c_str());
+    if (!cfg) {
+      std::fprintf(stderr, "tree_svd: cannot read %s%s/config.txt\n", root.c_str(), q.c_str());
+      return 1;
+    }
+    std::string line;
+    while (std::getline(cfg, line)) shots.push_back(line);
+  }
+  if (round_index < 0 || round_index > (int)shots.size() || per < 1 || count < 1) {
+    std::fprintf(stderr, "tree_svd: bad round_index / batch / count\n");
+    return 2;
+  }
+  ::mkdir((root + bq).c_str(), 0755);
+  std::ofstream oc((root + bq + "/config.txt").c_str());
+  for (int i = 0; i < round_index; ++i) oc << shots[i] << "\n";
+  std::vector<int32_t> pending;
+  int64_t written = 0;
+  for (size_t f = round_index; f < shots.size() && written < count; ++f) {
+    int32_t *e = nullptr;
+    int64_t m = 0;
+    tsvd_status st = tsvd_read_edge_file(shots[f].c_str(), compat ? 1 : 0, &e, &m);
+    if (st != TSVD_OK) return die(shots[f].c_str(), st);
+    pending.insert(pending.end(), e, e + 2 * m);
+    tsvd_free(e);
+    while ((int64_t)pending.size() >= 2 * per && written < count) {
+      ++written;
+      const std::string name = "./" + root + bq + "/" + bq + "-Train-" +
+                               std::to_string(round_index) + "-" + std::to_string(written) + ".txt";
+      std::ofstream out(name.c_str());
+      for (int64_t i = 0; i < per; ++i) out << pending[2 * i] << " " << pending[2 * i + 1] << "\n";
+      oc << name << "\n";
+      pending.erase(pending.begin(), pending.begin() + 2 * per);
+    }
+  }
+  if (written < count)
+    std::printf("We have read all consecutive edges, but there are not enough edges till the end!\n");
+  std::printf("wrote %lld batches of %lld edges\n", (long long)written, (long long)per);
+  return 0;
+}
+
+static bool write_npy(const std::string &path, const std::vector<double> &a, size_t rows,
+                      size_t cols) {
+  std::ofstream os(path.c_str(), std::ios::binary);
+  if (!os) return false;
+  std::string hdr = "{'descr': '<f8', 'fortran_order': False, 'shape': (" + std::to_string(rows) +
+                    ", " + std::to_string(cols) + "), }";
+  while ((10 + hdr.size() + 1) % 64) hdr += ' ';
+  hdr += '\n';
+  const unsigned short hl = (unsigned short)hdr.size();
+  os.write("\x93NUMPY\x01\x00", 8);
+  os.put((char)(hl & 0xff));
+  os.put((char)(hl >> 8));
+  os << hdr;
+  os.write(reinterpret_cast<const char *>(a.data()), (std::streamsize)(rows * cols * sizeof(double)));
+  return (bool)os;
+}
+
 int main(int argc, char **argv) {
+  if (argc >= 2 && !std::strcmp(argv[1], "split")) return split_main(argc, argv);
   if (argc < 14) {
     std::fprintf(stderr,
                  "usage: %s <u_nc|d_nc|u_lp|d_lp> queryname EBpath alpha pass rmax NUMTHREAD "
@@ -60,10 +149,11 @@ int main(int argc, char **argv) {
   const int dyn = (int)std::strtod(argv[11], &endp);
   const int lazy = (int)std::strtod(argv[12], &endp);
   const double delta = std::strtod(argv[13], &endp);
-  bool compat = false;
+  bool compat = false, npy = false;
   int device = 0;
   for (int i = 14; i < argc; ++i) {
     if (!std::strcmp(argv[i], "--compat")) compat = true;
+    else if (!std::strcmp(argv[i], "--npy")) npy = true;
     else if (!std::strcmp(argv[i], "--device") && i + 1 < argc) device = std::atoi(argv[++i]);
   }
   const std::string dataset = std::string(lp ? "DY_LP_Dataset/" : "DY_Dataset/") + queryname + "/";
@@ -143,14 +233,31 @@ int main(int argc, char **argv) {
   const int T = (int)shots.size();
   std::vector<double> all((size_t)(T - 1) * S * d, 0.0), emb(S * d, 0.0);
   bool have = false;
-  for (int it = 1; it < T; ++it) {
+  // the next snapshot's file is read on a host thread while the GPU works
+  struct Loaded {
     int32_t *edges = nullptr;
     int64_t m = 0;
-    st = tsvd_read_edge_file(shots[it].c_str(), compat ? 1 : 0, &edges, &m);
-    if (st != TSVD_OK) return die(shots[it].c_str(), st);
-    st = tsvd_session_step(s, edges, m);
-    tsvd_free(edges);
+    tsvd_status st = TSVD_OK;
+  };
+  auto load = [&](int it, Loaded *out) {
+    out->st = tsvd_read_edge_file(shots[it].c_str(), compat ? 1 : 0, &out->edges, &out->m);
+  };
+  Loaded cur, nxt;
+  load(1, &cur);
+  for (int it = 1; it < T; ++it) {
+    std::thread reader;
+    if (it + 1 < T) reader = std::thread(load, it + 1, &nxt);
+    if (cur.st != TSVD_OK) {
+      if (reader.joinable()) reader.join();
+      return die(shots[it].c_str(), cur.st);
+    }
+    st = tsvd_session_step(s, cur.edges, cur.m);
+    tsvd_free(cur.edges);
+    cur.edges = nullptr;
+    if (reader.joinable()) reader.join();
     if (st != TSVD_OK) return die("step", st);
+    cur = nxt;
+    nxt = Loaded();
     tsvd_step_stats ss;
     tsvd_session_last_stats(s, &ss);
     std::printf("Iter = %d, edges %lld, pushes %lld, dirty %d, time = %.3f ms\n", it,
@@ -195,5 +302,12 @@ int main(int argc, char **argv) {
     if (r + 1 < rows) os << "\n";
   }
   std::printf("wrote %s\n", out.c_str());
+  if (npy) {
+    if (!write_npy(out + ".npy", all, rows, d)) {
+      std::fprintf(stderr, "tree_svd: cannot write %s.npy\n", out.c_str());
+      return 1;
+    }
+    std::printf("wrote %s.npy\n", out.c_str());
+  }
   return 0;
 }

@@ -197,6 +197,33 @@ extern "C" tsvd_status tsvd_read_edge_file(const char *path,
                                            int32_t compat_dup_last,
                                            int32_t **edges, int64_t *m) {
   if (!path || !edges || !m) return tsvd::fail(TSVD_ERR_INVALID, "read_edge_file: null");
+  const size_t plen = std::strlen(path);
+  if (plen > 4 && std::strcmp(path + plen - 4, ".bin") == 0) {
+    // binary: raw int32 (from, to) pairs in host byte order
+    FILE *fb = std::fopen(path, "rb");
+    if (!fb) return tsvd::fail(TSVD_ERR_IO, "cannot open %s: %s", path, std::strerror(errno));
+    std::fseek(fb, 0, SEEK_END);
+    const long bytes = std::ftell(fb);
+    std::fseek(fb, 0, SEEK_SET);
+    if (bytes < 0 || bytes % 8) {
+      std::fclose(fb);
+      return tsvd::fail(TSVD_ERR_IO, "%s: size %ld is not a whole number of int32 pairs", path, bytes);
+    }
+    int32_t *out = (int32_t *)std::malloc(std::max<long>(bytes, 8));
+    if (!out) {
+      std::fclose(fb);
+      return tsvd::fail(TSVD_ERR_OOM, "read_edge_file: malloc");
+    }
+    const size_t got = std::fread(out, 1, (size_t)bytes, fb);
+    std::fclose(fb);
+    if (got != (size_t)bytes) {
+      std::free(out);
+      return tsvd::fail(TSVD_ERR_IO, "%s: short read", path);
+    }
+    *edges = out;
+    *m = bytes / 8;
+    return TSVD_OK;
+  }
   FILE *f = std::fopen(path, "rb");
   if (!f) return tsvd::fail(TSVD_ERR_IO, "cannot open %s: %s", path, std::strerror(errno));
   std::vector<char> buf;
@@ -246,4 +273,16 @@ extern "C" void tsvd_free(void *p) { std::free(p); }
 extern "C" float tsvd_gaussian(uint64_t seed, uint32_t stream, uint32_t row,
                                uint32_t col) {
   return tsvd_gauss_entry(seed, stream, row, col);
+}
+
+extern "C" tsvd_status tsvd_write_edge_file_binary(const char *path, const int32_t *edges,
+                                                   int64_t m) {
+  if (!path || (m > 0 && !edges) || m < 0) return tsvd::fail(TSVD_ERR_INVALID, "write_edge_file: bad arguments");
+  FILE *f = std::fopen(path, "wb");
+  if (!f) return tsvd::fail(TSVD_ERR_IO, "cannot create %s: %s", path, std::strerror(errno));
+  const size_t want = (size_t)m * 2 * sizeof(int32_t);
+  const size_t put = want ? std::fwrite(edges, 1, want, f) : 0;
+  const int rc = std::fclose(f);
+  if (put != want || rc != 0) return tsvd::fail(TSVD_ERR_IO, "%s: short write", path);
+  return TSVD_OK;
 }

@@ -113,6 +113,7 @@ _SIGS = {
     "tsvd_read_edge_file": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int32,
                                            ctypes.POINTER(_i32p), _i64p]),
     "tsvd_free": (None, [_vp]),
+    "tsvd_write_edge_file_binary": (ctypes.c_int, [ctypes.c_char_p, _i32p, ctypes.c_int64]),
     "tsvd_gaussian": (ctypes.c_float, [ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32,
                                        ctypes.c_uint32]),
     "frPCA": (None, [_vp, _vp, _vp, _vp, ctypes.c_int, ctypes.c_int]),
@@ -182,6 +183,11 @@ def read_edge_file(path, compat_dup_last=False):
     return arr.reshape(-1, 2)
 
 
+def write_edge_file_binary(path, edges):
+    e = np.ascontiguousarray(edges, dtype=np.int32).reshape(-1, 2)
+    _check(lib().tsvd_write_edge_file_binary(os.fsencode(path), _p(e, _i32p), e.shape[0]))
+
+
 def gaussian(seed, stream, row, col):
     return lib().tsvd_gaussian(seed, stream, row, col)
 
@@ -226,7 +232,7 @@ class Session:
                  dynamic_ppr_start_iter=100, lazy_update_start_iter=100, delta=0.3,
                  transform=TRANSFORM_LOG10_NC, dirty_rule=DIRTY_REFERENCE, dirty_frac=0.01,
                  root_scaling=ROOT_SQRT_SIGMA, refresh_mode=REFRESH_EXACT, seed=20231, device=0,
-                 max_push_rounds=0, push_levels=1, push_ratio=8.0, push_cofrac=1.0,
+                 max_push_rounds=0, push_levels=1, push_ratio=8.0, push_cofrac=0.5,
                  lp_right_factor=False):
         self.sources = np.ascontiguousarray(sources, dtype=np.int32)
         c = Config()
