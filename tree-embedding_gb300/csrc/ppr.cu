@@ -38,6 +38,7 @@ __device__ __forceinline__ void mark_pair(uint32_t *bits, int32_t u, int32_t c, 
   atomicOr(bits + (idx >> 5), 1u << (idx & 31));
 }
 
+
 struct StatAcc {
   unsigned long long pushes = 0, upd = 0, items = 0, iedges = 0;
 };
@@ -56,20 +57,23 @@ __device__ __forceinline__ void flush_stats(const StatAcc &acc, unsigned long lo
 // Scatter w (per lane) of vertex v's chunk c to neighbours [j0, j1):
 // fire-and-forget atomic adds (RED), and every neighbour's (u, chunk) is
 // marked in the touched bitset for collect_kernel.
-__device__ __forceinline__ void scatter_range(const PushArgs &a, int32_t v, int32_t c,
-                                              bool act, float w, int32_t j0, int32_t j1) {
+__device__ __forceinline__ void scatter_range(const PushArgs &a, const int32_t *nb, int32_t c,
+                                              bool act, float w, int32_t j0, int32_t j1,
+                                              int32_t mine) {
   const int lane = threadIdx.x & 31;
   float *rc = a.r + (int64_t)c * a.n * 32 + lane;  // r cell of (u, c * 32 + lane) = rc + 32 u
-  const int32_t *nb = a.nbr + a.off[v];
+  // `mine` holds the ids of neighbours [j0, j0 + 32); each batch loads the
+  // next batch's ids before issuing its own atomics
   for (int32_t jb = j0; jb < j1; jb += 32) {
     const int32_t jn = min(32, j1 - jb);
-    const int32_t mine = lane < jn ? __ldg(nb + jb + lane) : 0;
+    const int32_t next = lane < j1 - jb - 32 ? __ldg(nb + jb + 32 + lane) : 0;
     for (int32_t t = 0; t < jn; ++t) {
       const int32_t u = __shfl_sync(kFull, mine, t);
       if (act) atomicAdd(rc + (int64_t)u * 32, w);
     }
     // each lane marks the neighbour it loaded: 32 independent reductions
     if (lane < jn) mark_pair(a.tflag, mine, c, a.n);
+    mine = next;
   }
 }
 
@@ -84,10 +88,18 @@ __global__ void __launch_bounds__(256) push_kernel(PushArgs a) {
     const int32_t v = it.x, c = it.y;
     // the warp's next item is loaded while this one is pushed
     it = i + nw < nitems ? __ldg(a.front + i + nw) : make_int2(0, 0);
+    // Everything the item needs that does not depend on its residues is
+    // requested at once: degree, row start, reserve line, first neighbour ids
+    // (only this warp writes the reserve of (v, chunk c) in a round).
     const int32_t d = a.deg[v];
+    const int64_t o = a.off[v];
     const int32_t s = c * 32 + lane;
     float *rp = a.r + ppr_cell(v, s, a.n);
+    float *pp = a.p + ppr_cell(v, s, a.n);
     float x = __ldcg(rp);
+    const float pv = __ldcg(pp);
+    const int32_t *nb = a.nbr + o;
+    const int32_t mine0 = lane < d ? __ldg(nb + lane) : 0;
     // push above the current level of the threshold schedule; lanes between
     // rmax and that level are parked in the pending set for a later level
     bool act = s < a.nsrc && x > a.theta_f;
@@ -109,16 +121,13 @@ __global__ void __launch_bounds__(256) push_kernel(PushArgs a) {
       // Isolated source of an undirected graph: the reference assigns
       // pi = alpha * r and keeps r (ppr:1433-1441); directed dangling
       // vertices are skipped (ppr:2971-2976).
-      if (a.undirected && act) a.p[ppr_cell(v, s, a.n)] = a.alpha_f * x;
+      if (a.undirected && act) *pp = a.alpha_f * x;
       if (a.undirected && lane == 0 && a.vmark[v] == 0) a.vmark[v] = 1;
       continue;
     }
     if (act) x = atomicExch(rp, 0.0f);
     const float w = act ? x * (a.one_minus_alpha_f / (float)d) : 0.0f;
-    if (act) {
-      float *pp = a.p + ppr_cell(v, s, a.n);
-      *pp = fmaf(a.alpha_f, x, *pp);
-    }
+    if (act) *pp = fmaf(a.alpha_f, x, pv);
     if (lane == 0) {
       if (a.vmark[v] == 0) a.vmark[v] = 1;
       acc.pushes += __popc(mask);
@@ -153,7 +162,7 @@ __global__ void __launch_bounds__(256) push_kernel(PushArgs a) {
       if (ok) continue;
       // buffers full: process this hub inline
     }
-    scatter_range(a, v, c, act, w, 0, d);
+    scatter_range(a, nb, c, act, w, 0, d, mine0);
   }
   flush_stats(acc, a.stats);
 }
@@ -170,8 +179,11 @@ __global__ void __launch_bounds__(256) push_heavy_kernel(PushArgs a) {
     unsigned mask = a.heavy_mask[u.x];
     float w = a.heavy_w[(int64_t)u.x * 32 + lane];
     bool act = (mask >> lane) & 1u;
-    int32_t d = a.deg[it.x];
-    scatter_range(a, it.x, it.y, act, w, u.y, min(d, u.y + kHeavy));
+    const int32_t d = a.deg[it.x];
+    const int32_t *nb = a.nbr + a.off[it.x];
+    const int32_t j1 = min(d, u.y + kHeavy);
+    const int32_t mine0 = lane < j1 - u.y ? __ldg(nb + u.y + lane) : 0;
+    scatter_range(a, nb, it.y, act, w, u.y, j1, mine0);
   }
 }
 
