@@ -599,23 +599,21 @@ struct JacobiArgs {
 };
 
 __global__ void __launch_bounds__(JAC_THREADS) jacobi_kernel(JacobiArgs a) {
-  extern __shared__ __align__(16) float G[];  // packed upper triangle, then the pair table
+  extern __shared__ __align__(16) float G[];  // packed upper triangle
   __shared__ float pc[128], ps[128], pt[128];
   __shared__ int pp[128], pq[128];
   __shared__ int rotated;
   __shared__ float dmax;
   const int n = a.n, np = n + (n & 1), P = np / 2;
-  const int npairs = P * (P + 1) / 2;
-  uint16_t *tab = reinterpret_cast<uint16_t *>(G + n * (n + 1) / 2);
+  const int R = (P + 1) / 2;               // block-row groups
+  const int Gs = (int)blockDim.x / R;      // threads per group (P <= 128: >= 16)
+  const int r = (int)threadIdx.x / Gs, jg = (int)threadIdx.x % Gs;
   const int prob = blockIdx.x;
   const double *Gin = a.g[prob];
   for (int idx = threadIdx.x; idx < n * n; idx += blockDim.x) {
     int i = idx / n, j = idx % n;
     if (i <= j) G[packed(i, j)] = (float)Gin[idx];
   }
-  // (k1 <= k2) pairs of rotation pairs, packed k1 << 8 | k2
-  for (int k2 = threadIdx.x; k2 < P; k2 += blockDim.x)
-    for (int k1 = 0; k1 <= k2; ++k1) tab[k2 * (k2 + 1) / 2 + k1] = (uint16_t)((k1 << 8) | k2);
   float2 *log = a.log + (int64_t)prob * JAC_MAX_SWEEPS * (np - 1) * P;
   __syncthreads();
   int sweep = 0;
@@ -653,31 +651,43 @@ __global__ void __launch_bounds__(JAC_THREADS) jacobi_kernel(JacobiArgs a) {
       }
       __syncthreads();
       // G <- J^T G J, 2x2 block by 2x2 block; each entry belongs to one block.
-      for (int b = threadIdx.x; b < npairs; b += blockDim.x) {
-        const int k1 = tab[b] >> 8, k2 = tab[b] & 0xff;
-        const int p1 = pp[k1], q1 = pq[k1], p2 = pp[k2], q2 = pq[k2];
-        if (k1 == k2) {
-          if (q1 < n && pt[k1] != 0.f) {
-            float apq = G[packed(p1, q1)];
-            G[packed(p1, p1)] -= pt[k1] * apq;
-            G[packed(q1, q1)] += pt[k1] * apq;
-            G[packed(p1, q1)] = 0.f;
+      // Thread group r owns the block rows k1 = r and k1 = P-1-r (P+1 blocks
+      // together, so the groups are balanced) and loads their rotations once.
+      if (r < R) {
+        const int ra = r, rb = P - 1 - r;
+        const int na = P - ra, ntot = ra == rb ? na : na + r + 1;
+        const int pa_ = pp[ra], qa = pq[ra], pb_ = pp[rb], qb = pq[rb];
+        const float ca = pc[ra], sa = ps[ra], ta = pt[ra];
+        const float cb = pc[rb], sb = ps[rb], tb = pt[rb];
+        for (int e = jg; e < ntot; e += Gs) {
+          const bool first = e < na;
+          const int k2 = first ? ra + e : rb + (e - na);
+          const int p1 = first ? pa_ : pb_, q1 = first ? qa : qb;
+          const float c1 = first ? ca : cb, s1 = first ? sa : sb, t1 = first ? ta : tb;
+          if (k2 == (first ? ra : rb)) {  // diagonal block: the rotation's own pair
+            if (q1 < n && t1 != 0.f) {
+              const float apq = G[packed(p1, q1)];
+              G[packed(p1, p1)] -= t1 * apq;
+              G[packed(q1, q1)] += t1 * apq;
+              G[packed(p1, q1)] = 0.f;
+            }
+            continue;
           }
-          continue;
+          const float c2 = pc[k2], s2 = ps[k2];
+          if (s1 == 0.f && s2 == 0.f) continue;
+          const int p2 = pp[k2], q2 = pq[k2];
+          const bool hq1 = q1 < n, hq2 = q2 < n;
+          float b00 = G[pk(p1, p2)];
+          float b01 = hq2 ? G[pk(p1, q2)] : 0.f;
+          float b10 = hq1 ? G[pk(q1, p2)] : 0.f;
+          float b11 = (hq1 && hq2) ? G[pk(q1, q2)] : 0.f;
+          float t00 = c1 * b00 - s1 * b10, t01 = c1 * b01 - s1 * b11;
+          float t10 = s1 * b00 + c1 * b10, t11 = s1 * b01 + c1 * b11;
+          G[pk(p1, p2)] = t00 * c2 - t01 * s2;
+          if (hq2) G[pk(p1, q2)] = t00 * s2 + t01 * c2;
+          if (hq1) G[pk(q1, p2)] = t10 * c2 - t11 * s2;
+          if (hq1 && hq2) G[pk(q1, q2)] = t10 * s2 + t11 * c2;
         }
-        const float c1 = pc[k1], s1 = ps[k1], c2 = pc[k2], s2 = ps[k2];
-        if (s1 == 0.f && s2 == 0.f) continue;
-        const bool hq1 = q1 < n, hq2 = q2 < n;
-        float b00 = G[pk(p1, p2)];
-        float b01 = hq2 ? G[pk(p1, q2)] : 0.f;
-        float b10 = hq1 ? G[pk(q1, p2)] : 0.f;
-        float b11 = (hq1 && hq2) ? G[pk(q1, q2)] : 0.f;
-        float t00 = c1 * b00 - s1 * b10, t01 = c1 * b01 - s1 * b11;
-        float t10 = s1 * b00 + c1 * b10, t11 = s1 * b01 + c1 * b11;
-        G[pk(p1, p2)] = t00 * c2 - t01 * s2;
-        if (hq2) G[pk(p1, q2)] = t00 * s2 + t01 * c2;
-        if (hq1) G[pk(q1, p2)] = t10 * c2 - t11 * s2;
-        if (hq1 && hq2) G[pk(q1, q2)] = t10 * s2 + t11 * c2;
       }
       __syncthreads();
     }
@@ -941,7 +951,7 @@ tsvd_status jacobi_eig_batched(double *const *g, int n, float *const *lambda, fl
   w += round_up((size_t)nprob * sizeof(int32_t), 256);
   a.rank = (int32_t *)w;
   const int P = np / 2;
-  size_t smem = (size_t)n * (n + 1) / 2 * sizeof(float) + (size_t)P * (P + 1) / 2 * sizeof(uint16_t);
+  size_t smem = (size_t)n * (n + 1) / 2 * sizeof(float);
   static size_t cur = 0;
   if (smem > cur) {
     TSVD_TRY(set_smem((const void *)jacobi_kernel, smem));

@@ -189,10 +189,14 @@ __global__ void __launch_bounds__(256) push_heavy_kernel(PushArgs a) {
 
 // Scan the touched bitset; for each touched (u, chunk) with some residue
 // above theta and deg(u) > 0, append it to the next frontier. Clears the bits.
+// A warp takes the set bits of a word four at a time: lane group g (8 lanes)
+// reads pair g's 128-byte residue line as eight float4, so four lines are in
+// flight per warp instruction. Padding sources (s >= |S|) hold zero residue.
 __global__ void __launch_bounds__(256) collect_kernel(CollectArgs a) {
   __shared__ int2 buf[2048];
   __shared__ int32_t nbuf, gbase;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int grp = lane >> 3, gl = lane & 7;
   const int64_t words_per_iter = 64;  // 8 warps x 8 words
   for (int64_t w0 = (int64_t)blockIdx.x * words_per_iter; w0 < a.nwords;
        w0 += (int64_t)gridDim.x * words_per_iter) {
@@ -205,17 +209,36 @@ __global__ void __launch_bounds__(256) collect_kernel(CollectArgs a) {
       if (!bits) continue;
       if (lane == 0) a.tflag[wi] = 0;
       while (bits) {
-        const int b = __ffs(bits) - 1;
-        bits &= bits - 1;
-        const int64_t idx = wi * 32 + b;
-        const int32_t u = (int32_t)(idx % a.n), c = (int32_t)(idx / a.n);
-        if (a.deg[u] == 0) continue;
-        const int32_t s = c * 32 + lane;
-        const float x = s < a.nsrc ? __ldcg(a.r + ppr_cell(u, s, a.n)) : 0.0f;
-        if (__ballot_sync(kFull, x > a.theta_f)) {
-          if (lane == 0) buf[atomicAdd(&nbuf, 1)] = make_int2(u, c);
-        } else if (a.theta_f > a.rmax_f && __ballot_sync(kFull, x > a.rmax_f)) {
-          if (lane == 0) mark_pair(a.pend, u, c, a.n);  // for a lower level
+        // the next (up to) four set bits, one per lane group
+        uint32_t rest = bits;
+        int mybit = -1;
+        for (int g = 0; g < 4 && rest; ++g) {
+          const int bpos = __ffs(rest) - 1;
+          rest &= rest - 1;
+          if (g == grp) mybit = bpos;
+        }
+        bits = rest;
+        int32_t u = 0, c = 0;
+        bool live = mybit >= 0;
+        if (live) {
+          const int64_t idx = wi * 32 + mybit;
+          u = (int32_t)(idx % a.n);
+          c = (int32_t)(idx / a.n);
+          live = a.deg[u] != 0;
+        }
+        float m = 0.f;
+        if (live) {
+          const float4 x4 = __ldcg(reinterpret_cast<const float4 *>(
+              a.r + ppr_cell(u, c * 32 + gl * 4, a.n)));
+          m = fmaxf(fmaxf(x4.x, x4.y), fmaxf(x4.z, x4.w));
+        }
+        const unsigned above = __ballot_sync(kFull, live && m > a.theta_f);
+        const unsigned parked = a.theta_f > a.rmax_f
+                                    ? __ballot_sync(kFull, live && m > a.rmax_f) & ~above : 0u;
+        const unsigned gmask = 0xFFu << (grp * 8);
+        if (gl == 0 && live) {
+          if (above & gmask) buf[atomicAdd(&nbuf, 1)] = make_int2(u, c);
+          else if (parked & gmask) mark_pair(a.pend, u, c, a.n);  // for a lower level
         }
       }
     }
