@@ -189,14 +189,15 @@ __global__ void __launch_bounds__(256) push_heavy_kernel(PushArgs a) {
 
 // Scan the touched bitset; for each touched (u, chunk) with some residue
 // above theta and deg(u) > 0, append it to the next frontier. Clears the bits.
-// A warp takes the set bits of a word four at a time: lane group g (8 lanes)
-// reads pair g's 128-byte residue line as eight float4, so four lines are in
-// flight per warp instruction. Padding sources (s >= |S|) hold zero residue.
+// A warp takes the set bits of a word eight at a time: lane group g (4 lanes)
+// reads pair g's 128-byte residue line as eight float4 (two per lane), so
+// eight lines are in flight per warp. Padding sources (s >= |S|) hold zero
+// residue.
 __global__ void __launch_bounds__(256) collect_kernel(CollectArgs a) {
   __shared__ int2 buf[2048];
   __shared__ int32_t nbuf, gbase;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int grp = lane >> 3, gl = lane & 7;
+  const int grp = lane >> 2, gl = lane & 3;
   const int64_t words_per_iter = 64;  // 8 warps x 8 words
   for (int64_t w0 = (int64_t)blockIdx.x * words_per_iter; w0 < a.nwords;
        w0 += (int64_t)gridDim.x * words_per_iter) {
@@ -209,10 +210,10 @@ __global__ void __launch_bounds__(256) collect_kernel(CollectArgs a) {
       if (!bits) continue;
       if (lane == 0) a.tflag[wi] = 0;
       while (bits) {
-        // the next (up to) four set bits, one per lane group
+        // the next (up to) eight set bits, one per lane group
         uint32_t rest = bits;
         int mybit = -1;
-        for (int g = 0; g < 4 && rest; ++g) {
+        for (int g = 0; g < 8 && rest; ++g) {
           const int bpos = __ffs(rest) - 1;
           rest &= rest - 1;
           if (g == grp) mybit = bpos;
@@ -228,14 +229,15 @@ __global__ void __launch_bounds__(256) collect_kernel(CollectArgs a) {
         }
         float m = 0.f;
         if (live) {
-          const float4 x4 = __ldcg(reinterpret_cast<const float4 *>(
-              a.r + ppr_cell(u, c * 32 + gl * 4, a.n)));
-          m = fmaxf(fmaxf(x4.x, x4.y), fmaxf(x4.z, x4.w));
+          const float4 *line = reinterpret_cast<const float4 *>(a.r + ppr_cell(u, c * 32, a.n));
+          const float4 x0 = __ldcg(line + gl), x1 = __ldcg(line + gl + 4);
+          m = fmaxf(fmaxf(fmaxf(x0.x, x0.y), fmaxf(x0.z, x0.w)),
+                    fmaxf(fmaxf(x1.x, x1.y), fmaxf(x1.z, x1.w)));
         }
         const unsigned above = __ballot_sync(kFull, live && m > a.theta_f);
         const unsigned parked = a.theta_f > a.rmax_f
                                     ? __ballot_sync(kFull, live && m > a.rmax_f) & ~above : 0u;
-        const unsigned gmask = 0xFFu << (grp * 8);
+        const unsigned gmask = 0xFu << (grp * 4);
         if (gl == 0 && live) {
           if (above & gmask) buf[atomicAdd(&nbuf, 1)] = make_int2(u, c);
           else if (parked & gmask) mark_pair(a.pend, u, c, a.n);  // for a lower level
