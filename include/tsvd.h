@@ -215,6 +215,8 @@ typedef struct tsvd_step_stats {
   double ms_materialize_kernel; /* device time of the block materialization      */
   int64_t push_item_edges;  /* sum of deg(v) over pushed items (neighbour-list reads) */
   double ms_lp;             /* LP right factor of the refreshed blocks            */
+  int32_t eig_sweeps_frpca; /* Jacobi sweeps of the blocks' eigSVD (max)          */
+  int32_t eig_sweeps_merge; /* Jacobi sweeps of the merges (max over levels)      */
 } tsvd_step_stats;
 tsvd_status tsvd_session_last_stats(tsvd_session *s, tsvd_step_stats *out);
 

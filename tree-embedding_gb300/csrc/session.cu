@@ -526,6 +526,7 @@ static tsvd_status stage_factorize(tsvd_session *s, int iter) {
   }
   std::vector<double> ssum(nf);
   TSVD_TRY(frpca_batch(s->fw, probs.data(), nf, s->q, s->cfg.seed, s->S, s->st, ssum.data()));
+  s->last.eig_sweeps_frpca = s->fw.last_sweeps;
   // Residual ||A - U S V^T||_F = sqrt(||A||^2 - sum sigma^2) for an orthonormal
   // basis (the reference forms the dense product, Tree_u_NC.cpp:158-204).
   if (iter >= s->cfg.lazy_update_start_iter - 1)
@@ -558,6 +559,7 @@ static tsvd_status stage_merge(tsvd_session *s) {
     int mode = 0;
     if (root) mode = s->cfg.root_scaling == TSVD_ROOT_U ? 2 : 1;
     TSVD_TRY(merge_batch(s->fw, probs.data(), (int)probs.size(), h, s->S, mode, s->st));
+    s->last.eig_sweeps_merge = std::max(s->last.eig_sweeps_merge, s->fw.last_sweeps);
     s->last.merged_nodes += (int)probs.size();
     if (root) {
       TSVD_CUDA(cudaMemcpyAsync(s->node_b(0), s->embedding, sizeof(float) * s->node_elems(),
