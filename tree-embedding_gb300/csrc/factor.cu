@@ -3,9 +3,10 @@
 // frPCA follows Code/frpca.c:239-326 (k = d, s = l - d oversampling, q
 // passes over A): a Gaussian start (frpca.c:257), products with A and A^T,
 // a normalization after every product, and a final eigSVD of A^T Q
-// (frpca.c:294-312). Normalizations use CholeskyQR2 where the reference uses
-// LU (LUfraction) or eigSVD; all three return a basis of the same column
-// space, which is the only thing the next product consumes. Normalizing
+// (frpca.c:294-312). Normalizations use CholeskyQR (one pass between
+// products, CholeskyQR2 for the final basis) where the reference uses LU
+// (LUfraction) or eigSVD; all return a basis of the same column space, which
+// is the only thing the next product consumes. Normalizing
 // A^T Q as well keeps every basis within one condition number of A, so the
 // half-precision split operands stay accurate.
 //
@@ -143,16 +144,19 @@ __global__ void concat_kernel(const float *const *children, int h, int d, int ns
   }
 }
 
-tsvd_status cholqr2(FrpcaWork &W, float *const *x, const int32_t *rows, int max_rows,
-                    double *const *g, float *const *t, __half *const *hi, __half *const *lo,
-                    int nprob, cudaStream_t st) {
-  for (int pass = 0; pass < 2; ++pass) {
+// CholeskyQR with `passes` passes (2 = CholeskyQR2); the last pass also writes
+// the fp16 hi/lo split of the basis.
+tsvd_status cholqr(FrpcaWork &W, float *const *x, const int32_t *rows, int max_rows,
+                   double *const *g, float *const *t, __half *const *hi, __half *const *lo,
+                   int nprob, cudaStream_t st, int passes) {
+  for (int pass = 0; pass < passes; ++pass) {
+    const bool last = pass == passes - 1;
     TSVD_TRY(gram_batched((const float *const *)x, rows, max_rows, W.l, kLp, g, W.gram_work,
                           W.gram_bytes, nprob, st));
     TSVD_TRY(chol_inverse_batched(g, t, W.l, nprob, st));
     TSVD_TRY(apply_right_batched((const float *const *)x, rows, max_rows, kLp,
                                  (const float *const *)t, kLp, W.l, W.l, nullptr, x, kLp,
-                                 pass ? hi : nullptr, pass ? lo : nullptr, kSplitScale, nprob,
+                                 last ? hi : nullptr, last ? lo : nullptr, kSplitScale, nprob,
                                  st));
   }
   return TSVD_OK;
@@ -278,6 +282,7 @@ tsvd_status frpca_batch(FrpcaWork &W, const FrpcaProblem *probs, int nprob, int 
 
   GemmBatch gb{d_at, d_nc, sp, nprob};
   const size_t ybytes = (size_t)nprob * SK * sizeof(float);
+  const int niter = (q - 1) / 2;
   float in_scale = 1.f / kSplitScale;
   if (q % 2 == 0) {
     omega_kernel<<<dim3(grid_for((int64_t)max_nc * kLp, 256, 4), nprob), 256, 0, st>>>(
@@ -285,7 +290,7 @@ tsvd_status frpca_batch(FrpcaWork &W, const FrpcaProblem *probs, int nprob, int 
     TSVD_LAUNCH_CHECK();
     TSVD_TRY(gemm_fwd(gb, (const __half *const *)d_xhi, nullptr, d_y, W.y, ybytes, sp, max_nc,
                       1.f, st));
-    TSVD_TRY(cholqr2(W, d_y, d_sprows, sp, d_g, d_t, d_qhi, d_qlo, nprob, st));
+    TSVD_TRY(cholqr(W, d_y, d_sprows, sp, d_g, d_t, d_qhi, d_qlo, nprob, st, niter ? 1 : 2));
   } else {
     const float split = 2048.f;
     randq_kernel<<<dim3(grid_for(SK, 256, 4), nprob), 256, 0, st>>>(d_y, d_qhi, d_qlo, d_blk, sp,
@@ -293,14 +298,18 @@ tsvd_status frpca_batch(FrpcaWork &W, const FrpcaProblem *probs, int nprob, int 
     TSVD_LAUNCH_CHECK();
     in_scale = 1.f / split;
   }
-  const int niter = (q - 1) / 2;
+  // Between products one CholeskyQR pass suffices: every product multiplies
+  // the condition number of an (almost) orthonormal basis by at most
+  // sigma_1 / sigma_l of A, and only the span goes on (the reference uses an
+  // LU factor there, frpca.c:261-291). The last basis Q, which B = Q V S is
+  // built from, gets both passes.
   for (int it = 1; it <= niter; ++it) {
     TSVD_TRY(gemm_bwd(gb, (const __half *const *)d_qhi, (const __half *const *)d_qlo, d_z, sp,
                       max_nc, in_scale, st));
-    TSVD_TRY(cholqr2(W, d_z, d_nc, max_nc, d_g, d_t, d_xhi, d_xlo, nprob, st));
+    TSVD_TRY(cholqr(W, d_z, d_nc, max_nc, d_g, d_t, d_xhi, d_xlo, nprob, st, 1));
     TSVD_TRY(gemm_fwd(gb, (const __half *const *)d_xhi, (const __half *const *)d_xlo, d_y, W.y,
                       ybytes, sp, max_nc, 1.f / kSplitScale, st));
-    TSVD_TRY(cholqr2(W, d_y, d_sprows, sp, d_g, d_t, d_qhi, d_qlo, nprob, st));
+    TSVD_TRY(cholqr(W, d_y, d_sprows, sp, d_g, d_t, d_qhi, d_qlo, nprob, st, it == niter ? 2 : 1));
     in_scale = 1.f / kSplitScale;
   }
   TSVD_TRY(gemm_bwd(gb, (const __half *const *)d_qhi, (const __half *const *)d_qlo, d_z, sp,
