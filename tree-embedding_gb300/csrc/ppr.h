@@ -4,18 +4,21 @@
 
 namespace tsvd {
 
-// Cell of (vertex v, source s) in the chunk-major r / p arrays: the 32
-// sources of one chunk of one vertex share a 128-byte line, and the lines of
+// Sources per chunk. The kChunk sources of one chunk of one vertex share a
+// 256-byte pair of lines; a warp holds them as one float2 per lane.
+constexpr int kChunk = 64;
+
+// Cell of (vertex v, source s) in the chunk-major r / p arrays: the lines of
 // one chunk are contiguous over the n vertices.
 __host__ __device__ __forceinline__ int64_t ppr_cell(int32_t v, int32_t s, int32_t n) {
-  return ((int64_t)(s >> 5) * n + v) * 32 + (s & 31);
+  return ((int64_t)(s >> 6) * n + v) * kChunk + (s & (kChunk - 1));
 }
 
 constexpr int kStatSlots = 64;  // push counters are spread over this many slots
 
 struct PprState {
   int32_t n = 0, nsrc = 0, sp = 0, chunks = 0;
-  float *r = nullptr, *p = nullptr;  // [chunks][n][32], see ppr_cell
+  float *r = nullptr, *p = nullptr;  // [chunks][n][kChunk], see ppr_cell
   uint32_t *tflag = nullptr;         // touched (vertex, chunk) bitset, chunk-major
   uint32_t *pend = nullptr;          // parked below the current threshold level
   int64_t nwords = 0;                // words of either bitset
