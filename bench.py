@@ -44,6 +44,13 @@ def parse():
     ap.add_argument("--sources", type=int, default=None)
     ap.add_argument("--parts", type=int, default=None)
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--host-reserve", action="store_true",
+                    help="keep the PPR reserve in pinned host memory (ppr_host_reserve), for "
+                         "workloads whose state exceeds HBM (rmat-d-6.2m)")
+    ap.add_argument("--pipelined", action="store_true",
+                    help="time tsvd_session_run (factor stage of snapshot k overlapped with the "
+                         "push of k+1: more snapshots/s, longer per-snapshot latency) instead of "
+                         "one tsvd_session_step per snapshot")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--seed", type=int, default=20231)
     return ap.parse_args()
@@ -127,16 +134,27 @@ def peaks():
 
 # ------------------------------------------------------------------ our arm
 def run_ours(args, cfg, snaps, sources, device):
+    """Our arm. Each timed snapshot is one tsvd_session_step(_device) call, or
+    with --pipelined all K go through one tsvd_session_run(_device) call (the
+    factor stage of snapshot k overlapped with the push of snapshot k+1).
+    Every snapshot is complete (embedding written) inside the timed region.
+    Per-snapshot latency (stats ms_total) runs from the start of a snapshot's
+    insert to the end of its factor stage."""
     import torch
     import tsvd_gb300 as T
     import workloads as W
 
     torch.cuda.set_device(device)
-    kw = W.session_kwargs(cfg, dynamic_start=2, lazy_start=2, seed=args.seed)
+    kw = W.session_kwargs(cfg, dynamic_start=2, lazy_start=2)
     kw["device"] = device
-    timed = snaps[1 + args.warmup: 1 + args.warmup + args.steps]
-    # --- device-resident inputs: all deltas uploaded before the timed region
-    dev = [torch.from_numpy(np.ascontiguousarray(e)).to(f"cuda:{device}") for e in snaps]
+    kw["seed"] = args.seed
+    kw["ppr_host_reserve"] = args.host_reserve
+    t0i, t1i = 1 + args.warmup, 1 + args.warmup + args.steps
+    timed = snaps[t0i:t1i]
+    off = np.concatenate([[0], np.cumsum([len(e) for e in timed])]).astype(np.int64)
+    # --- device-resident inputs: every delta uploaded before the timed region
+    dev = [torch.from_numpy(np.ascontiguousarray(e)).to(f"cuda:{device}") for e in snaps[:t0i]]
+    dev_timed = torch.from_numpy(np.ascontiguousarray(np.concatenate(timed))).to(f"cuda:{device}")
     res = {}
     with T.Session(cfg["n"], sources, **kw) as s:
         s.step_device(dev[0].data_ptr(), len(snaps[0]))  # set-up: first snapshot, from scratch
@@ -144,61 +162,68 @@ def run_ours(args, cfg, snaps, sources, device):
             s.step_device(dev[1 + k].data_ptr(), len(snaps[1 + k]))
         stream = torch.cuda.ExternalStream(s.stream(), device=device)
         ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        per_step, stage = [], []
         launches0 = T.launch_count()
         torch.cuda.synchronize(device)
         with ClockSampler(device) as clk:
             ev0.record(stream)
             t0 = time.perf_counter()
-            for k in range(args.steps):
-                i = 1 + args.warmup + k
-                s.step_device(dev[i].data_ptr(), len(snaps[i]))
-                st = s.stats()
-                per_step.append(st["ms_total"])
-                stage.append(st)
-            ev1.record(stream)
+            if args.pipelined:
+                stage, _ = s.run_device(dev_timed.data_ptr(), off, embeddings=False)
+            else:
+                stage = []
+                for k in range(args.steps):
+                    s.step_device(dev_timed.data_ptr() + int(off[k]) * 8, int(off[k + 1] - off[k]))
+                    stage.append(s.stats())
+            ev1.record(stream)  # after the calls returned: every snapshot is complete
             torch.cuda.synchronize(device)
             wall = time.perf_counter() - t0
         launches = T.launch_count() - launches0
         ms = ev0.elapsed_time(ev1)
-        res.update(ms=ms, wall=wall, per_step=per_step, stages=stage, launches=launches,
-                   clocks=clk.summary(), edges=int(sum(len(e) for e in timed)))
-    del dev
+        res.update(ms=ms, wall=wall, per_step=[st["ms_total"] for st in stage], stages=stage,
+                   launches=launches, clocks=clk.summary(), edges=int(off[-1]))
+    del dev, dev_timed
     torch.cuda.empty_cache()
     if args.no_e2e:
         return res
-    # --- end to end through the C-ABI with host buffers (pinned), result read back
-    pinned = [torch.from_numpy(np.ascontiguousarray(e)).pin_memory() for e in snaps]
-    emb = np.zeros((len(sources), cfg["rank_d"]), np.float64)
+    # --- end to end through the C-ABI: host edges (pinned) copied in and every
+    # snapshot's embedding read back inside the timed region
+    pinned_timed = torch.from_numpy(np.ascontiguousarray(np.concatenate(timed))).pin_memory()
     import ctypes
     with T.Session(cfg["n"], sources, **kw) as s:
         L = T.lib()
-        step = lambda i: T._check(L.tsvd_session_step(
-            s._h, ctypes.cast(pinned[i].data_ptr(), ctypes.POINTER(ctypes.c_int32)), len(snaps[i])))
-        step(0)
-        for k in range(args.warmup):
-            step(1 + k)
+        for i in range(t0i):
+            e = torch.from_numpy(np.ascontiguousarray(snaps[i])).pin_memory()
+            T._check(L.tsvd_session_step(
+                s._h, ctypes.cast(e.data_ptr(), ctypes.POINTER(ctypes.c_int32)), len(snaps[i])))
+        emb = np.zeros((args.steps, len(sources), cfg["rank_d"]), np.float64)
+        stats = (T.StepStats * args.steps)()
         stream = torch.cuda.ExternalStream(s.stream(), device=device)
         ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        lat = []
         torch.cuda.synchronize(device)
+        i32p, f64p = ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_double)
         ev0.record(stream)
-        for k in range(args.steps):
-            i = 1 + args.warmup + k
-            t = time.perf_counter()
-            step(i)
-            T._check(L.tsvd_session_embedding(s._h, emb.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
-            lat.append((time.perf_counter() - t) * 1e3)
+        if args.pipelined:
+            T._check(L.tsvd_session_run(
+                s._h, ctypes.cast(pinned_timed.data_ptr(), i32p),
+                off.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), args.steps,
+                emb.ctypes.data_as(f64p), stats))
+        else:
+            for k in range(args.steps):
+                T._check(L.tsvd_session_step(
+                    s._h, ctypes.cast(pinned_timed.data_ptr() + int(off[k]) * 8, i32p),
+                    int(off[k + 1] - off[k])))
+                T._check(L.tsvd_session_embedding(s._h, emb[k].ctypes.data_as(f64p)))
+                T._check(L.tsvd_session_last_stats(s._h, ctypes.byref(stats[k])))
         ev1.record(stream)
         torch.cuda.synchronize(device)
+        assert np.isfinite(emb).all()
         res["e2e_ms"] = ev0.elapsed_time(ev1)
-        res["e2e_lat"] = lat
-        res["h2d"] = int(sum(len(snaps[1 + args.warmup + k]) * 8 for k in range(args.steps)) / args.steps)
-        res["d2h"] = int(emb.size * 4)
+        res["e2e_lat"] = [stats[k].ms_total for k in range(args.steps)]
+        res["h2d"] = int(off[-1] * 8 / args.steps)
+        res["d2h"] = int(len(sources) * cfg["rank_d"] * 4)
     return res
 
 
-# ------------------------------------------------------------------ CPU baseline
 def cpu_sample(cfg, snaps, sources, budget_sources=None, threads=None):
     """Times the CPU oracle (the reference algorithm restated) on a bounded
     sample of one dynamic snapshot and scales it to the full workload:
@@ -291,12 +316,12 @@ def run_reference(args):
 
 
 # DRAM bytes (read + write) of push_kernel + push_heavy_kernel per pushed
-# item-neighbour (one 128-byte residual-line atomic), from one ncu capture of
+# item-neighbour (one 256-byte residue-run atomic), from one ncu capture of
 # every push launch of a timed rmat-d-2.7m snapshot (dram__bytes_read.sum +
-# dram__bytes_write.sum, one pass): 2310.0 GB over 1.323e10 item-neighbours
-# (profiles/push_kernel_rmat-d-2.7m.md). `traffic` scales it to the launches
-# of the run being reported.
-PUSH_TRAFFIC_BYTES_PER_ITEM_EDGE = 174.6
+# dram__bytes_write.sum, one pass): 2580.3 GB over 7.478e9 item-neighbours,
+# one 256-byte run atomic each (profiles/push_kernel_rmat-d-2.7m.md).
+# `traffic` scales it to the launches of the run being reported.
+PUSH_TRAFFIC_BYTES_PER_ITEM_EDGE = 345.0
 
 
 def push_roofline(stages):
@@ -312,7 +337,7 @@ def push_roofline(stages):
     `achieved_min` counts the bytes this design has to move at least: per lane
     push 16 (fp32 residue exchange + reserve update), per lane edge update 8
     (fp32 atomic read-modify-write), per item-neighbour 4 (the neighbour id is
-    read once for 32 sources), per item 20 (frontier entry, row start,
+    read once for the 64 sources of a chunk), per item 20 (frontier entry, row start,
     degree)."""
     pk, _ = peaks()
     peak = float(pk.get("hbm_gbs", 6800.0))
@@ -386,7 +411,11 @@ def main():
                        "n_parts": cfg["n_parts"], "rank_d": cfg["rank_d"],
                        "passes_q": cfg["passes_q"], "snapshots": cfg["snapshots"],
                        "l2": "working set (PPR state) larger than L2",
-                       "parallelism": "replicas x%d" % world},
+                       "parallelism": "replicas x%d" % world,
+                       "ppr_reserve": "pinned host memory" if args.host_reserve else "HBM",
+                       "driver": ("tsvd_session_run: factor stage of snapshot k overlapped "
+                                  "with the push of k+1") if args.pipelined
+                       else "tsvd_session_step per snapshot"},
             "clocks": res["clocks"], "gpu_launches": res["launches"],
             "stage_ms_mean": {k: float(np.mean([s[k] for s in res["stages"]]))
                               for k in ("ms_insert", "ms_push", "ms_log", "ms_frpca", "ms_merge")},

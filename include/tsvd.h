@@ -173,6 +173,11 @@ typedef struct tsvd_config {
                             /* (default 0.5; 1 = plain rmax test only)               */
   int32_t lp_right_factor;  /* 1: after every snapshot, V_b = A_b^T U for each block  */
                             /* refreshed in it (LP drivers; needs TSVD_ROOT_U)        */
+  int32_t ppr_host_reserve; /* 1: the reserve p (half of the PPR state) lives in     */
+                            /* pinned host memory, read and written by the kernels    */
+                            /* over NVLink-C2C; the residues stay in HBM. For graphs  */
+                            /* whose 16 N Sp bytes of state exceed HBM (N 6.2M,       */
+                            /* |S| 3000: 305 GB)                                      */
 } tsvd_config;
 
 /* Fills the reference's defaults (Tree_u_NC, run.sh: alpha .5, q 12, ...). */
@@ -210,7 +215,7 @@ typedef struct tsvd_step_stats {
   int32_t factorized_blocks;
   int32_t merged_nodes;
   double ms_insert, ms_refresh, ms_push, ms_log, ms_frpca, ms_merge, ms_total;
-  int64_t push_items;       /* (vertex, 32-source chunk) items pushed             */
+  int64_t push_items;       /* (vertex, 64-source chunk) items pushed             */
   double ms_push_kernels;   /* device time of the push scatter kernels            */
   double ms_materialize_kernel; /* device time of the block materialization      */
   int64_t push_item_edges;  /* sum of deg(v) over pushed items (neighbour-list reads) */
@@ -219,6 +224,24 @@ typedef struct tsvd_step_stats {
   int32_t eig_sweeps_merge; /* Jacobi sweeps of the merges (max over levels)      */
 } tsvd_step_stats;
 tsvd_status tsvd_session_last_stats(tsvd_session *s, tsvd_step_stats *out);
+
+/* The driver loop over `count` snapshots (Tree_u_NC.cpp:507-911 without the
+ * file reads): snapshot k is the pairs [offsets[k], offsets[k+1]) of `edges`
+ * (offsets: count + 1 pair indices, host memory). Each snapshot does what
+ * tsvd_session_step does, but the factor stage of snapshot k (frPCA of the
+ * dirty blocks, merge, LP right factor) runs on a second thread and stream
+ * while snapshot k+1 is inserted, refreshed, pushed and materialized.
+ * embeddings (optional, host): count x |S| x d doubles, snapshot k's
+ * embedding at k * |S| * d (zeros before the first one). stats (optional):
+ * count entries; ms_total is the snapshot's latency, from the start of its
+ * insert to the end of its factor stage. Returns after the last snapshot is
+ * complete; tsvd_session_last_stats then reports the last snapshot. */
+tsvd_status tsvd_session_run(tsvd_session *s, const int32_t *edges, const int64_t *offsets,
+                             int32_t count, double *embeddings, tsvd_step_stats *stats);
+/* Same, with `edges` in device memory (owned by the caller). */
+tsvd_status tsvd_session_run_device(tsvd_session *s, const int32_t *edges_dev,
+                                    const int64_t *offsets, int32_t count, double *embeddings,
+                                    tsvd_step_stats *stats);
 
 /* ---- link prediction (LP drivers) ---------------------------------------
  * Replaces mkl_right_matrix_multiplication_without_norm

@@ -306,3 +306,129 @@ def test_lp_right_factor_and_scores(directed):
         with pytest.raises(T.TsvdError):
             s.lp_scores(np.array([[not_a_source, 0]]))
     assert clean_seen  # the lazy rule kept some block's V and U across a snapshot
+
+
+@pytest.mark.parametrize("directed,rule", [(False, T.DIRTY_REFERENCE), (True, T.DIRTY_FROBENIUS)])
+def test_pipelined_run_matches_steps(directed, rule):
+    """tsvd_session_run overlaps the factor stage of snapshot k with the push
+    of snapshot k+1. Its per-snapshot embeddings and refactorized block
+    counts agree with one-at-a-time steps up to the push-order differences of
+    two PPR runs (the reference dirty rule reads the previous snapshot's
+    residuals, so a stale read would change which blocks are refactorized).
+    Push order can flip a lazy decision that is within a few percent of its
+    threshold; the comparison stops at the first such near-tie of the stepped
+    run. The first snapshot only grows the graph (lazy_update_start_iter 3,
+    the second is pushed from scratch): its embedding is zeros."""
+    cfg = small_cfg(directed, n=8000, m=60000, sources=96, n_parts=4, rank_d=32, snapshots=6)
+    _, snaps, src = W.build(cfg, seed=41)
+    kw = W.session_kwargs(cfg, dynamic_start=3, lazy_start=3)
+    kw["dirty_rule"] = rule
+    ref_emb, ref_stats = [], []
+    tie_from = len(snaps)
+    with T.Session(cfg["n"], src, **kw) as a:
+        prev_resid = None
+        for k, e in enumerate(snaps):
+            st = a.step(e)
+            ref_stats.append(st)
+            ref_emb.append(a.embedding() if not st["skipped"] else None)
+            info = a.block_info()
+            if st["iter"] >= kw["lazy_update_start_iter"]:
+                if rule == T.DIRTY_REFERENCE:
+                    lhs = prev_resid + info["norm_diff"]
+                    thr = kw["delta"] * np.sqrt(2) * info["norm"]
+                else:
+                    lhs, thr = info["norm_diff"], kw["dirty_frac"] * info["norm"]
+                if (np.abs(lhs - thr) <= 0.05 * info["norm"]).any():
+                    tie_from = min(tie_from, k)
+            prev_resid = info["resid"]
+        _, sig_ref = a.tree_factor(0)
+    assert tie_from >= 2  # the from-scratch snapshot and the first lazy decision compare
+    import torch
+    dev = torch.from_numpy(np.concatenate(snaps)).cuda()
+    off = np.concatenate([[0], np.cumsum([len(e) for e in snaps])])
+    for use_device in (False, True):
+        with T.Session(cfg["n"], src, **kw) as s:
+            if use_device:
+                stats, emb = s.run_device(dev.data_ptr(), off)
+            else:
+                stats, emb = s.run(snaps)
+            _, sig = s.tree_factor(0)
+            assert s.stats()["iter"] == len(snaps)
+            assert np.allclose(s.embedding(), emb[-1])
+        assert [x["iter"] for x in stats] == [x["iter"] for x in ref_stats]
+        assert [x["skipped"] for x in stats] == [x["skipped"] for x in ref_stats]
+        assert stats[0]["skipped"] == 1 and not emb[0].any()
+        for k in range(1, len(snaps)):
+            st = stats[k]
+            assert np.isfinite(emb[k]).all()
+            assert st["edges_inserted"] == len(snaps[k])
+            assert st["ms_total"] >= st["ms_push"] > 0 and st["ms_frpca"] > 0
+            if k < tie_from:
+                assert st["factorized_blocks"] == ref_stats[k]["factorized_blocks"], k
+                err = gram_rel_err(emb[k], ref_emb[k])
+                assert err < 3e-2, (k, err)
+        if tie_from == len(snaps):
+            assert np.allclose(sig[:16], sig_ref[:16], rtol=5e-3)
+
+
+def test_pipelined_run_lp_and_errors():
+    """The LP right factor on the pipelined path: after the run, the blocks
+    refreshed in the last snapshot hold V_b = A_b^T U with that snapshot's U.
+    A snapshot with an invalid endpoint fails the run with TSVD_ERR_INVALID,
+    after the snapshot before it has completed; the session stays usable."""
+    cfg = small_cfg(True, n=6000, m=40000, sources=64, n_parts=4, rank_d=32, snapshots=4)
+    _, snaps, src = W.build(cfg, seed=43)
+    kw = W.session_kwargs(cfg, dynamic_start=2, lazy_start=2)
+    kw.update(transform=T.TRANSFORM_LOG10_LP, root_scaling=T.ROOT_U, lp_right_factor=True)
+    P, cd = cfg["n_parts"], cfg["n"] // cfg["n_parts"]
+    with T.Session(cfg["n"], src, **kw) as s:
+        stats, emb = s.run(snaps)
+        U = emb[-1]
+        assert np.abs(U.T @ U - np.eye(cfg["rank_d"])).max() < 5e-3
+        V = s.lp_right_factor().astype(np.float64)
+        dirty = s.block_info()["dirty"]
+        assert dirty.any()
+        for b in np.flatnonzero(dirty):
+            c0 = b * cd
+            c1 = cfg["n"] if b == P - 1 else c0 + cd
+            ref = s.block_dense(b).astype(np.float64).T @ U
+            assert np.abs(V[c0:c1] - ref).max() <= 1e-4 * max(np.abs(ref).max(), 1e-30)
+    bad = [snaps[0], snaps[1], np.array([[0, cfg["n"]]], np.int32), snaps[2]]
+    with T.Session(cfg["n"], src, **kw) as s:
+        with pytest.raises(T.TsvdError) as ei:
+            s.run(bad)
+        assert ei.value.status == 1
+        assert s.stats()["iter"] == 2  # the last completed snapshot
+        s.step(snaps[2])
+        assert np.isfinite(s.embedding()).all()
+
+
+def test_host_reserve_matches_device_reserve():
+    """ppr_host_reserve: the reserve p in mapped pinned host memory (reached
+    over NVLink-C2C), the residues in HBM. Refresh and push keep the push
+    identity and the rmax bound and stay within the error bound of the
+    oracle, and whole snapshots give the embedding of the all-device layout
+    up to push order."""
+    cfg = small_cfg(True)
+    _, snaps, src = W.build(cfg, seed=47)
+    g = native.OracleGraph(cfg["n"], True)
+    ors = [native.OraclePPR(cfg["n"], src) for _ in range(2)]
+    kw = W.session_kwargs(cfg, dynamic_start=2)
+    with T.Session(cfg["n"], src, ppr_host_reserve=True, **kw) as s:
+        for it, e in enumerate(snaps[:3], start=1):
+            s.graph_insert(e)
+            g.insert(e)
+            for t in range(2):
+                s.ppr_refresh(it, bool(t))
+                s.ppr_push(bool(t))
+                ors[t].refresh(g, t, it, 2, cfg["alpha"], cfg["rmax"])
+                ors[t].push(g, t, cfg["alpha"], cfg["rmax"])
+                _ppr_checks(s, g, src, cfg, bool(t), ors[t])
+    kw = W.session_kwargs(cfg, dynamic_start=2, lazy_start=2)
+    emb = {}
+    for host in (False, True):
+        with T.Session(cfg["n"], src, ppr_host_reserve=host, **kw) as s:
+            for e in snaps:
+                s.step(e)
+            emb[host] = s.embedding()
+    assert gram_rel_err(emb[True], emb[False]) < 3e-2

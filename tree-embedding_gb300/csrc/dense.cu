@@ -786,13 +786,13 @@ __global__ void __launch_bounds__(256) jacobi_replay_kernel(JacobiArgs a, float 
 
 // ------------------------------------------------------------------ host side
 int sm_count() {
-  static int n = 0;
-  if (n == 0) {
-    int dev = 0;
+  // initialized once, thread-safely (a pipelined run calls this from two threads)
+  static const int n = [] {
+    int dev = 0, v = 0;
     cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-    if (n <= 0) n = 1;
-  }
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+    return v > 0 ? v : 1;
+  }();
   return n;
 }
 

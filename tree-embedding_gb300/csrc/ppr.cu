@@ -372,6 +372,21 @@ __global__ void init_sources_kernel(const int32_t *__restrict__ sources, int32_t
   if (blockIdx.x == 0 && threadIdx.x == 0) *count = nsrc;
 }
 
+// Zero fill with 16-byte stores (also for p in mapped host memory).
+__global__ void zero_kernel(float4 *__restrict__ x, int64_t n4) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n4;
+       i += (int64_t)gridDim.x * blockDim.x)
+    x[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+tsvd_status zero_floats(float *x, size_t count, cudaStream_t st) {
+  // count is a multiple of 4: n * Sp with Sp a multiple of kChunk
+  zero_kernel<<<grid_for((int64_t)(count / 4), 256, 8), 256, 0, st>>>(
+      reinterpret_cast<float4 *>(x), (int64_t)(count / 4));
+  TSVD_LAUNCH_CHECK();
+  return TSVD_OK;
+}
+
 float largest_float_not_above(double x) {
   float f = (float)x;
   if ((double)f > x) f = nextafterf(f, -INFINITY);
@@ -380,7 +395,7 @@ float largest_float_not_above(double x) {
 
 }  // namespace
 
-tsvd_status ppr_alloc(PprState &P, int32_t n, int32_t nsrc, int32_t sp) {
+tsvd_status ppr_alloc(PprState &P, int32_t n, int32_t nsrc, int32_t sp, bool host_reserve) {
   P.n = n;
   P.nsrc = nsrc;
   P.sp = sp;
@@ -388,9 +403,24 @@ tsvd_status ppr_alloc(PprState &P, int32_t n, int32_t nsrc, int32_t sp) {
   P.chunks = sp / kChunk;
   size_t cells = (size_t)n * sp;
   TSVD_CUDA(cudaMalloc(&P.r, cells * sizeof(float)));
-  TSVD_CUDA(cudaMalloc(&P.p, cells * sizeof(float)));
   TSVD_CUDA(cudaMemset(P.r, 0, cells * sizeof(float)));
-  TSVD_CUDA(cudaMemset(P.p, 0, cells * sizeof(float)));
+  if (host_reserve) {
+    void *h = nullptr;
+    if (cudaHostAlloc(&h, cells * sizeof(float), cudaHostAllocMapped | cudaHostAllocPortable) !=
+        cudaSuccess) {
+      cudaGetLastError();
+      return fail(TSVD_ERR_OOM, "ppr: %.1f GB of pinned host memory for the reserve",
+                  cells * 4.0 / 1e9);
+    }
+    P.p_host = static_cast<float *>(h);
+    void *d = nullptr;
+    TSVD_CUDA(cudaHostGetDevicePointer(&d, h, 0));
+    P.p = static_cast<float *>(d);
+  } else {
+    TSVD_CUDA(cudaMalloc(&P.p, cells * sizeof(float)));
+  }
+  TSVD_TRY(zero_floats(P.p, cells, nullptr));
+  TSVD_CUDA(cudaDeviceSynchronize());
   P.nwords = ceil_div((int64_t)n * P.chunks, 32);
   TSVD_CUDA(cudaMalloc(&P.tflag, P.nwords * sizeof(uint32_t)));
   TSVD_CUDA(cudaMemset(P.tflag, 0, P.nwords * sizeof(uint32_t)));
@@ -414,7 +444,12 @@ tsvd_status ppr_alloc(PprState &P, int32_t n, int32_t nsrc, int32_t sp) {
 }
 
 void ppr_free(PprState &P) {
-  cudaFree(P.r); cudaFree(P.p); cudaFree(P.tflag); cudaFree(P.pend);
+  cudaFree(P.r);
+  if (P.p_host)
+    cudaFreeHost(P.p_host);
+  else
+    cudaFree(P.p);
+  cudaFree(P.tflag); cudaFree(P.pend);
   cudaFree(P.front[0]); cudaFree(P.front[1]);
   cudaFree(P.heavy_w); cudaFree(P.heavy_item); cudaFree(P.heavy_mask); cudaFree(P.units);
   cudaFree(P.upd); cudaFree(P.counters); cudaFree(P.stats);
@@ -432,7 +467,7 @@ tsvd_status ppr_refresh(PprState &P, const Adjacency &A, const int32_t *sources_
   (void)vmark;
   if (from_scratch) {
     TSVD_CUDA(cudaMemsetAsync(P.r, 0, (size_t)P.n * P.sp * sizeof(float), st));
-    TSVD_CUDA(cudaMemsetAsync(P.p, 0, (size_t)P.n * P.sp * sizeof(float), st));
+    TSVD_TRY(zero_floats(P.p, (size_t)P.n * P.sp, st));
     TSVD_CUDA(cudaMemsetAsync(P.tflag, 0, P.nwords * sizeof(uint32_t), st));
     TSVD_CUDA(cudaMemsetAsync(P.pend, 0, P.nwords * sizeof(uint32_t), st));
     P.cur = 0;

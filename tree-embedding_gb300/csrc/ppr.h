@@ -19,6 +19,7 @@ constexpr int kStatSlots = 64;  // push counters are spread over this many slots
 struct PprState {
   int32_t n = 0, nsrc = 0, sp = 0, chunks = 0;
   float *r = nullptr, *p = nullptr;  // [chunks][n][kChunk], see ppr_cell
+  float *p_host = nullptr;           // p's host allocation when it is mapped pinned host memory
   uint32_t *tflag = nullptr;         // touched (vertex, chunk) bitset, chunk-major
   uint32_t *pend = nullptr;          // parked below the current threshold level
   int64_t nwords = 0;                // words of either bitset
@@ -104,7 +105,9 @@ struct RefreshArgs {
   float inv_alpha_f, oma_over_alpha_f;
 };
 
-tsvd_status ppr_alloc(PprState &P, int32_t n, int32_t nsrc, int32_t sp);
+// host_reserve: p in pinned host memory mapped into the device address space
+// (the kernels reach it over NVLink-C2C); r always in device memory.
+tsvd_status ppr_alloc(PprState &P, int32_t n, int32_t nsrc, int32_t sp, bool host_reserve);
 void ppr_free(PprState &P);
 tsvd_status ppr_refresh(PprState &P, const Adjacency &A, const int32_t *sources_dev,
                         bool from_scratch, const PprParams &prm, uint8_t *vmark,

@@ -7,7 +7,9 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <functional>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "blocks.h"
@@ -84,6 +86,11 @@ struct tsvd_session {
   int iter = 0;
   tsvd_step_stats last{};
   cudaEvent_t ev[8]{};
+  // pipelined runs: the factor stage of snapshot k runs on st2 while the
+  // graph insert, refresh and push of snapshot k+1 run on st
+  cudaStream_t st2 = nullptr;
+  cudaEvent_t pev[2][8]{};        // per snapshot (two in flight): [0..3] insert..log, [4..7] factor
+  float *emb_stage = nullptr;     // pinned host copy of one embedding
   // LP right factor (cfg.lp_right_factor)
   float *lp_v = nullptr;          // [n][kLp]: row b*col_dim + c = V of block b's column c
   float *lp_u = nullptr;          // [nparts][S][d]: the root factor each V_b was made with
@@ -211,8 +218,16 @@ extern "C" void tsvd_config_default(tsvd_config *c) {
 static tsvd_status session_alloc(tsvd_session *s) {
   const tsvd_config &c = s->cfg;
   TSVD_CUDA(cudaSetDevice(c.device));
-  TSVD_CUDA(cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking));
+  // The factor stream of a pipelined run gets the lowest priority: its
+  // blocks fill the SMs the insert and push leave idle instead of delaying
+  // the insert's short dependent kernels.
+  int prio_low = 0, prio_high = 0;
+  TSVD_CUDA(cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high));
+  TSVD_CUDA(cudaStreamCreateWithPriority(&s->st, cudaStreamNonBlocking, prio_high));
+  TSVD_CUDA(cudaStreamCreateWithPriority(&s->st2, cudaStreamNonBlocking, prio_low));
   for (auto &e : s->ev) TSVD_CUDA(cudaEventCreate(&e));
+  for (auto &set : s->pev)
+    for (auto &e : set) TSVD_CUDA(cudaEventCreate(&e));
   const int ndir = s->directed ? 2 : 1;
   for (int dd = 0; dd < ndir; ++dd) {
     Adjacency &A = s->adj[dd];
@@ -223,7 +238,7 @@ static tsvd_status session_alloc(tsvd_session *s) {
     TSVD_CUDA(cudaMemset(A.deg, 0, sizeof(int32_t) * s->n));
     TSVD_CUDA(cudaMalloc(&A.former, sizeof(int32_t) * s->n));
     TSVD_CUDA(cudaMemset(A.former, 0, sizeof(int32_t) * s->n));
-    TSVD_TRY(ppr_alloc(s->ppr[dd], s->n, s->S, s->sp));
+    TSVD_TRY(ppr_alloc(s->ppr[dd], s->n, s->S, s->sp, c.ppr_host_reserve != 0));
   }
   TSVD_CUDA(cudaMalloc(&s->vmark, s->n));
   TSVD_CUDA(cudaMemset(s->vmark, 0, s->n));
@@ -268,6 +283,7 @@ static tsvd_status session_alloc(tsvd_session *s) {
   TSVD_CUDA(cudaMemset(s->tree_sigma, 0, sizeof(float) * s->d * s->total_nodes));
   TSVD_CUDA(cudaMalloc(&s->embedding, sizeof(float) * s->node_elems()));
   TSVD_CUDA(cudaMemset(s->embedding, 0, sizeof(float) * s->node_elems()));
+  TSVD_CUDA(cudaMallocHost(&s->emb_stage, sizeof(float) * s->node_elems()));
   TSVD_CUDA(cudaMalloc(&s->bad_dev, sizeof(int32_t)));
   if (c.lp_right_factor) {
     TSVD_CUDA(cudaMalloc(&s->lp_v, sizeof(float) * s->n * kLp));
@@ -293,6 +309,7 @@ static void session_release(tsvd_session *s) {
   if (!s) return;
   cudaSetDevice(s->cfg.device);
   if (s->st) cudaStreamSynchronize(s->st);
+  if (s->st2) cudaStreamSynchronize(s->st2);
   for (int dd = 0; dd < 2; ++dd) {
     adjacency_free(s->adj[dd]);
     if (s->ppr[dd].r) ppr_free(s->ppr[dd]);
@@ -307,9 +324,14 @@ static void session_release(tsvd_session *s) {
   cudaFree(s->lp_v); cudaFree(s->lp_u); cudaFree(s->lp_valid_dev); cudaFree(s->colpos);
   cudaFree(s->src_row); cudaFree(s->pairs_dev); cudaFree(s->scores_dev);
   frpca_work_free(s->fw);
+  cudaFreeHost(s->emb_stage);
   for (auto &e : s->ev)
     if (e) cudaEventDestroy(e);
+  for (auto &set : s->pev)
+    for (auto &e : set)
+      if (e) cudaEventDestroy(e);
   if (s->st) cudaStreamDestroy(s->st);
+  if (s->st2) cudaStreamDestroy(s->st2);
 }
 
 extern "C" tsvd_status tsvd_session_create(const tsvd_config *cfg, tsvd_session **out) {
@@ -423,7 +445,9 @@ static tsvd_status insert_device(tsvd_session *s, const int32_t *edges_dev, int6
   return TSVD_OK;
 }
 
-static tsvd_status stage_materialize(tsvd_session *s, int iter) {
+// Column map, log transform and block norms of the converged PPR state
+// (launch and read-back; the dirty decision is materialize_decide).
+static tsvd_status materialize_launch(tsvd_session *s) {
   const int P = s->nparts;
   TSVD_TRY(colmap_update(s->vmark, s->colmap, s->colpos, s->ncols_dev, s->n, s->col_dim, P, s->st));
   TSVD_CUDA(cudaMemcpyAsync(s->ncols_h.data(), s->ncols_dev, sizeof(int32_t) * P,
@@ -468,13 +492,22 @@ static tsvd_status stage_materialize(tsvd_session *s, int iter) {
   TSVD_CUDA(cudaMemcpyAsync(ss.data(), s->stored_dev, sizeof(unsigned long long) * P, cudaMemcpyDeviceToHost, s->st));
   TSVD_CUDA(cudaStreamSynchronize(s->st));
   s->last.ms_materialize_kernel = ms_between(s->ev[6], s->ev[7]);
-  // Lazy-update decision (ppr:2700-2729) or unconditional refresh (Tree_u_NC.cpp:642-668).
+  for (int b = 0; b < P; ++b) {
+    s->nnz_h[b] = (int64_t)nn[b];
+    s->stored_h[b] = (int64_t)ss[b];
+  }
+  return TSVD_OK;
+}
+// Lazy-update decision (ppr:2700-2729) or unconditional refresh
+// (Tree_u_NC.cpp:642-668). The reference rule reads the residuals of the
+// previous factorization, so a pipelined run calls this only after the
+// previous snapshot's factor stage has finished.
+static tsvd_status materialize_decide(tsvd_session *s, int iter) {
+  const int P = s->nparts;
   const bool with_norm = iter >= s->cfg.lazy_update_start_iter;
   s->factor_now.clear();
   int ndirty = 0;
   for (int b = 0; b < P; ++b) {
-    s->nnz_h[b] = (int64_t)nn[b];
-    s->stored_h[b] = (int64_t)ss[b];
     bool dirty = true;
     if (with_norm) {
       const double a_norm = std::sqrt(std::max(s->norm2_h[b], 0.0));
@@ -497,7 +530,7 @@ static tsvd_status stage_materialize(tsvd_session *s, int iter) {
     s->atcur[b] = 1 - s->atcur[b];
     s->ncols_old_h[b] = s->ncols_h[b];
     s->norm2_acc[b] = s->norm2_h[b];
-    if (ss[b] > 0) s->factor_now.push_back(b);  // nonZeros() == 0 blocks are skipped
+    if (s->stored_h[b] > 0) s->factor_now.push_back(b);  // nonZeros() == 0 blocks are skipped
   }
   TSVD_CUDA(cudaMemcpyAsync(s->ncols_old_dev, s->ncols_old_h.data(), sizeof(int32_t) * P,
                             cudaMemcpyHostToDevice, s->st));
@@ -506,17 +539,45 @@ static tsvd_status stage_materialize(tsvd_session *s, int iter) {
   return TSVD_OK;
 }
 
-static tsvd_status stage_factorize(tsvd_session *s, int iter) {
-  const int nf = (int)s->factor_now.size();
-  s->last.factorized_blocks = nf;
+static tsvd_status stage_materialize(tsvd_session *s, int iter) {
+  TSVD_TRY(materialize_launch(s));
+  return materialize_decide(s, iter);
+}
+
+// What the factor stage of one snapshot needs from the host-side block
+// state, copied when the snapshot's dirty decision is made: a pipelined run
+// changes that state for the next snapshot while this one is factorized.
+struct FactorJob {
+  int iter = 0;
+  std::vector<int> factor_now;     // dirty blocks with stored entries
+  std::vector<int> atcur;          // accepted buffer of every block
+  std::vector<int32_t> ncols;      // compacted columns of every block
+  std::vector<uint8_t> dirty;
+  std::vector<double> norm2_acc;   // ||A_b||^2 of the accepted matrices
+  tsvd_step_stats stats{};
+};
+
+static void make_job(const tsvd_session *s, int iter, FactorJob &job) {
+  job.iter = iter;
+  job.factor_now = s->factor_now;
+  job.atcur = s->atcur;
+  job.ncols = s->ncols_h;
+  job.dirty = s->dirty_h;
+  job.norm2_acc = s->norm2_acc;
+  job.stats = s->last;
+}
+
+static tsvd_status stage_factorize(tsvd_session *s, FactorJob &job, cudaStream_t st) {
+  const int nf = (int)job.factor_now.size();
+  job.stats.factorized_blocks = nf;
   if (nf == 0) return TSVD_OK;
   std::vector<FrpcaProblem> probs(nf);
   for (int i = 0; i < nf; ++i) {
-    int b = s->factor_now[i];
+    int b = job.factor_now[i];
     FrpcaProblem &P = probs[i];
     P.block = b;
-    P.at = s->at_block(s->atcur[b], b);
-    P.ncols = s->ncols_h[b];
+    P.at = s->at_block(job.atcur[b], b);
+    P.ncols = job.ncols[b];
     P.colmap = s->colmap + (size_t)b * s->col_dim;
     P.col_base = b * s->col_dim;
     P.b_out = s->node_b(s->leaf_start + b);
@@ -525,24 +586,24 @@ static tsvd_status stage_factorize(tsvd_session *s, int iter) {
     P.v_out = nullptr;
   }
   std::vector<double> ssum(nf);
-  TSVD_TRY(frpca_batch(s->fw, probs.data(), nf, s->q, s->cfg.seed, s->S, s->st, ssum.data()));
-  s->last.eig_sweeps_frpca = s->fw.last_sweeps;
+  TSVD_TRY(frpca_batch(s->fw, probs.data(), nf, s->q, s->cfg.seed, s->S, st, ssum.data()));
+  job.stats.eig_sweeps_frpca = s->fw.last_sweeps;
   // Residual ||A - U S V^T||_F = sqrt(||A||^2 - sum sigma^2) for an orthonormal
   // basis (the reference forms the dense product, Tree_u_NC.cpp:158-204).
-  if (iter >= s->cfg.lazy_update_start_iter - 1)
+  if (job.iter >= s->cfg.lazy_update_start_iter - 1)
     for (int i = 0; i < nf; ++i) {
-      int b = s->factor_now[i];
-      s->resid[b] = std::sqrt(std::max(s->norm2_acc[b] - ssum[i], 0.0));
+      int b = job.factor_now[i];
+      s->resid[b] = std::sqrt(std::max(job.norm2_acc[b] - ssum[i], 0.0));
     }
   return TSVD_OK;
 }
 
-static tsvd_status stage_merge(tsvd_session *s) {
-  s->last.merged_nodes = 0;
-  if (s->factor_now.empty()) return TSVD_OK;
+static tsvd_status stage_merge(tsvd_session *s, FactorJob &job, cudaStream_t st) {
+  job.stats.merged_nodes = 0;
+  if (job.factor_now.empty()) return TSVD_OK;
   const int h = s->h;
   std::vector<int> level;
-  for (int b : s->factor_now) {
+  for (int b : job.factor_now) {
     int par = (s->leaf_start + b - 1) / h;
     if (std::find(level.begin(), level.end(), par) == level.end()) level.push_back(par);
   }
@@ -558,12 +619,12 @@ static tsvd_status stage_merge(tsvd_session *s) {
     }
     int mode = 0;
     if (root) mode = s->cfg.root_scaling == TSVD_ROOT_U ? 2 : 1;
-    TSVD_TRY(merge_batch(s->fw, probs.data(), (int)probs.size(), h, s->S, mode, s->st));
-    s->last.eig_sweeps_merge = std::max(s->last.eig_sweeps_merge, s->fw.last_sweeps);
-    s->last.merged_nodes += (int)probs.size();
+    TSVD_TRY(merge_batch(s->fw, probs.data(), (int)probs.size(), h, s->S, mode, st));
+    job.stats.eig_sweeps_merge = std::max(job.stats.eig_sweeps_merge, s->fw.last_sweeps);
+    job.stats.merged_nodes += (int)probs.size();
     if (root) {
       TSVD_CUDA(cudaMemcpyAsync(s->node_b(0), s->embedding, sizeof(float) * s->node_elems(),
-                                cudaMemcpyDeviceToDevice, s->st));
+                                cudaMemcpyDeviceToDevice, st));
       s->has_embedding = true;
       break;
     }
@@ -575,38 +636,38 @@ static tsvd_status stage_merge(tsvd_session *s) {
     std::sort(next.begin(), next.end());
     level.swap(next);
   }
-  TSVD_CUDA(cudaStreamSynchronize(s->st));
+  TSVD_CUDA(cudaStreamSynchronize(st));
   return TSVD_OK;
 }
 
 // LP right factor of the blocks refreshed in this snapshot (Tree_u_LP.cpp:
 // 1024-1044: the blocks whose update record is this iteration), with this
 // snapshot's root factor U, which is kept beside them for scoring.
-static tsvd_status stage_lp(tsvd_session *s, int iter) {
+static tsvd_status stage_lp(tsvd_session *s, const FactorJob &job, cudaStream_t st) {
   if (!s->cfg.lp_right_factor || !s->has_embedding) return TSVD_OK;
   std::vector<LpProblem> probs;
   std::vector<int> blocks;
   for (int b = 0; b < s->nparts; ++b) {
-    if (!s->dirty_h[b]) continue;
+    if (!job.dirty[b]) continue;
     LpProblem p;
-    p.at = s->at_block(s->atcur[b], b);
-    p.ncols = s->ncols_h[b];
+    p.at = s->at_block(job.atcur[b], b);
+    p.ncols = job.ncols[b];
     p.v_out = s->lp_v + (size_t)b * s->col_dim * kLp;
     probs.push_back(p);
     blocks.push_back(b);
   }
   if (probs.empty()) return TSVD_OK;
-  TSVD_TRY(lp_right_batch(s->fw, probs.data(), (int)probs.size(), s->embedding, s->S, s->d, s->st));
+  TSVD_TRY(lp_right_batch(s->fw, probs.data(), (int)probs.size(), s->embedding, s->S, s->d, st));
   std::vector<int32_t> valid(s->nparts);
   for (int b : blocks) {
     TSVD_CUDA(cudaMemcpyAsync(s->lp_u + (size_t)b * s->node_elems(), s->embedding,
-                              sizeof(float) * s->node_elems(), cudaMemcpyDeviceToDevice, s->st));
-    s->lp_iter[b] = iter;
+                              sizeof(float) * s->node_elems(), cudaMemcpyDeviceToDevice, st));
+    s->lp_iter[b] = job.iter;
   }
   for (int b = 0; b < s->nparts; ++b) valid[b] = s->lp_iter[b] >= 0;
   TSVD_CUDA(cudaMemcpyAsync(s->lp_valid_dev, valid.data(), sizeof(int32_t) * s->nparts,
-                            cudaMemcpyHostToDevice, s->st));
-  TSVD_CUDA(cudaStreamSynchronize(s->st));
+                            cudaMemcpyHostToDevice, st));
+  TSVD_CUDA(cudaStreamSynchronize(st));
   return TSVD_OK;
 }
 
@@ -628,48 +689,111 @@ static tsvd_status stage_ppr(tsvd_session *s, int iter, int dir) {
   return TSVD_OK;
 }
 
-static tsvd_status step_device(tsvd_session *s, const int32_t *edges_dev, int64_t m) {
-  TSVD_CUDA(cudaSetDevice(s->cfg.device));
+static tsvd_status stage_edges_to_device(tsvd_session *s, const int32_t *edges, int64_t m);
+
+// Graph insert (after the copy of host edges, when on_device is false),
+// refresh + push and materialization of one snapshot on the main stream;
+// ea[0..3] mark its stage boundaries. after_insert (optional) runs once the
+// insert is issued. Snapshots before lazy_update_start_iter - 1 only grow the
+// graph (Tree_u_NC.cpp:516): they return with *skipped set.
+static tsvd_status stage_front(tsvd_session *s, const int32_t *edges, bool on_device, int64_t m,
+                               cudaEvent_t *ea, bool *skipped,
+                               const std::function<tsvd_status()> &after_insert = nullptr) {
   const int iter = ++s->iter;
   std::memset(&s->last, 0, sizeof s->last);
   s->last.iter = iter;
-  cudaEvent_t *ev = s->ev;
-  TSVD_CUDA(cudaEventRecord(ev[0], s->st));
-  TSVD_TRY(insert_device(s, edges_dev, m));
-  TSVD_CUDA(cudaEventRecord(ev[1], s->st));
-  // Tree_u_NC.cpp:516 — snapshots before lazy_update_start_iter-1 only grow the graph
+  *skipped = false;
+  TSVD_CUDA(cudaEventRecord(ea[0], s->st));
+  if (!on_device) {
+    TSVD_TRY(stage_edges_to_device(s, edges, m));
+    edges = s->edges_dev;
+  }
+  TSVD_TRY(insert_device(s, edges, m));
+  TSVD_CUDA(cudaEventRecord(ea[1], s->st));
+  if (after_insert) TSVD_TRY(after_insert());
   if (s->cfg.lazy_update_start_iter != 100 && iter < s->cfg.lazy_update_start_iter - 1) {
     s->last.skipped = 1;
     TSVD_CUDA(cudaStreamSynchronize(s->st));
-    s->last.ms_insert = s->last.ms_total = ms_between(ev[0], ev[1]);
+    s->last.ms_insert = s->last.ms_total = ms_between(ea[0], ea[1]);
+    *skipped = true;
     return TSVD_OK;
   }
   TSVD_TRY(stage_ppr(s, iter, 0));
   if (s->directed) TSVD_TRY(stage_ppr(s, iter, 1));
-  TSVD_CUDA(cudaEventRecord(ev[2], s->st));
-  TSVD_TRY(stage_materialize(s, iter));
-  TSVD_CUDA(cudaEventRecord(ev[3], s->st));
-  TSVD_TRY(stage_factorize(s, iter));
-  TSVD_CUDA(cudaEventRecord(ev[4], s->st));
-  TSVD_TRY(stage_merge(s));
-  TSVD_CUDA(cudaEventRecord(ev[5], s->st));
-  TSVD_CUDA(cudaEventSynchronize(ev[5]));
-  if (s->cfg.lp_right_factor) {
-    TSVD_TRY(stage_lp(s, iter));
-    TSVD_CUDA(cudaEventRecord(ev[6], s->st));
-    TSVD_CUDA(cudaEventSynchronize(ev[6]));
-    s->last.ms_lp = ms_between(ev[5], ev[6]);
-  }
-  s->last.ms_insert = ms_between(ev[0], ev[1]);
-  s->last.ms_push = ms_between(ev[1], ev[2]);
-  s->last.ms_log = ms_between(ev[2], ev[3]);
-  s->last.ms_frpca = ms_between(ev[3], ev[4]);
-  s->last.ms_merge = ms_between(ev[4], ev[5]);
-  s->last.ms_total = ms_between(ev[0], ev[5]) + s->last.ms_lp;
+  TSVD_CUDA(cudaEventRecord(ea[2], s->st));
+  TSVD_TRY(materialize_launch(s));
+  TSVD_CUDA(cudaEventRecord(ea[3], s->st));
   return TSVD_OK;
 }
 
-static tsvd_status stage_edges_to_device(tsvd_session *s, const int32_t *edges, int64_t m) {
+// Factorization, merge and LP right factor of one snapshot on stream st,
+// then (when out is given) the read-back of its embedding, widened to double
+// (|S| x d; zeros before the first embedding). eb[0..3] mark the stage
+// boundaries. Returns with st drained.
+static tsvd_status stage_back(tsvd_session *s, FactorJob &job, cudaStream_t st, cudaEvent_t *eb,
+                              double *out) {
+  TSVD_CUDA(cudaEventRecord(eb[0], st));
+  TSVD_TRY(stage_factorize(s, job, st));
+  TSVD_CUDA(cudaEventRecord(eb[1], st));
+  TSVD_TRY(stage_merge(s, job, st));
+  TSVD_CUDA(cudaEventRecord(eb[2], st));
+  if (s->cfg.lp_right_factor) TSVD_TRY(stage_lp(s, job, st));
+  const size_t E = s->node_elems();
+  if (out && s->has_embedding)
+    TSVD_CUDA(cudaMemcpyAsync(s->emb_stage, s->embedding, sizeof(float) * E,
+                              cudaMemcpyDeviceToHost, st));
+  TSVD_CUDA(cudaEventRecord(eb[3], st));
+  TSVD_CUDA(cudaEventSynchronize(eb[3]));
+  if (out) {
+    if (s->has_embedding)
+      for (size_t i = 0; i < E; ++i) out[i] = s->emb_stage[i];
+    else
+      std::fill(out, out + E, 0.0);
+  }
+  return TSVD_OK;
+}
+
+// Stage times of a finished snapshot. ms_total is its latency: from the
+// start of its graph insert to the end of its factor stage.
+static void finish_stats(tsvd_step_stats &st, cudaEvent_t *ea, cudaEvent_t *eb) {
+  st.ms_insert = ms_between(ea[0], ea[1]);
+  st.ms_push = ms_between(ea[1], ea[2]);
+  st.ms_log = ms_between(ea[2], ea[3]);
+  st.ms_frpca = ms_between(eb[0], eb[1]);
+  st.ms_merge = ms_between(eb[1], eb[2]);
+  st.ms_lp = ms_between(eb[2], eb[3]);
+  st.ms_total = ms_between(ea[0], eb[3]);
+}
+
+static tsvd_status step_device(tsvd_session *s, const int32_t *edges, bool on_device, int64_t m) {
+  TSVD_CUDA(cudaSetDevice(s->cfg.device));
+  bool skipped = false;
+  TSVD_TRY(stage_front(s, edges, on_device, m, s->ev, &skipped));
+  if (skipped) return TSVD_OK;
+  TSVD_TRY(materialize_decide(s, s->iter));
+  FactorJob job;
+  make_job(s, s->iter, job);
+  TSVD_TRY(stage_back(s, job, s->st, s->ev + 4, nullptr));
+  finish_stats(job.stats, s->ev, s->ev + 4);
+  s->last = job.stats;
+  return TSVD_OK;
+}
+
+// The current embedding, widened to double, into out (|S| x d); zeros before
+// the first one. Drains st.
+static tsvd_status embedding_to_host(tsvd_session *s, cudaStream_t st, double *out) {
+  const size_t E = s->node_elems();
+  if (!s->has_embedding) {
+    std::fill(out, out + E, 0.0);
+    return TSVD_OK;
+  }
+  TSVD_CUDA(cudaMemcpyAsync(s->emb_stage, s->embedding, sizeof(float) * E, cudaMemcpyDeviceToHost, st));
+  TSVD_CUDA(cudaStreamSynchronize(st));
+  for (size_t i = 0; i < E; ++i) out[i] = s->emb_stage[i];
+  return TSVD_OK;
+}
+
+static tsvd_status reserve_edges(tsvd_session *s, int64_t m) {
   if (m > s->edges_cap) {
     cudaFree(s->edges_dev);
     s->edges_dev = nullptr;
@@ -678,6 +802,11 @@ static tsvd_status stage_edges_to_device(tsvd_session *s, const int32_t *edges, 
     TSVD_CUDA(cudaMalloc(&s->edges_dev, sizeof(int32_t) * 2 * cap));
     s->edges_cap = cap;
   }
+  return TSVD_OK;
+}
+
+static tsvd_status stage_edges_to_device(tsvd_session *s, const int32_t *edges, int64_t m) {
+  TSVD_TRY(reserve_edges(s, m));
   if (m > 0)
     TSVD_CUDA(cudaMemcpyAsync(s->edges_dev, edges, sizeof(int32_t) * 2 * m, cudaMemcpyHostToDevice,
                               s->st));
@@ -686,15 +815,120 @@ static tsvd_status stage_edges_to_device(tsvd_session *s, const int32_t *edges, 
 
 extern "C" tsvd_status tsvd_session_step(tsvd_session *s, const int32_t *edges, int64_t m) {
   if (!s || (m > 0 && !edges) || m < 0) return fail(TSVD_ERR_INVALID, "bad arguments");
-  TSVD_CUDA(cudaSetDevice(s->cfg.device));
-  TSVD_TRY(stage_edges_to_device(s, edges, m));
-  return step_device(s, s->edges_dev, m);
+  return step_device(s, edges, false, m);
 }
 
 extern "C" tsvd_status tsvd_session_step_device(tsvd_session *s, const int32_t *edges_dev,
                                                 int64_t m) {
   if (!s || (m > 0 && !edges_dev) || m < 0) return fail(TSVD_ERR_INVALID, "bad arguments");
-  return step_device(s, edges_dev, m);
+  return step_device(s, edges_dev, true, m);
+}
+
+// Snapshots [0, count): snapshot k's edges are the pairs [offsets[k],
+// offsets[k+1]) of `edges` (device memory when on_device). The factor stage
+// of snapshot k (frPCA, merge, LP right factor) runs on a worker thread and
+// the low-priority second stream, started once the insert of snapshot k+1 is
+// issued (the insert's short dependent kernels run on an idle GPU), while
+// this thread refreshes, pushes and materializes snapshot k+1. The two
+// overlap without sharing buffers: the materialization of k+1 writes only
+// the candidate block buffers, which the factor stage of k does not read,
+// and the dirty decision of k+1 (which reads the residuals of k) waits for
+// the factor stage of k. A failing snapshot still lets the factor stage of
+// the one before it finish, so the session stays consistent.
+static tsvd_status run_snapshots(tsvd_session *s, const int32_t *edges, bool on_device,
+                                 const int64_t *offsets, int32_t count, double *emb_out,
+                                 tsvd_step_stats *stats_out) {
+  TSVD_CUDA(cudaSetDevice(s->cfg.device));
+  int64_t max_m = 0;
+  for (int k = 0; k < count; ++k) {
+    const int64_t m = offsets[k + 1] - offsets[k];
+    if (m < 0 || offsets[k] < 0) return fail(TSVD_ERR_INVALID, "offsets must not decrease");
+    max_m = std::max(max_m, m);
+  }
+  if (max_m > 0 && !edges) return fail(TSVD_ERR_INVALID, "null edges");
+  if (!on_device) TSVD_TRY(reserve_edges(s, max_m));  // no reallocation while the worker runs
+  const size_t E = s->node_elems();
+  FactorJob jobs[2];
+  std::thread worker;
+  tsvd_status wst = TSVD_OK;
+  std::string wmsg;
+  int prepared = -1;  // snapshot whose factor job is built but not started
+  int pending = -1;   // snapshot whose factor job is running
+  auto launch = [&]() -> tsvd_status {
+    if (prepared < 0) return TSVD_OK;
+    const int k = prepared;
+    prepared = -1;
+    cudaEvent_t *ea = s->pev[k & 1];
+    if (cudaStreamWaitEvent(s->st2, ea[3], 0) != cudaSuccess)
+      return fail(TSVD_ERR_DEVICE, "cudaStreamWaitEvent failed");
+    FactorJob *job = &jobs[k & 1];
+    double *out = emb_out ? emb_out + k * E : nullptr;
+    wst = TSVD_OK;
+    try {
+      worker = std::thread([s, job, &wst, &wmsg, ea, out]() {
+        tsvd_status r = cudaSetDevice(s->cfg.device) == cudaSuccess
+                            ? TSVD_OK
+                            : fail(TSVD_ERR_DEVICE, "cudaSetDevice failed on the factor thread");
+        if (r == TSVD_OK) r = stage_back(s, *job, s->st2, ea + 4, out);
+        if (r != TSVD_OK) wmsg = tsvd_last_error();
+        wst = r;
+      });
+    } catch (...) {
+      return fail(TSVD_ERR_STATE, "could not start the factor thread");
+    }
+    pending = k;
+    return TSVD_OK;
+  };
+  auto join = [&]() -> tsvd_status {
+    if (worker.joinable()) worker.join();
+    if (pending < 0) return TSVD_OK;
+    const int k = pending;
+    pending = -1;
+    if (wst != TSVD_OK) return fail(wst, "%s", wmsg.c_str());
+    FactorJob &job = jobs[k & 1];
+    finish_stats(job.stats, s->pev[k & 1], s->pev[k & 1] + 4);
+    s->last = job.stats;
+    if (stats_out) stats_out[k] = job.stats;
+    return TSVD_OK;
+  };
+  tsvd_status st = TSVD_OK;
+  for (int k = 0; k < count; ++k) {
+    const int64_t m = offsets[k + 1] - offsets[k];
+    const int32_t *e = edges ? edges + 2 * offsets[k] : nullptr;
+    cudaEvent_t *ea = s->pev[k & 1];
+    bool skipped = false;
+    if ((st = stage_front(s, e, on_device, m, ea, &skipped, launch)) != TSVD_OK) break;
+    const tsvd_step_stats front = s->last;
+    if ((st = join()) != TSVD_OK) break;  // the factor stage of snapshot k - 1
+    s->last = front;
+    if (skipped) {
+      if (stats_out) stats_out[k] = s->last;
+      if (emb_out && (st = embedding_to_host(s, s->st, emb_out + k * E)) != TSVD_OK) break;
+      continue;
+    }
+    if ((st = materialize_decide(s, s->iter)) != TSVD_OK) break;
+    make_job(s, s->iter, jobs[k & 1]);
+    prepared = k;
+  }
+  // the last prepared job (also after a failure: its blocks are accepted)
+  tsvd_status ls = launch();
+  if (ls != TSVD_OK && st == TSVD_OK) st = ls;
+  const tsvd_status js = join();
+  return st != TSVD_OK ? st : js;
+}
+
+extern "C" tsvd_status tsvd_session_run(tsvd_session *s, const int32_t *edges,
+                                        const int64_t *offsets, int32_t count, double *embeddings,
+                                        tsvd_step_stats *stats) {
+  if (!s || !offsets || count < 0) return fail(TSVD_ERR_INVALID, "bad arguments");
+  return run_snapshots(s, edges, false, offsets, count, embeddings, stats);
+}
+
+extern "C" tsvd_status tsvd_session_run_device(tsvd_session *s, const int32_t *edges_dev,
+                                               const int64_t *offsets, int32_t count,
+                                               double *embeddings, tsvd_step_stats *stats) {
+  if (!s || !offsets || count < 0) return fail(TSVD_ERR_INVALID, "bad arguments");
+  return run_snapshots(s, edges_dev, true, offsets, count, embeddings, stats);
 }
 
 extern "C" tsvd_status tsvd_session_embedding(tsvd_session *s, double *out) {
@@ -772,13 +1006,24 @@ extern "C" tsvd_status tsvd_blocks_materialize(tsvd_session *s, int32_t iter, ui
 extern "C" tsvd_status tsvd_blocks_factorize(tsvd_session *s, int32_t iter) {
   if (!s) return fail(TSVD_ERR_INVALID, "null session");
   TSVD_CUDA(cudaSetDevice(s->cfg.device));
-  return stage_factorize(s, iter);
+  FactorJob job;
+  make_job(s, iter, job);
+  TSVD_TRY(stage_factorize(s, job, s->st));
+  TSVD_CUDA(cudaStreamSynchronize(s->st));
+  s->last.factorized_blocks = job.stats.factorized_blocks;
+  s->last.eig_sweeps_frpca = job.stats.eig_sweeps_frpca;
+  return TSVD_OK;
 }
 
 extern "C" tsvd_status tsvd_tree_merge(tsvd_session *s) {
   if (!s) return fail(TSVD_ERR_INVALID, "null session");
   TSVD_CUDA(cudaSetDevice(s->cfg.device));
-  return stage_merge(s);
+  FactorJob job;
+  make_job(s, s->iter, job);
+  TSVD_TRY(stage_merge(s, job, s->st));
+  s->last.merged_nodes = job.stats.merged_nodes;
+  s->last.eig_sweeps_merge = job.stats.eig_sweeps_merge;
+  return TSVD_OK;
 }
 
 // ------------------------------------------------------------------ inspection
@@ -824,7 +1069,7 @@ extern "C" tsvd_status tsvd_ppr_state(tsvd_session *s, int32_t transpose, int32_
   const PprState &P = s->ppr[transpose ? 1 : 0];
   std::vector<float> tmp((size_t)s->n * s->sp);
   TSVD_CUDA(cudaMemcpy(tmp.data(), which ? P.p : P.r, sizeof(float) * tmp.size(),
-                       cudaMemcpyDeviceToHost));
+                       cudaMemcpyDefault));  // p may be mapped host memory
   for (int v = 0; v < s->n; ++v)
     for (int k = 0; k < s->S; ++k) out[(size_t)k * s->n + v] = tmp[ppr_cell(v, k, s->n)];
   return TSVD_OK;

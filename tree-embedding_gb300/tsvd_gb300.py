@@ -42,6 +42,7 @@ class Config(ctypes.Structure):
         ("device", ctypes.c_int32), ("max_push_rounds", ctypes.c_int32),
         ("push_levels", ctypes.c_int32), ("push_ratio", ctypes.c_double),
         ("push_cofrac", ctypes.c_double), ("lp_right_factor", ctypes.c_int32),
+        ("ppr_host_reserve", ctypes.c_int32),
     ]
 
 
@@ -90,6 +91,10 @@ _SIGS = {
     "tsvd_session_destroy": (ctypes.c_int, [_vp]),
     "tsvd_session_step": (ctypes.c_int, [_vp, _i32p, ctypes.c_int64]),
     "tsvd_session_step_device": (ctypes.c_int, [_vp, _vp, ctypes.c_int64]),
+    "tsvd_session_run": (ctypes.c_int, [_vp, _i32p, _i64p, ctypes.c_int32, _f64p,
+                                        ctypes.POINTER(StepStats)]),
+    "tsvd_session_run_device": (ctypes.c_int, [_vp, _vp, _i64p, ctypes.c_int32, _f64p,
+                                               ctypes.POINTER(StepStats)]),
     "tsvd_session_embedding": (ctypes.c_int, [_vp, _f64p]),
     "tsvd_session_embedding_device": (ctypes.c_int, [_vp, ctypes.POINTER(_vp)]),
     "tsvd_session_last_stats": (ctypes.c_int, [_vp, ctypes.POINTER(StepStats)]),
@@ -234,7 +239,7 @@ class Session:
                  transform=TRANSFORM_LOG10_NC, dirty_rule=DIRTY_REFERENCE, dirty_frac=0.01,
                  root_scaling=ROOT_SQRT_SIGMA, refresh_mode=REFRESH_EXACT, seed=20231, device=0,
                  max_push_rounds=0, push_levels=1, push_ratio=8.0, push_cofrac=0.5,
-                 lp_right_factor=False):
+                 lp_right_factor=False, ppr_host_reserve=False):
         self.sources = np.ascontiguousarray(sources, dtype=np.int32)
         c = Config()
         lib().tsvd_config_default(ctypes.byref(c))
@@ -253,6 +258,7 @@ class Session:
         c.push_levels, c.push_ratio = int(push_levels), float(push_ratio)
         c.push_cofrac = float(push_cofrac)
         c.lp_right_factor = int(bool(lp_right_factor))
+        c.ppr_host_reserve = int(bool(ppr_host_reserve))
         self.cfg = c
         self.n, self.S, self.d = c.n_vertices, c.n_sources, c.rank_d
         self.n_parts, self.h, self.directed = c.n_parts, c.hierarchy_n, bool(directed)
@@ -284,6 +290,32 @@ class Session:
 
     def step_device(self, ptr, m):
         _check(lib().tsvd_session_step_device(self._h, _vp(ptr), int(m)))
+
+    def run(self, snapshots, embeddings=True):
+        """Several snapshots in one call, the factor stage of each overlapped
+        with the next one's push (tsvd_session_run). `snapshots` is a list of
+        (m, 2) edge arrays. Returns (list of stats dicts, embeddings array of
+        shape (len(snapshots), |S|, d) or None)."""
+        snaps = [np.ascontiguousarray(e, dtype=np.int32).reshape(-1, 2) for e in snapshots]
+        off = np.zeros(len(snaps) + 1, np.int64)
+        off[1:] = np.cumsum([len(e) for e in snaps])
+        edges = np.ascontiguousarray(np.concatenate(snaps) if snaps else np.zeros((0, 2), np.int32))
+        return self._run(lambda *a: lib().tsvd_session_run(self._h, _p(edges, _i32p), *a),
+                         off, embeddings)
+
+    def run_device(self, ptr, offsets, embeddings=True):
+        """tsvd_session_run_device: snapshot k is the device pairs
+        [offsets[k], offsets[k+1]) at `ptr`."""
+        off = np.ascontiguousarray(offsets, dtype=np.int64)
+        return self._run(lambda *a: lib().tsvd_session_run_device(self._h, _vp(ptr), *a),
+                         off, embeddings)
+
+    def _run(self, call, off, embeddings):
+        count = len(off) - 1
+        stats = (StepStats * max(count, 1))()
+        emb = np.zeros((count, self.S, self.d), np.float64) if embeddings else None
+        _check(call(_p(off, _i64p), count, _p(emb, _f64p) if embeddings else None, stats))
+        return [stats[k].as_dict() for k in range(count)], emb
 
     def embedding(self):
         out = np.zeros((self.S, self.d), np.float64)
