@@ -169,8 +169,8 @@ typedef struct tsvd_config {
   int32_t max_push_rounds;  /* bound on frontier rounds per push (0 = default)       */
   int32_t push_levels;      /* threshold schedule: push r > rmax*ratio^k, k = L-1..0  */
   double push_ratio;        /* (1 level = the plain rmax test)                      */
-  double push_cofrac;       /* co-push residues > rmax*cofrac on lines being pushed  */
-                            /* (default 0.5; 1 = plain rmax test only)               */
+  double push_cofrac;       /* co-push residues > rmax*cofrac on runs being pushed   */
+                            /* (default 0.85; 1 = plain rmax test only)              */
   int32_t lp_right_factor;  /* 1: after every snapshot, V_b = A_b^T U for each block  */
                             /* refreshed in it (LP drivers; needs TSVD_ROOT_U)        */
   int32_t ppr_host_reserve; /* 1: the reserve p (half of the PPR state) lives in     */

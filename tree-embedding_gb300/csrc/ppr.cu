@@ -58,23 +58,30 @@ __device__ __forceinline__ void flush_stats(const StatAcc &acc, unsigned long lo
   if (acc.iedges) atomicAdd(slot + 3, acc.iedges);
 }
 
-// Scatter w (two sources per lane) of vertex v's chunk c to neighbours
-// [j0, j1): fire-and-forget vector atomic adds (RED.v2), and every
-// neighbour's (u, chunk) is marked in the touched bitset for collect_kernel.
+// Scatter w (sources 2 lane, 2 lane + 1; zero for sources not pushed) of
+// vertex v's chunk c to neighbours [j0, j1): fire-and-forget vector atomic
+// adds, and every neighbour's (u, chunk) is marked in the touched bitset for
+// collect_kernel. Each half-warp takes one neighbour per instruction, lane q
+// adding sources 4q..4q+3 as one float4 (RED.v4): two 256-byte runs per warp
+// instruction, half the L1 requests of one float2 per lane and neighbour.
 __device__ __forceinline__ void scatter_range(const PushArgs &a, const int32_t *nb, int32_t c,
-                                              bool act, float2 w, int32_t j0, int32_t j1,
-                                              int32_t mine) {
+                                              float2 w, int32_t j0, int32_t j1, int32_t mine) {
   const int lane = threadIdx.x & 31;
-  // r cells of (u, c * 64 + 2 lane + {0, 1}) = rc + 32 u
-  float2 *rc = reinterpret_cast<float2 *>(a.r + (int64_t)c * a.n * kChunk) + lane;
+  const int q = lane & 15, half = lane >> 4;
+  const float4 w4 = make_float4(__shfl_sync(kFull, w.x, 2 * q), __shfl_sync(kFull, w.y, 2 * q),
+                                __shfl_sync(kFull, w.x, 2 * q + 1),
+                                __shfl_sync(kFull, w.y, 2 * q + 1));
+  const bool act = w4.x != 0.0f || w4.y != 0.0f || w4.z != 0.0f || w4.w != 0.0f;
+  // r cells of (u, c * 64 + 4 q + {0..3}) = rc + 16 u
+  float4 *rc = reinterpret_cast<float4 *>(a.r + (int64_t)c * a.n * kChunk) + q;
   // `mine` holds the ids of neighbours [j0, j0 + 32); each batch loads the
   // next batch's ids before issuing its own atomics
   for (int32_t jb = j0; jb < j1; jb += 32) {
     const int32_t jn = min(32, j1 - jb);
     const int32_t next = lane < j1 - jb - 32 ? __ldg(nb + jb + 32 + lane) : 0;
-    for (int32_t t = 0; t < jn; ++t) {
-      const int32_t u = __shfl_sync(kFull, mine, t);
-      if (act) atomicAdd(rc + (int64_t)u * (kChunk / 2), w);
+    for (int32_t t = 0; t < jn; t += 2) {
+      const int32_t u = __shfl_sync(kFull, mine, (t + half) & 31);
+      if (act && t + half < jn) atomicAdd(rc + (int64_t)u * (kChunk / 4), w4);
     }
     // each lane marks the neighbour it loaded: 32 independent reductions
     if (lane < jn) mark_pair(a.tflag, mine, c, a.n);
@@ -141,7 +148,6 @@ __global__ void __launch_bounds__(256) push_kernel(PushArgs a) {
     if (act)  // only this warp writes the reserve of (v, chunk c) in a round
       *reinterpret_cast<float2 *>(pp) = make_float2(act0 ? fmaf(a.alpha_f, x.x, pv.x) : pv.x,
                                                     act1 ? fmaf(a.alpha_f, x.y, pv.y) : pv.y);
-    const unsigned mask = __ballot_sync(kFull, act);
     const int npush = __popc(__ballot_sync(kFull, act0)) + __popc(__ballot_sync(kFull, act1));
     if (lane == 0) {
       if (a.vmark[v] == 0) a.vmark[v] = 1;
@@ -166,10 +172,7 @@ __global__ void __launch_bounds__(256) push_kernel(PushArgs a) {
       const bool units_reserved = (int64_t)u0 + units <= a.unit_cap;
       if (ok) {
         reinterpret_cast<float2 *>(a.heavy_w)[(int64_t)slot * 32 + lane] = w;
-        if (lane == 0) {
-          a.heavy_item[slot] = make_int2(v, c);
-          a.heavy_mask[slot] = mask;
-        }
+        if (lane == 0) a.heavy_item[slot] = make_int2(v, c);
       }
       if (units_reserved)
         for (int32_t k = lane; k < units; k += 32)
@@ -177,7 +180,7 @@ __global__ void __launch_bounds__(256) push_kernel(PushArgs a) {
       if (ok) continue;
       // buffers full: process this hub inline
     }
-    scatter_range(a, nb, c, act, w, 0, d, mine0);
+    scatter_range(a, nb, c, w, 0, d, mine0);
   }
   flush_stats(acc, a.stats);
 }
@@ -191,14 +194,12 @@ __global__ void __launch_bounds__(256) push_heavy_kernel(PushArgs a) {
     int2 u = a.units[i];
     if (u.x < 0) continue;
     int2 it = a.heavy_item[u.x];
-    unsigned mask = a.heavy_mask[u.x];
     const float2 w = reinterpret_cast<const float2 *>(a.heavy_w)[(int64_t)u.x * 32 + lane];
-    bool act = (mask >> lane) & 1u;
     const int32_t d = a.deg[it.x];
     const int32_t *nb = a.nbr + a.off[it.x];
     const int32_t j1 = min(d, u.y + kHeavy);
     const int32_t mine0 = lane < j1 - u.y ? __ldg(nb + u.y + lane) : 0;
-    scatter_range(a, nb, it.y, act, w, u.y, j1, mine0);
+    scatter_range(a, nb, it.y, w, u.y, j1, mine0);
   }
 }
 
@@ -432,7 +433,6 @@ tsvd_status ppr_alloc(PprState &P, int32_t n, int32_t nsrc, int32_t sp, bool hos
   P.unit_cap = 1 << 22;
   TSVD_CUDA(cudaMalloc(&P.heavy_w, (size_t)P.heavy_cap * kChunk * sizeof(float)));
   TSVD_CUDA(cudaMalloc(&P.heavy_item, (size_t)P.heavy_cap * sizeof(int2)));
-  TSVD_CUDA(cudaMalloc(&P.heavy_mask, (size_t)P.heavy_cap * sizeof(uint32_t)));
   TSVD_CUDA(cudaMalloc(&P.units, (size_t)P.unit_cap * sizeof(int2)));
   TSVD_CUDA(cudaMalloc(&P.upd, (size_t)n * sizeof(int32_t)));
   TSVD_CUDA(cudaMalloc(&P.counters, 16 * sizeof(int32_t)));
@@ -451,7 +451,7 @@ void ppr_free(PprState &P) {
     cudaFree(P.p);
   cudaFree(P.tflag); cudaFree(P.pend);
   cudaFree(P.front[0]); cudaFree(P.front[1]);
-  cudaFree(P.heavy_w); cudaFree(P.heavy_item); cudaFree(P.heavy_mask); cudaFree(P.units);
+  cudaFree(P.heavy_w); cudaFree(P.heavy_item); cudaFree(P.units);
   cudaFree(P.upd); cudaFree(P.counters); cudaFree(P.stats);
   cudaFreeHost(P.host_counters);
   for (auto &e : P.kev)
@@ -534,7 +534,7 @@ tsvd_status job_begin(PushJob &J, PprState &P, const Adjacency &A, const PprPara
   pa.alpha_f = (float)prm.alpha; pa.one_minus_alpha_f = (float)(1.0 - prm.alpha);
   pa.rmax_f = rmax_f; pa.undirected = prm.undirected; pa.vmark = vmark;
   pa.co_f = prm.cofrac >= 1.0 ? rmax_f : (float)(prm.rmax * std::max(prm.cofrac, 0.0));
-  pa.heavy_w = P.heavy_w; pa.heavy_item = P.heavy_item; pa.heavy_mask = P.heavy_mask;
+  pa.heavy_w = P.heavy_w; pa.heavy_item = P.heavy_item;
   pa.heavy_count = P.counters + 2; pa.heavy_cap = P.heavy_cap;
   pa.units = P.units; pa.unit_count = P.counters + 3; pa.unit_cap = P.unit_cap;
   pa.overflow = P.counters + 4; pa.stats = P.stats;

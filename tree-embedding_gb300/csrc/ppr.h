@@ -29,7 +29,6 @@ struct PprState {
   bool seeded = false;
   float *heavy_w = nullptr;
   int2 *heavy_item = nullptr;
-  uint32_t *heavy_mask = nullptr;
   int2 *units = nullptr;
   int32_t heavy_cap = 0, unit_cap = 0;
   int32_t *upd = nullptr;
@@ -69,7 +68,6 @@ struct PushArgs {
   uint8_t *vmark;
   float *heavy_w;
   int2 *heavy_item;
-  uint32_t *heavy_mask;
   int32_t *heavy_count;
   int32_t heavy_cap;
   int2 *units;

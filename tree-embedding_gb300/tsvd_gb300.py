@@ -238,7 +238,7 @@ class Session:
                  dynamic_ppr_start_iter=100, lazy_update_start_iter=100, delta=0.3,
                  transform=TRANSFORM_LOG10_NC, dirty_rule=DIRTY_REFERENCE, dirty_frac=0.01,
                  root_scaling=ROOT_SQRT_SIGMA, refresh_mode=REFRESH_EXACT, seed=20231, device=0,
-                 max_push_rounds=0, push_levels=1, push_ratio=8.0, push_cofrac=0.5,
+                 max_push_rounds=0, push_levels=1, push_ratio=8.0, push_cofrac=0.85,
                  lp_right_factor=False, ppr_host_reserve=False):
         self.sources = np.ascontiguousarray(sources, dtype=np.int32)
         c = Config()
