@@ -318,10 +318,10 @@ def run_reference(args):
 # DRAM bytes (read + write) of push_kernel + push_heavy_kernel per pushed
 # item-neighbour (one 256-byte residue-run atomic), from one ncu capture of
 # every push launch of a timed rmat-d-2.7m snapshot (dram__bytes_read.sum +
-# dram__bytes_write.sum, one pass): 2580.3 GB over 7.478e9 item-neighbours,
+# dram__bytes_write.sum, one pass): 2443.6 GB over 7.615e9 item-neighbours,
 # one 256-byte run atomic each (profiles/push_kernel_rmat-d-2.7m.md).
 # `traffic` scales it to the launches of the run being reported.
-PUSH_TRAFFIC_BYTES_PER_ITEM_EDGE = 345.0
+PUSH_TRAFFIC_BYTES_PER_ITEM_EDGE = 320.9
 
 
 def push_roofline(stages):
