@@ -5,8 +5,13 @@
 #
 # The six functions are taken from Code/ppr_computation_store_dynamic.h by line
 # range; the rest of that header needs MKL, Eigen, Boost and emhash, none of
-# which exist here, so frpca.c, the log/SVD code and the drivers stay
-# unbuildable. Outputs go only to oracle/_ref/.
+# which exist here, so the log code and the drivers stay unbuildable.
+#
+# Second library, oracle/_ref/libtsvd_ref_frpca.so: the reference's frpca.c and
+# matrix_vector_functions_intel_mkl{,_ext}.c compiled unchanged against the MKL
+# stand-in in oracle/mkl_shim/ (dense BLAS/LAPACKE from the OpenBLAS bundled
+# with scipy; sparse products and random streams in mkl_shim.c), wrapped by
+# oracle/ref_frpca_shim.c. Outputs go only to oracle/_ref/.
 set -e
 HERE=$(cd "$(dirname "$0")" && pwd)
 REF=${TSVD_REFERENCE_DIR:-/root/reference/Code}
@@ -38,3 +43,16 @@ done
 ${CXX:-g++} -O2 -ffp-contract=off -fPIC -shared -std=c++14 -w \
   -I"$REF" -I"$OUT" "$HERE/ref_shim.cpp" -o "$OUT/libtsvd_ref.so"
 echo "built $OUT/libtsvd_ref.so"
+
+OB=$(${PYTHON:-python3} -c "import scipy, os, glob; print((glob.glob(os.path.join(os.path.dirname(scipy.__file__), '..', 'scipy.libs', 'libscipy_openblas-*.so')) + [''])[0])")
+if [ -z "$OB" ] || [ ! -f "$REF/frpca.c" ]; then
+  echo "scipy OpenBLAS or frpca.c not found; skipping oracle/_ref/libtsvd_ref_frpca.so" >&2
+  exit 0
+fi
+${CC:-gcc} -O2 -ffp-contract=off -fPIC -shared -std=gnu99 -w \
+  -I"$HERE/mkl_shim" -I"$REF" \
+  "$REF/frpca.c" "$REF/matrix_vector_functions_intel_mkl.c" \
+  "$REF/matrix_vector_functions_intel_mkl_ext.c" \
+  "$HERE/mkl_shim/mkl_shim.c" "$HERE/ref_frpca_shim.c" \
+  "$OB" -Wl,-rpath,"$(dirname "$OB")" -lm -o "$OUT/libtsvd_ref_frpca.so"
+echo "built $OUT/libtsvd_ref_frpca.so"

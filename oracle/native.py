@@ -229,3 +229,68 @@ class RefPPR:
         out = np.zeros((self.s, self.n), np.float64)
         ref_lib().ref_ppr_dense(self.h, _ptr(out, _f64p))
         return out
+
+
+# ---------------------------------------------------- reference frPCA / merge
+_REF_FRPCA_SO = os.path.join(HERE, "_ref", "libtsvd_ref_frpca.so")
+_ref_frpca_lib = None
+
+
+def ref_frpca_available():
+    return os.path.exists(_REF_FRPCA_SO)
+
+
+def ref_frpca_lib():
+    """The reference's frpca.c and matrix_vector_functions_intel_mkl{,_ext}.c
+    compiled against oracle/mkl_shim (oracle/build_ref.sh)."""
+    global _ref_frpca_lib
+    if _ref_frpca_lib is None:
+        L = ctypes.CDLL(_REF_FRPCA_SO)
+        L.tsvd_ref_set_seed.argtypes = [ctypes.c_uint64]
+        L.tsvd_ref_last_gaussian.restype = ctypes.c_int
+        L.tsvd_ref_last_gaussian.argtypes = [_f32p, ctypes.c_int]
+        L.tsvd_ref_frpca.restype = ctypes.c_int
+        L.tsvd_ref_frpca.argtypes = [ctypes.c_int, ctypes.c_int, _i32p, _i32p, _f64p,
+                                     ctypes.c_int, ctypes.c_int, _f64p, _f64p, _f64p]
+        L.tsvd_ref_merge_svd.restype = ctypes.c_int
+        L.tsvd_ref_merge_svd.argtypes = [ctypes.c_int, ctypes.c_int, _f64p, ctypes.c_int, _f64p,
+                                         _f64p]
+        _ref_frpca_lib = L
+    return _ref_frpca_lib
+
+
+def ref_frpca(A, k, q, seed=7):
+    """frPCA(A, k, q) of the reference (Code/frpca.c:239-326) on a scipy CSR
+    matrix. Returns U (m x k), S (k, in the reference's order), V (n x k) and
+    the Gaussian test matrix it drew (n x (k+5) for even q, m x (k+5) for odd
+    q), so the oracle can be run on the same one."""
+    L = ref_frpca_lib()
+    m, n = A.shape
+    rp = np.ascontiguousarray(A.indptr, np.int32)
+    ci = np.ascontiguousarray(A.indices, np.int32)
+    va = np.ascontiguousarray(A.data, np.float64)
+    U = np.zeros(m * k)
+    S = np.zeros(k)
+    V = np.zeros(n * k)
+    L.tsvd_ref_set_seed(seed)
+    L.tsvd_ref_frpca(m, n, _ptr(rp, _i32p), _ptr(ci, _i32p), _ptr(va, _f64p), k, q,
+                     _ptr(U, _f64p), _ptr(S, _f64p), _ptr(V, _f64p))
+    rows, l = (n if q % 2 == 0 else m), k + 5
+    g = np.zeros(rows * l, np.float32)
+    got = L.tsvd_ref_last_gaussian(_ptr(g, _f32p), rows * l)
+    assert got == rows * l, (got, rows * l)
+    omega = g.astype(np.float64).reshape(l, rows).T  # column-major, as the reference's mat
+    return U.reshape(k, m).T, S, V.reshape(k, n).T, omega
+
+
+def ref_merge_svd(M, d):
+    """dense_sub_svd_function's factor U_d S_d of M (Code/Tree_u_NC.cpp:238-262
+    via truncated_singular_value_decomposition, matrix_vector_functions_intel_mkl.c
+    :1259-1300). Returns (U S (m x d), sigma (d,))."""
+    L = ref_frpca_lib()
+    m, n = M.shape
+    Mc = np.asfortranarray(M, np.float64).ravel(order="F")
+    US = np.zeros(m * d)
+    sig = np.zeros(d)
+    L.tsvd_ref_merge_svd(m, n, _ptr(Mc, _f64p), d, _ptr(US, _f64p), _ptr(sig, _f64p))
+    return US.reshape(d, m).T, sig

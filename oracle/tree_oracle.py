@@ -19,12 +19,13 @@ module, as the checker. It restates the reference's algorithm literally:
 The reference seeds its Gaussian test matrix from time(NULL)
 (Code/matrix_vector_functions_intel_mkl.c:495); the oracle and the GPU both
 draw it from the shared counter-based generator instead, so the two consume
-identical test matrices. Where the reference has no tests or golden vectors
-for these steps (it has none), parity of this module with the reference is
-by construction of the restatement: the push/refresh/insert half is pinned
-bit-exactly against the reference compiled from its own sources
-(oracle/build_ref.sh); the frPCA/merge half (MKL-dependent) is parity
-unpinned.
+identical test matrices. The reference has no tests or golden vectors for
+these steps; this module is pinned against the reference compiled from its
+own sources (oracle/build_ref.sh): the push/refresh/insert half bit-exactly
+(oracle/_ref/libtsvd_ref.so), frPCA and the merge SVD to float64 rounding
+(oracle/_ref/libtsvd_ref_frpca.so: frpca.c and the MKL helper files built
+against the OpenBLAS-backed MKL stand-in in oracle/mkl_shim/, run on the same
+Gaussian draw), with golden fixtures of both in tests/golden/.
 """
 import ctypes
 

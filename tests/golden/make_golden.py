@@ -1,4 +1,5 @@
-"""Generates tests/golden/ref_ppr_*.npz from the reference's own code.
+"""Generates tests/golden/ref_ppr_*.npz, ref_frpca_*.npz and ref_merge.npz
+from the reference's own code.
 
 Runs the reference's graph store (Code/Graph_dynamic.h, fed through its own
 file reader) and its dense-path refresh + push functions
@@ -7,8 +8,15 @@ oracle/build_ref.sh into oracle/_ref/libtsvd_ref.so) on small seeded graphs,
 and stores the inputs and the reference's outputs (adjacency, degrees,
 residue, reserve, accumulated dense matrix) after every snapshot.
 
+The frPCA and merge fixtures come from the reference's frpca.c and
+matrix_vector_functions_intel_mkl{,_ext}.c compiled against the MKL stand-in
+(oracle/_ref/libtsvd_ref_frpca.so): a seeded sparse matrix, the Gaussian test
+matrix the reference drew, and its U, S, V; a seeded two-child merge matrix
+and dense_sub_svd_function's U S and singular values.
+
     sh oracle/build_ref.sh && python tests/golden/make_golden.py
 """
+import scipy.sparse as sp
 import os
 import sys
 import tempfile
@@ -63,9 +71,49 @@ def make(name, directed, n, S, sizes, alpha, rmax, dyn, nparts, seed):
     np.savez_compressed(os.path.join(HERE, "ref_ppr_%s.npz" % name), **out)
 
 
+FRPCA_CASES = {
+    # name: (m, n, rank, support fraction, k, q, seed)
+    "q6": (120, 500, 20, 0.12, 16, 6, 404),
+    "q3": (96, 400, 16, 0.15, 12, 3, 505),
+}
+
+
+def make_frpca(name, m, n, rank, frac, k, q, seed):
+    """A sum of `rank` sparse non-negative rank-one terms with weights 0.8^i
+    (rank <= k + 5, so frPCA recovers it up to rounding whatever the
+    Gaussian draw)."""
+    rng = np.random.default_rng(seed)
+    D = np.zeros((m, n))
+    for i in range(rank):
+        u = np.where(rng.random(m) < frac, rng.random(m) + 0.5, 0.0)
+        v = np.where(rng.random(n) < frac, rng.random(n) + 0.5, 0.0)
+        D += 5.0 * 0.8 ** i * np.outer(u, v)
+    A = sp.csr_matrix(D)
+    U, S, V, omega = native.ref_frpca(A, k, q, seed=seed)
+    np.savez_compressed(os.path.join(HERE, "ref_frpca_%s.npz" % name), indptr=A.indptr,
+                        indices=A.indices, data=A.data, shape=np.array(A.shape), k=k, q=q,
+                        omega=omega.astype(np.float32), U=U, S=S, V=V)
+
+
+def make_merge(seed=606, rows=150, d=32, h=2):
+    rng = np.random.default_rng(seed)
+    kids = []
+    for c in range(h):
+        Q = np.linalg.qr(rng.standard_normal((rows, d)))[0]
+        kids.append(Q * np.geomspace(50.0 / (c + 1), 0.5, d)[None, :])
+    M = np.hstack(kids)
+    US, sigma = native.ref_merge_svd(M, d)
+    np.savez_compressed(os.path.join(HERE, "ref_merge.npz"), M=M, d=d, US=US, sigma=sigma)
+
+
 if __name__ == "__main__":
-    if not native.ref_available():
+    if not native.ref_available() or not native.ref_frpca_available():
         native.build_ref()
     for name, args in CASES.items():
         make(name, *args)
         print("wrote", name)
+    for name, args in FRPCA_CASES.items():
+        make_frpca(name, *args)
+        print("wrote frpca", name)
+    make_merge()
+    print("wrote merge")

@@ -180,6 +180,27 @@ def test_frpca_abi_matches_oracle():
     assert np.linalg.norm(R - Ro) / np.linalg.norm(Ro) < 1e-3
 
 
+@pytest.mark.parametrize("name", ["q6", "q3"])
+def test_frpca_abi_matches_reference_golden(name):
+    """The GPU frPCA against the reference's own frpca.c output on the same
+    matrix (tests/golden/ref_frpca_*.npz, made by the reference compiled
+    against the MKL stand-in). The two draw different Gaussian matrices, so
+    the comparison is on what the randomization leaves fixed: the leading
+    singular values and the gap-separated leading subspace."""
+    import os
+    import scipy.sparse as sp
+    z = np.load(os.path.join(os.path.dirname(__file__), "golden", "ref_frpca_%s.npz" % name))
+    A = sp.csr_matrix((z["data"], z["indices"], z["indptr"]), shape=tuple(z["shape"]))
+    k, q = int(z["k"]), int(z["q"])
+    U, S, V = T.frpca(A.indptr, A.indices, A.data, A.shape, k, q, seed=5)
+    Sr, Ur, Vr = z["S"][::-1], z["U"][:, ::-1], z["V"][:, ::-1]  # reference order: ascending
+    j = gap_index(Sr, k)
+    assert j > 0
+    assert np.allclose(S[:j], Sr[:j], rtol=1e-3)
+    assert max_principal_sine(U[:, :j], Ur[:, :j]) < 1e-2
+    assert max_principal_sine(V[:, :j], Vr[:, :j]) < 1e-2
+
+
 def _lowrank_exact(m, n, s, seed):
     rng = np.random.default_rng(seed)
     U0, _ = np.linalg.qr(rng.standard_normal((m, len(s))))

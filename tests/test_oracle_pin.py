@@ -104,3 +104,65 @@ def test_oracle_push_identity_and_threshold():
         r, p = o.residue(), o.reserve()
         assert push_identity_residual(p, r, src, P, alpha) < 1e-5
         assert (r[:, deg > 0] <= rmax).all()
+
+
+# ------------------------------------------------- frPCA and merge (MKL path)
+FRPCA_GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden",
+                                             "ref_frpca_*.npz")))
+MERGE_GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "ref_merge.npz")
+
+
+def _csr(z):
+    import scipy.sparse as sp
+    return sp.csr_matrix((z["data"], z["indices"], z["indptr"]), shape=tuple(z["shape"]))
+
+
+def _check_frpca_against(A, k, q, omega, U, S, V, tol):
+    """Oracle frPCA on the reference's own Gaussian draw vs the reference's
+    U, S, V: same values, columns equal up to sign."""
+    from oracle.tree_oracle import frpca
+    if q % 2 == 0:
+        Uo, So, Vo = frpca(A.toarray(), k, q, omega=omega)
+    else:
+        Uo, So, Vo = frpca(A.toarray(), k, q, qrand=omega)
+    assert np.allclose(So, S, rtol=tol, atol=tol * np.abs(S).max())
+    for X, Xo in ((U, Uo), (V, Vo)):
+        cos = np.abs(np.sum(X * Xo, 0)) / (np.linalg.norm(X, axis=0) * np.linalg.norm(Xo, axis=0))
+        assert np.abs(cos - 1).max() < tol, np.abs(cos - 1).max()
+
+
+@pytest.mark.parametrize("path", FRPCA_GOLDEN, ids=[os.path.basename(p) for p in FRPCA_GOLDEN])
+def test_oracle_frpca_reproduces_reference_golden(path):
+    """tests/golden/ref_frpca_*.npz: the reference's frpca.c (compiled against
+    the MKL stand-in) on a seeded sparse matrix, with the Gaussian matrix it
+    drew. The oracle restates frpca.c:239-326 (LUfraction :4-41, eigSVD
+    :99-136) and must reproduce U, S, V to float64 rounding."""
+    z = np.load(path)
+    _check_frpca_against(_csr(z), int(z["k"]), int(z["q"]), z["omega"].astype(np.float64),
+                         z["U"], z["S"], z["V"], 1e-9)
+
+
+def test_oracle_merge_reproduces_reference_golden():
+    """tests/golden/ref_merge.npz: dense_sub_svd_function's U_d S_d and
+    singular values (LAPACK gesvd through the reference's own
+    truncated_singular_value_decomposition) of a two-child merge matrix,
+    against the oracle's merge step (numpy SVD)."""
+    z = np.load(MERGE_GOLDEN)
+    M, d = z["M"], int(z["d"])
+    U, S, _ = np.linalg.svd(M, full_matrices=False)
+    US = U[:, :d] * S[None, :d]
+    assert np.allclose(S[:d], z["sigma"], rtol=1e-12)
+    cos = np.abs(np.sum(US * z["US"], 0)) / (np.linalg.norm(US, axis=0) * np.linalg.norm(z["US"], axis=0))
+    assert np.abs(cos - 1).max() < 1e-10
+
+
+@pytest.mark.skipif(not native.ref_frpca_available(), reason="reference frpca.c not compiled here")
+@pytest.mark.parametrize("q", [2, 5, 6])
+def test_oracle_frpca_matches_reference_live(q):
+    import scipy.sparse as sp
+    rng = np.random.default_rng(40 + q)
+    m, n, k = 90, 420, 10
+    base = (rng.standard_normal((m, 16)) * np.geomspace(3.0, 0.1, 16)) @ rng.standard_normal((16, n))
+    A = sp.csr_matrix(np.where(rng.random((m, n)) < 0.15, np.abs(base) + 0.5, 0.0))
+    U, S, V, omega = native.ref_frpca(A, k, q, seed=q)
+    _check_frpca_against(A, k, q, omega, U, S, V, 1e-9)
