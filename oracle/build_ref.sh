@@ -3,9 +3,10 @@
 # the reference sources where they lie into oracle/_ref/libtsvd_ref.so (test
 # infrastructure: it pins the CPU oracle; nothing in the product uses it).
 #
-# The six functions are taken from Code/ppr_computation_store_dynamic.h by line
-# range; the rest of that header needs MKL, Eigen, Boost and emhash, none of
-# which exist here, so the log code and the drivers stay unbuildable.
+# The six refresh/push functions and the four log-transform functions are taken
+# from Code/ppr_computation_store_dynamic.h by line range; the rest of that
+# header needs MKL, Eigen, Boost and emhash, none of which exist here, so the
+# drivers stay unbuildable.
 #
 # Second library, oracle/_ref/libtsvd_ref_frpca.so: the reference's frpca.c and
 # matrix_vector_functions_intel_mkl{,_ext}.c compiled unchanged against the MKL
@@ -30,7 +31,11 @@ for spec in \
   2945:3030:nodegree_DenseDirectedDynamicForwardPush \
   3356:3437:nodegree_DenseDirectedDynamicForwardPushTranspose \
   3811:3898:nodegree_DenseDirected_Refresh_PPR_initialization \
-  4133:4228:nodegree_DenseDirected_Refresh_PPR_initialization_Transpose; do
+  4133:4228:nodegree_DenseDirected_Refresh_PPR_initialization_Transpose \
+  2527:2561:Log_sparse_matrix_entries \
+  2598:2638:Log_sparse_matrix_entries_LP \
+  2649:2732:Log_sparse_matrix_entries_with_norm_computation \
+  2742:2826:Log_sparse_matrix_entries_with_norm_computation_LP; do
   a=${spec%%:*}; rest=${spec#*:}; b=${rest%%:*}; name=${rest#*:}
   first=$(sed -n "${a}p" "$H")
   case "$first" in

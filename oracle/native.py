@@ -160,6 +160,8 @@ def ref_lib():
                                    ctypes.c_int, ctypes.c_int]
         L.ref_ppr_state.argtypes = [ctypes.c_void_p, ctypes.c_int, _f32p]
         L.ref_ppr_dense.argtypes = [ctypes.c_void_p, _f64p]
+        L.ref_log_blocks.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                     ctypes.c_double, _f64p, _f64p, _i32p, _i64p]
         _ref = L
     return _ref
 
@@ -229,6 +231,21 @@ class RefPPR:
         out = np.zeros((self.s, self.n), np.float64)
         ref_lib().ref_ppr_dense(self.h, _ptr(out, _f64p))
         return out
+
+    def log_blocks(self, lp, with_norm, iter, delta, resid):
+        """The reference's log transform + lazy test of every block of the
+        accumulated dense matrix (Code/ppr_computation_store_dynamic.h
+        :2527-2826). Returns (accepted log blocks |S| x N, update record per
+        block: -1 kept / iter refreshed, nnz record)."""
+        nparts = len(resid)
+        acc = np.zeros((self.s, self.n), np.float64)
+        rec = np.zeros(nparts, np.int32)
+        nnz = np.zeros(nparts, np.int64)
+        r = np.ascontiguousarray(resid, np.float64)
+        ref_lib().ref_log_blocks(self.h, int(lp), int(with_norm), int(iter), float(delta),
+                                 _ptr(r, _f64p), _ptr(acc, _f64p), _ptr(rec, _i32p),
+                                 _ptr(nnz, _i64p))
+        return acc, rec, nnz
 
 
 # ---------------------------------------------------- reference frPCA / merge

@@ -13,6 +13,12 @@
 // The only reference type those functions touch beyond the graph and queue is
 // d_row_tree_mkl::dense_mat_mapping[b](row, col) += x; a minimal stand-in with
 // that member is defined below.
+//
+// Also compiled: the four log-transform + lazy-test functions of the same
+// header (lines 2527-2561, 2598-2638, 2649-2732, 2742-2826). They use Eigen's
+// SparseMatrix (sparseView of the dense block, InnerIterator, norm, a
+// difference); Eigen is not in this image, so a minimal column-major sparse
+// matrix with that interface is written below.
 #include <algorithm>  // Graph_dynamic.h expects it first, as in the drivers
 #include <cmath>
 #include <cstdio>
@@ -27,15 +33,107 @@
 
 using namespace std;
 
+enum { ColMajor = 0 };
+
+// Column-major compressed sparse matrix: the subset of Eigen::SparseMatrix the
+// log functions use. Stored entries keep their order (rows ascending within a
+// column); norm() sums the squares in that order.
+template <typename T, int Options, typename Index>
+class SparseMatrix {
+ public:
+  struct Storage {
+    void squeeze() {}
+  };
+  int nrows = 0, ncols = 0;
+  vector<Index> outer = vector<Index>(1, 0), inner;
+  vector<T> val;
+
+  void resize(int r, int c) {
+    nrows = r;
+    ncols = c;
+    outer.assign((size_t)c + 1, 0);
+    inner.clear();
+    val.clear();
+  }
+  int outerSize() const { return ncols; }
+  Storage data() { return Storage(); }
+  double norm() const {
+    double acc = 0;
+    for (T x : val) acc += (double)x * (double)x;
+    return std::sqrt(acc);
+  }
+  // this - o over the union of the two patterns; an empty (0 x 0) operand is zero
+  SparseMatrix operator-(const SparseMatrix &o) const {
+    const SparseMatrix &a = *this;
+    SparseMatrix out;
+    const int c = std::max(a.ncols, o.ncols);
+    out.resize(std::max(a.nrows, o.nrows), c);
+    for (int j = 0; j < c; ++j) {
+      Index p = j < a.ncols ? a.outer[j] : 0, pe = j < a.ncols ? a.outer[j + 1] : 0;
+      Index q = j < o.ncols ? o.outer[j] : 0, qe = j < o.ncols ? o.outer[j + 1] : 0;
+      while (p < pe || q < qe) {
+        if (q >= qe || (p < pe && a.inner[p] < o.inner[q])) {
+          out.inner.push_back(a.inner[p]);
+          out.val.push_back(a.val[p++]);
+        } else if (p >= pe || o.inner[q] < a.inner[p]) {
+          out.inner.push_back(o.inner[q]);
+          out.val.push_back(-o.val[q++]);
+        } else {
+          out.inner.push_back(a.inner[p]);
+          out.val.push_back(a.val[p++] - o.val[q++]);
+        }
+      }
+      out.outer[j + 1] = (Index)out.val.size();
+    }
+    return out;
+  }
+
+  class InnerIterator {
+   public:
+    InnerIterator(SparseMatrix &m, int col) : m_(m), p_(m.outer[col]), end_(m.outer[col + 1]) {}
+    explicit operator bool() const { return p_ < end_; }
+    InnerIterator &operator++() {
+      ++p_;
+      return *this;
+    }
+    T value() const { return m_.val[p_]; }
+    T &valueRef() { return m_.val[p_]; }
+    Index row() const { return m_.inner[p_]; }
+
+   private:
+    SparseMatrix &m_;
+    Index p_, end_;
+  };
+};
+
 struct RefDenseBlock {
   int rows = 0, cols = 0;
   vector<double> v;
   double &operator()(int i, int j) { return v[(size_t)j * rows + i]; }
+  // the non-zero entries, as Eigen's sparseView() keeps them
+  SparseMatrix<double, 0, int> sparseView() const {
+    SparseMatrix<double, 0, int> m;
+    m.resize(rows, cols);
+    for (int j = 0; j < cols; ++j) {
+      for (int i = 0; i < rows; ++i) {
+        const double x = v[(size_t)j * rows + i];
+        if (x != 0.0) {
+          m.inner.push_back(i);
+          m.val.push_back(x);
+        }
+      }
+      m.outer[j + 1] = (int)m.val.size();
+    }
+    return m;
+  }
 };
 
 class d_row_tree_mkl {
  public:
   unordered_map<int, RefDenseBlock> dense_mat_mapping;
+  unordered_map<int, SparseMatrix<double, 0, int>> mat_mapping;
+  int row_dim = 0;
+  vector<double> norm_B_Bid_difference_vec;
 };
 
 #include "ref_functions.inc"
@@ -58,6 +156,7 @@ struct RefPPR {
   vector<bool *> flags;
   vector<Queue> queues;
   d_row_tree_mkl tree;
+  vector<long long int> nnz_record;
 };
 
 }  // namespace
@@ -238,6 +337,49 @@ void ref_ppr_dense(void *sp, double *out) {
     for (int i = 0; i < blk.rows; ++i)
       for (int j = 0; j < blk.cols; ++j)
         out[(size_t)i * st->n + (size_t)b * st->col_dim + j] = blk(i, j);
+  }
+}
+
+// The reference's log transform + lazy test of every block of the
+// accumulated dense matrix: Log_sparse_matrix_entries[_LP] when with_norm is
+// 0 (every block accepted), ..._with_norm_computation[_LP] otherwise, reading
+// resid[b] as norm_B_Bid_difference_vec[b]. Outputs: the accepted log blocks
+// (mat_mapping) as |S| x N doubles, the update record (-1: kept, iter:
+// refreshed) and the nnz record.
+void ref_log_blocks(void *sp, int lp, int with_norm, int iter, double delta,
+                    const double *resid, double *accepted, int *record, long long *nnz) {
+  RefPPR *st = (RefPPR *)sp;
+  const int P = st->nparts;
+  d_row_tree_mkl &t = st->tree;
+  t.row_dim = st->S;
+  t.norm_B_Bid_difference_vec.assign(resid, resid + P);
+  st->nnz_record.resize(P, 0);
+  unordered_map<int, vector<int>> vec_mapping;
+  for (int b = 0; b < P; ++b) vec_mapping[b].resize(t.dense_mat_mapping[b].cols);
+  vector<int> upd(P, 0);
+  for (int b = 0; b < P; ++b) {
+    if (!with_norm) {
+      if (lp)
+        Log_sparse_matrix_entries_LP(b, st->rmax, &t, vec_mapping, st->nnz_record);
+      else
+        Log_sparse_matrix_entries(b, st->rmax, &t, vec_mapping, st->nnz_record);
+      upd[b] = iter;
+    } else if (lp) {
+      Log_sparse_matrix_entries_with_norm_computation_LP(b, st->rmax, &t, vec_mapping, upd, iter,
+                                                         delta, st->S, 0, st->nnz_record);
+    } else {
+      Log_sparse_matrix_entries_with_norm_computation(b, st->rmax, &t, vec_mapping, upd, iter,
+                                                      delta, st->S, 0, st->nnz_record);
+    }
+  }
+  memset(accepted, 0, sizeof(double) * (size_t)st->S * st->n);
+  for (int b = 0; b < P; ++b) {
+    SparseMatrix<double, 0, int> &m = t.mat_mapping[b];
+    for (int j = 0; j < m.ncols; ++j)
+      for (int q = m.outer[j]; q < m.outer[j + 1]; ++q)
+        accepted[(size_t)m.inner[q] * st->n + (size_t)b * st->col_dim + j] = m.val[q];
+    record[b] = upd[b];
+    nnz[b] = st->nnz_record[b];
   }
 }
 

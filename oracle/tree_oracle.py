@@ -22,7 +22,9 @@ draw it from the shared counter-based generator instead, so the two consume
 identical test matrices. The reference has no tests or golden vectors for
 these steps; this module is pinned against the reference compiled from its
 own sources (oracle/build_ref.sh): the push/refresh/insert half bit-exactly
-(oracle/_ref/libtsvd_ref.so), frPCA and the merge SVD to float64 rounding
+(oracle/_ref/libtsvd_ref.so), the log transform and lazy test to the last bit
+of log10 (same library, with a sparse-matrix stand-in for Eigen), frPCA and
+the merge SVD to float64 rounding
 (oracle/_ref/libtsvd_ref_frpca.so: frpca.c and the MKL helper files built
 against the OpenBLAS-backed MKL stand-in in oracle/mkl_shim/, run on the same
 Gaussian draw), with golden fixtures of both in tests/golden/.

@@ -12,7 +12,9 @@ The frPCA and merge fixtures come from the reference's frpca.c and
 matrix_vector_functions_intel_mkl{,_ext}.c compiled against the MKL stand-in
 (oracle/_ref/libtsvd_ref_frpca.so): a seeded sparse matrix, the Gaussian test
 matrix the reference drew, and its U, S, V; a seeded two-child merge matrix
-and dense_sub_svd_function's U S and singular values.
+and dense_sub_svd_function's U S and singular values. ref_log.npz: the
+reference's log transform + lazy test (Log_sparse_matrix_entries*, both
+transforms) on its own accumulated matrix over a few snapshots.
 
     sh oracle/build_ref.sh && python tests/golden/make_golden.py
 """
@@ -95,6 +97,39 @@ def make_frpca(name, m, n, rank, frac, k, q, seed):
                         omega=omega.astype(np.float32), U=U, S=S, V=V)
 
 
+def make_log(seed=707, n=200, S=6, P=4, alpha=0.2, rmax=1e-4, delta=0.3, snaps=4):
+    """The reference's log transform + lazy test (both transforms) on the
+    dense matrix its own push accumulated, snapshot by snapshot, with
+    residuals drawn on the scale of the block norms."""
+    rng = np.random.default_rng(seed)
+    out = dict(n=n, S=S, P=P, alpha=alpha, rmax=rmax, delta=delta, nsnap=snaps)
+    for lp in (0, 1):
+        g = native.RefGraph(n, 0)
+        src = np.sort(rng.choice(n, S, replace=False)).astype(np.int32)
+        st = native.RefPPR(n, src, P, alpha, rmax)
+        out["sources_%d" % lp] = src
+        cd = n // P
+        prev = np.ones(P)
+        with tempfile.TemporaryDirectory() as d:
+            for it in range(1, snaps + 1):
+                e = rng.integers(0, n, (1200 if it == 1 else 50, 2)).astype(np.int32)
+                e = e[e[:, 0] != e[:, 1]]
+                path = os.path.join(d, "s%d.txt" % it)
+                native.write_edge_file(path, e, trailing_newline=True)
+                g.insert_file(path)
+                st.step(g, 0, it, 2)
+                dense = st.dense()
+                # residuals on the scale of the accepted blocks: both decisions occur
+                resid = rng.uniform(0.2, 0.6, P) * prev
+                acc, rec, nnz = st.log_blocks(lp, it >= 2, it, delta, resid)
+                prev = np.array([np.linalg.norm(acc[:, b * cd:(n if b == P - 1 else (b + 1) * cd)])
+                                 for b in range(P)])
+                for k, v in dict(dense=dense, resid=resid, accepted=acc, record=rec,
+                                 nnz=nnz).items():
+                    out["%s_%d_%d" % (k, lp, it)] = v
+    np.savez_compressed(os.path.join(HERE, "ref_log.npz"), **out)
+
+
 def make_merge(seed=606, rows=150, d=32, h=2):
     rng = np.random.default_rng(seed)
     kids = []
@@ -117,3 +152,5 @@ if __name__ == "__main__":
         print("wrote frpca", name)
     make_merge()
     print("wrote merge")
+    make_log()
+    print("wrote log")

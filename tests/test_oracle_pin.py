@@ -166,3 +166,78 @@ def test_oracle_frpca_matches_reference_live(q):
     A = sp.csr_matrix(np.where(rng.random((m, n)) < 0.15, np.abs(base) + 0.5, 0.0))
     U, S, V, omega = native.ref_frpca(A, k, q, seed=q)
     _check_frpca_against(A, k, q, omega, U, S, V, 1e-9)
+
+
+@pytest.mark.skipif(not native.ref_available(), reason="reference sources not compiled here")
+@pytest.mark.parametrize("transform", [0, 1])
+def test_oracle_log_and_lazy_test_match_reference_live(transform):
+    """The reference's own Log_sparse_matrix_entries[_LP] and
+    ..._with_norm_computation[_LP] (compiled from its header by line range,
+    with a minimal sparse-matrix stand-in for Eigen) on the dense matrix its
+    own push accumulated, against the oracle's log transform and reference
+    lazy rule on the same matrix and residuals: the same accepted blocks (up
+    to the last bit of log10, where numpy's and the C library's differ by one
+    ulp on a few percent of inputs), identical keep / refresh decisions (cases
+    within 1e-9 of the threshold excluded), identical nnz counts."""
+    from oracle.tree_oracle import OracleTreeSVD, TRANSFORM_LOG10_LP, TRANSFORM_LOG10_NC
+    rng = np.random.default_rng(11 + transform)
+    n, S, P, alpha, rmax, delta = 360, 10, 4, 0.2, 1e-4, 0.3
+    rg = native.RefGraph(n, 0)
+    src = np.sort(rng.choice(n, S, replace=False)).astype(np.int32)
+    rp = native.RefPPR(n, src, P, alpha, rmax)
+    tf = TRANSFORM_LOG10_LP if transform else TRANSFORM_LOG10_NC
+    o = OracleTreeSVD(n, src, alpha=alpha, rmax=rmax, n_parts=P, lazy_update_start_iter=2,
+                      delta=delta, transform=tf)
+    kept = refreshed = 0
+    for it in range(1, 6):
+        e = rng.integers(0, n, (1500 if it == 1 else 60, 2)).astype(np.int32)
+        e = e[e[:, 0] != e[:, 1]]
+        rg.insert(e, trailing_newline=True)
+        rp.step(rg, 0, it, 2)
+        dense = rp.dense()
+        # residuals on the scale of the block norms, so both decisions occur
+        norms = np.array([np.linalg.norm(o.accepted[b]) if o.accepted[b] is not None else 1.0
+                          for b in range(P)])
+        resid = rng.uniform(0.0, 0.5, P) * norms
+        with_norm = it >= 2
+        acc, rec, nnz = rp.log_blocks(transform, with_norm, it, delta, resid)
+        o.resid[:] = resid
+        o.blocks_stage(it, p=dense)
+        for b in range(P):
+            c0, c1 = o.block_cols(b)
+            margin = o.resid[b] + o.norm_diff[b] - delta * np.sqrt(2.0) * o.norm[b]
+            if with_norm and abs(margin) <= 1e-9 * o.norm[b]:
+                continue
+            assert (rec[b] != -1) == bool(o.dirty[b]), (it, b, rec[b], o.dirty[b])
+            kept += rec[b] == -1
+            refreshed += rec[b] != -1
+            assert np.allclose(acc[:, c0:c1], o.accepted[b], rtol=1e-15, atol=0), (it, b)
+            assert np.array_equal(acc[:, c0:c1] != 0, o.accepted[b] != 0)
+            if rec[b] != -1:
+                assert nnz[b] == (np.count_nonzero(o.accepted[b]) if transform else
+                                  np.count_nonzero(dense[:, c0:c1] > rmax))
+    assert kept > 0 and refreshed > 0
+
+
+def test_oracle_log_and_lazy_test_reproduce_reference_golden():
+    """tests/golden/ref_log.npz: the reference's log transform + lazy test on
+    its own accumulated matrix (both transforms, four snapshots), replayed
+    through the oracle's block stage with the same matrix and residuals."""
+    from oracle.tree_oracle import OracleTreeSVD, TRANSFORM_LOG10_LP, TRANSFORM_LOG10_NC
+    z = np.load(os.path.join(os.path.dirname(__file__), "golden", "ref_log.npz"))
+    n, P, rmax, delta = int(z["n"]), int(z["P"]), float(z["rmax"]), float(z["delta"])
+    for lp in (0, 1):
+        o = OracleTreeSVD(n, z["sources_%d" % lp], alpha=float(z["alpha"]), rmax=rmax, n_parts=P,
+                          lazy_update_start_iter=2, delta=delta,
+                          transform=TRANSFORM_LOG10_LP if lp else TRANSFORM_LOG10_NC)
+        for it in range(1, int(z["nsnap"]) + 1):
+            o.resid[:] = z["resid_%d_%d" % (lp, it)]
+            o.blocks_stage(it, p=z["dense_%d_%d" % (lp, it)])
+            acc, rec = z["accepted_%d_%d" % (lp, it)], z["record_%d_%d" % (lp, it)]
+            for b in range(P):
+                c0, c1 = o.block_cols(b)
+                margin = o.resid[b] + o.norm_diff[b] - delta * np.sqrt(2.0) * o.norm[b]
+                if it >= 2 and abs(margin) <= 1e-9 * o.norm[b]:
+                    continue
+                assert (rec[b] != -1) == bool(o.dirty[b]), (lp, it, b)
+                assert np.allclose(acc[:, c0:c1], o.accepted[b], rtol=1e-15, atol=0)
