@@ -98,6 +98,41 @@ def test_ppr_from_scratch_and_dynamic(directed):
                 _ppr_checks(s, g, src, cfg, bool(t), ors[t])
 
 
+@pytest.mark.parametrize("directed", [False, True])
+def test_ppr_hub_vertices(directed):
+    """Vertices with thousands of neighbours take the hub path: their pushes
+    are split into 1024-neighbour units (push_heavy_kernel). Three hubs of
+    2500-3000 neighbours on top of a small R-MAT graph, sources among the
+    hubs and their neighbours; same checks against the FIFO oracle."""
+    cfg = small_cfg(directed, n=5000, m=20000)
+    _, snaps, _ = W.build(cfg, seed=9)
+    rng = np.random.default_rng(9)
+    hubs = np.array([17, 1234, 4321], np.int32)
+    star = []
+    for h, k in zip(hubs, (2500, 2800, 3000)):
+        nb = rng.choice(np.setdiff1d(np.arange(cfg["n"]), hubs), k, replace=False).astype(np.int32)
+        star.append(np.stack([np.full(k, h, np.int32), nb], 1))
+        star.append(np.stack([nb[:k // 2], np.full(k // 2, h, np.int32)], 1))
+    first = np.concatenate([snaps[0]] + star).astype(np.int32)
+    src = np.unique(np.concatenate([hubs, star[0][:20, 1], rng.choice(cfg["n"], 20, replace=False)]))
+    src = src.astype(np.int32)
+    g = native.OracleGraph(cfg["n"], directed)
+    ors = [native.OraclePPR(cfg["n"], src) for _ in range(2 if directed else 1)]
+    kw = W.session_kwargs(cfg, dynamic_start=2)
+    with T.Session(cfg["n"], src, **kw) as s:
+        for it, e in enumerate([first, snaps[1], snaps[2]], start=1):
+            s.graph_insert(e)
+            g.insert(e)
+            deg, _ = g.degrees(0)
+            assert deg[hubs].min() > 2 * 1024
+            for t in range(2 if directed else 1):
+                s.ppr_refresh(it, bool(t))
+                s.ppr_push(bool(t))
+                ors[t].refresh(g, t, it, 2, cfg["alpha"], cfg["rmax"])
+                ors[t].push(g, t, cfg["alpha"], cfg["rmax"])
+                _ppr_checks(s, g, src, cfg, bool(t), ors[t])
+
+
 def test_ppr_intdiv_refresh_tracks_oracle():
     cfg = small_cfg()
     _, snaps, src = W.build(cfg, seed=9)
@@ -238,13 +273,16 @@ def test_frpca_abi_rank_deficient():
     assert max_principal_sine(U[:, :6], U0) < 1e-2
 
 
-@pytest.mark.parametrize("directed", [False, True])
-def test_session_matches_oracle_pipeline(directed):
+@pytest.mark.parametrize("directed,n,sources", [(False, 8000, 96), (True, 8000, 96),
+                                               (False, 7003, 40)])
+def test_session_matches_oracle_pipeline(directed, n, sources):
     """Whole snapshots through tsvd_session_step. The block stages (log
     transform, lazy test, frPCA, merge) are checked against the oracle run on
     the GPU's own reserve, so the comparison isolates their arithmetic; the
-    PPR stage is covered by test_ppr_from_scratch_and_dynamic."""
-    cfg = small_cfg(directed, n=8000, m=60000, sources=96, n_parts=4, rank_d=32, snapshots=4)
+    PPR stage is covered by test_ppr_from_scratch_and_dynamic. The last case
+    has a wider last block (7003 = 3 x 1750 + 1753) and fewer sources than
+    one 64-source chunk."""
+    cfg = small_cfg(directed, n=n, m=60000, sources=sources, n_parts=4, rank_d=32, snapshots=4)
     _, snaps, src = W.build(cfg, seed=21)
     kw = W.session_kwargs(cfg, dynamic_start=2, lazy_start=2)
     okw = dict(kw)
