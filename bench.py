@@ -44,6 +44,8 @@ def parse():
     ap.add_argument("--sources", type=int, default=None)
     ap.add_argument("--parts", type=int, default=None)
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--hierarchy", type=int, default=None,
+                    help="merge arity (the workload's default is 2; the reference's run.sh uses 8)")
     ap.add_argument("--host-reserve", action="store_true",
                     help="keep the PPR reserve in pinned host memory (ppr_host_reserve), for "
                          "workloads whose state exceeds HBM (rmat-d-6.2m)")
@@ -117,6 +119,8 @@ class ClockSampler:
 def workload(args):
     import workloads as W
     cfg = W.scaled(args.workload, n=args.n, m=args.m, sources=args.sources, n_parts=args.parts)
+    if args.hierarchy:
+        cfg["hierarchy_n"] = args.hierarchy
     need = 1 + args.warmup + args.steps
     if cfg["snapshots"] < need:
         cfg["snapshots"] = need  # the second half of the edges is cut into more, smaller deltas
@@ -409,6 +413,7 @@ def main():
             "config": {"workload": args.workload, "n": cfg["n"], "m": cfg["m"],
                        "directed": cfg["directed"], "sources": cfg["sources"],
                        "n_parts": cfg["n_parts"], "rank_d": cfg["rank_d"],
+                       "hierarchy_n": cfg["hierarchy_n"],
                        "passes_q": cfg["passes_q"], "snapshots": cfg["snapshots"],
                        "l2": "working set (PPR state) larger than L2",
                        "parallelism": "replicas x%d" % world,
@@ -425,7 +430,9 @@ def main():
             "push_items_mean": float(np.mean([s["push_items"] for s in res["stages"]])),
             "push_item_edges_mean": float(np.mean([s["push_item_edges"] for s in res["stages"]])),
             "ms_materialize_kernel_mean": float(np.mean([s["ms_materialize_kernel"] for s in res["stages"]])),
-            "dirty_blocks_mean": float(np.mean([s["dirty_blocks"] for s in res["stages"]]))}
+            "dirty_blocks_mean": float(np.mean([s["dirty_blocks"] for s in res["stages"]])),
+            "eig_sweeps_merge_max": int(max(s["eig_sweeps_merge"] for s in res["stages"])),
+            "merge_subspace_iters_max": int(max(s["merge_subspace_iters"] for s in res["stages"]))}
     line["roofline"] = push_roofline(res["stages"])
     if "e2e_ms" in res:
         line["e2e"] = {"value": edges_all / (res["e2e_ms"] / 1e3), "unit": "edge updates/s",

@@ -222,6 +222,8 @@ typedef struct tsvd_step_stats {
   double ms_lp;             /* LP right factor of the refreshed blocks            */
   int32_t eig_sweeps_frpca; /* Jacobi sweeps of the blocks' eigSVD (max)          */
   int32_t eig_sweeps_merge; /* Jacobi sweeps of the merges (max over levels)      */
+  int32_t merge_subspace_iters; /* subspace iterations of merges wider than 256  */
+                            /* columns (max over levels; 0 for narrow merges)    */
 } tsvd_step_stats;
 tsvd_status tsvd_session_last_stats(tsvd_session *s, tsvd_step_stats *out);
 

@@ -273,16 +273,22 @@ def test_frpca_abi_rank_deficient():
     assert max_principal_sine(U[:, :6], U0) < 1e-2
 
 
-@pytest.mark.parametrize("directed,n,sources", [(False, 8000, 96), (True, 8000, 96),
-                                               (False, 7003, 40)])
-def test_session_matches_oracle_pipeline(directed, n, sources):
+@pytest.mark.parametrize("directed,n,sources,parts,h,d", [
+    (False, 8000, 96, 4, 2, 32), (True, 8000, 96, 4, 2, 32), (False, 7003, 40, 4, 2, 32),
+    (False, 8000, 96, 8, 8, 40), (True, 8000, 300, 8, 8, 64), (False, 8000, 120, 64, 8, 40)])
+def test_session_matches_oracle_pipeline(directed, n, sources, parts, h, d):
     """Whole snapshots through tsvd_session_step. The block stages (log
     transform, lazy test, frPCA, merge) are checked against the oracle run on
     the GPU's own reserve, so the comparison isolates their arithmetic; the
-    PPR stage is covered by test_ppr_from_scratch_and_dynamic. The last case
+    PPR stage is covered by test_ppr_from_scratch_and_dynamic. The third case
     has a wider last block (7003 = 3 x 1750 + 1753) and fewer sources than
-    one 64-source chunk."""
-    cfg = small_cfg(directed, n=n, m=60000, sources=sources, n_parts=4, rank_d=32, snapshots=4)
+    one 64-source chunk. The last three merge 8 children at a time (the
+    reference's run.sh arity): 320, 512 and 320 columns per merge, wider than
+    one Jacobi matrix, through the subspace-iteration merge; the last with two
+    merge levels (64 -> 8 -> 1)."""
+    cfg = small_cfg(directed, n=n, m=60000, sources=sources, n_parts=parts, rank_d=d,
+                    snapshots=4)
+    cfg["hierarchy_n"] = h
     _, snaps, src = W.build(cfg, seed=21)
     kw = W.session_kwargs(cfg, dynamic_start=2, lazy_start=2)
     okw = dict(kw)

@@ -905,6 +905,77 @@ tsvd_status chol_inverse_batched(double *const *g, float *const *t, int l, int n
   return TSVD_OK;
 }
 
+// One block per problem: the lower Cholesky factor of G in fp64 in global
+// memory (it stays in L2), right-looking, a column per step. Directions whose
+// pivot falls below 1e-13 of the largest diagonal entry are dropped: unit
+// pivot, zero column, flag 1.0 after the factor (work: l*l + l doubles).
+__global__ void __launch_bounds__(1024) chol_wide_kernel(double *const *gs, double *work, int l) {
+  __shared__ double tol;
+  const double *G = gs[blockIdx.x];
+  double *A = work + (int64_t)blockIdx.x * (l * l + l);
+  double *drop = A + (int64_t)l * l;
+  for (int i = threadIdx.x; i < l * l; i += blockDim.x) A[i] = G[i];
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double mx = 0.0;
+    for (int i = 0; i < l; ++i) mx = fmax(mx, A[(int64_t)i * l + i]);
+    tol = mx * 1e-13;
+  }
+  __syncthreads();
+  for (int k = 0; k < l; ++k) {
+    if (threadIdx.x == 0) {
+      const double d = A[(int64_t)k * l + k];
+      const bool dk = !(d > tol) || !(d > 0.0);
+      drop[k] = dk ? 1.0 : 0.0;
+      A[(int64_t)k * l + k] = dk ? 1.0 : sqrt(d);
+    }
+    __syncthreads();
+    const double piv = A[(int64_t)k * l + k];
+    const bool dk = drop[k] != 0.0;
+    for (int i = k + 1 + threadIdx.x; i < l; i += blockDim.x)
+      A[(int64_t)i * l + k] = dk ? 0.0 : A[(int64_t)i * l + k] / piv;
+    __syncthreads();
+    const int n = l - k - 1;
+    for (int t = threadIdx.x; t < n * n; t += blockDim.x) {
+      const int i = k + 1 + t / n, j = k + 1 + t % n;
+      if (j <= i) A[(int64_t)i * l + j] -= A[(int64_t)i * l + k] * A[(int64_t)j * l + k];
+    }
+    __syncthreads();
+  }
+}
+
+// y = x R^-1 with R = L^T, one thread per row: y_j = (x_j - sum_{k<j} y_k
+// L[j][k]) / L[j][j] in fp64, dropped directions 0. x, y: rows x l (ld l) per
+// problem at stride `stride`.
+__global__ void trsm_rows_kernel(const float *__restrict__ x, float *__restrict__ y,
+                                 const double *__restrict__ work, int rows, int l,
+                                 int64_t stride) {
+  const int prob = blockIdx.y;
+  const double *L = work + (int64_t)prob * (l * l + l);
+  const double *drop = L + (int64_t)l * l;
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += gridDim.x * blockDim.x) {
+    const float *xr = x + prob * stride + (int64_t)r * l;
+    float *yr = y + prob * stride + (int64_t)r * l;
+    for (int j = 0; j < l; ++j) {
+      double s = xr[j];
+      const double *Lj = L + (int64_t)j * l;
+      for (int k = 0; k < j; ++k) s -= (double)yr[k] * Lj[k];
+      yr[j] = drop[j] != 0.0 ? 0.f : (float)(s / Lj[j]);
+    }
+  }
+}
+
+tsvd_status chol_solve_wide_batched(double *const *g, double *work, const float *x, float *y,
+                                    int rows, int l, int64_t stride, int nprob, cudaStream_t st) {
+  if (nprob == 0) return TSVD_OK;
+  if (l > 256 || l < 1) return fail(TSVD_ERR_INVALID, "chol wide: l=%d", l);
+  chol_wide_kernel<<<nprob, 1024, 0, st>>>(g, work, l);
+  TSVD_LAUNCH_CHECK();
+  trsm_rows_kernel<<<dim3(ceil_div(rows, 128), nprob), 128, 0, st>>>(x, y, work, rows, l, stride);
+  TSVD_LAUNCH_CHECK();
+  return TSVD_OK;
+}
+
 tsvd_status apply_right_batched(const float *const *x, const int32_t *rows, int max_rows, int ldx,
                                 const float *const *w, int ldw, int n_in, int n_out,
                                 const float *const *colscale, float *const *y, int ldy,

@@ -17,6 +17,8 @@
 #include <algorithm>
 #include <cmath>
 
+#include <cublas_v2.h>
+
 #include "factor.h"
 #include "philox_gauss.h"
 
@@ -220,6 +222,10 @@ void frpca_work_free(FrpcaWork &W) {
   cudaFree(W.qlo); cudaFree(W.g); cudaFree(W.t); cudaFree(W.lambda); cudaFree(W.v);
   cudaFree(W.colscale); cudaFree(W.sums); cudaFree(W.gram_work); cudaFree(W.jac_work); cudaFree(W.dptr);
   cudaFreeHost(W.hptr); cudaFree(W.dint); cudaFreeHost(W.hint);
+  cudaFree(W.wm); cudaFree(W.wv); cudaFree(W.ww); cudaFree(W.wy); cudaFree(W.wy2);
+  cudaFree(W.wchol); cudaFree(W.wnorm);
+  if (W.blas) cublasDestroy((cublasHandle_t)W.blas);
+  cudaGetLastError();  // the launch checks read this slot: leave nothing from teardown in it
   W = FrpcaWork();
 }
 
@@ -345,22 +351,18 @@ tsvd_status frpca_batch(FrpcaWork &W, const FrpcaProblem *probs, int nprob, int 
   return TSVD_OK;
 }
 
-tsvd_status merge_batch(FrpcaWork &W, const MergeProblem *probs, int nprob, int h, int nsrc,
-                        int root_mode, cudaStream_t st) {
-  if (nprob == 0) return TSVD_OK;
-  const int d = W.d, n = h * d;
-  if (n > 256) return fail(TSVD_ERR_INVALID, "merge: h*d = %d > 256", n);
-  if (nprob > W.nmax) return fail(TSVD_ERR_INVALID, "merge: too many parents");
-  TSVD_CUDA(cudaStreamSynchronize(st));
-  // per-parent concatenation buffers inside the z area (sized for both uses)
-  const int64_t RK = std::max<int64_t>(W.rows_max * kLp, (int64_t)W.sp * 256);
-  std::vector<const float *> ch((size_t)nprob * h);
-  std::vector<float *> m(nprob), lam(nprob), v(nprob), cs(nprob), out(nprob), sout(nprob);
+namespace {
+
+// The Rayleigh-Ritz end of a merge: for each problem, the n-column matrix
+// m[i] (|S| x n, ld n) -> Gram (compensated, fp64) -> Jacobi eigenpairs ->
+// out = m V_d diag(f(s)), sigma_out = s (the d largest singular values).
+tsvd_status merge_finish(FrpcaWork &W, const MergeProblem *probs, int nprob, int n, int nsrc,
+                         int root_mode, const std::vector<float *> &m, cudaStream_t st) {
+  const int d = W.d;
+  std::vector<float *> lam(nprob), v(nprob), cs(nprob), out(nprob), sout(nprob);
   std::vector<double *> g(nprob);
   std::vector<int32_t> rows(nprob, nsrc);
   for (int i = 0; i < nprob; ++i) {
-    for (int c = 0; c < h; ++c) ch[(size_t)i * h + c] = probs[i].children[c];
-    m[i] = W.z + i * RK;
     g[i] = W.g + (int64_t)i * 256 * 256;
     lam[i] = W.lambda + i * 256;
     v[i] = W.v + (int64_t)i * 256 * 256;
@@ -368,16 +370,14 @@ tsvd_status merge_batch(FrpcaWork &W, const MergeProblem *probs, int nprob, int 
     out[i] = probs[i].out;
     sout[i] = probs[i].sigma_out;
   }
+  TSVD_CUDA(cudaStreamSynchronize(st));  // the pointer staging area is reused
   PtrPack pk(W);
-  auto d_ch = pk.add(ch);
-  auto d_m = pk.add(m), d_lam = pk.add(lam), d_v = pk.add(v), d_cs = pk.add(cs),
-       d_out = pk.add(out), d_sout = pk.add(sout);
+  auto d_m = pk.add(m);
+  auto d_lam = pk.add(lam), d_v = pk.add(v), d_cs = pk.add(cs), d_out = pk.add(out),
+       d_sout = pk.add(sout);
   auto d_g = pk.add(g);
   const int32_t *d_rows = pk.add_int(rows);
   TSVD_TRY(pk.upload(st));
-  concat_kernel<<<dim3(grid_for((int64_t)nsrc * n, 256, 4), nprob), 256, 0, st>>>(d_ch, h, d, nsrc,
-                                                                                 d_m);
-  TSVD_LAUNCH_CHECK();
   TSVD_TRY(gram_batched((const float *const *)d_m, d_rows, nsrc, n, n, d_g, W.gram_work,
                         W.gram_bytes, nprob, st));
   TSVD_TRY(jacobi_eig_batched(d_g, n, d_lam, d_v, nprob, W.jac_work, W.jac_bytes, st,
@@ -389,6 +389,228 @@ tsvd_status merge_batch(FrpcaWork &W, const MergeProblem *probs, int nprob, int 
                                (const float *const *)d_v, n, n, d, (const float *const *)d_cs,
                                d_out, d, nullptr, nullptr, 1.f, nprob, st));
   return TSVD_OK;
+}
+
+__global__ void colnorm_kernel(const float *__restrict__ m, int64_t nsrc, int n,
+                               float *__restrict__ norm) {
+  const int prob = blockIdx.y;
+  const float *M = m + (int64_t)prob * nsrc * n;
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
+    float acc = 0.f;
+    for (int64_t s = 0; s < nsrc; ++s) acc = fmaf(M[s * n + c], M[s * n + c], acc);
+    norm[(int64_t)prob * n + c] = acc;
+  }
+}
+
+// V[i] (n x p, row-major) = the columns sel[i][0..p) of the n x n identity.
+__global__ void select_basis_kernel(const int32_t *__restrict__ sel, int n, int p,
+                                    float *__restrict__ v) {
+  const int prob = blockIdx.y;
+  float *V = v + (int64_t)prob * n * p;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < (int64_t)n * p;
+       i += (int64_t)gridDim.x * blockDim.x)
+    V[i] = 0.f;
+  __syncthreads();
+  if (blockIdx.x == 0)
+    for (int j = threadIdx.x; j < p; j += blockDim.x) V[(int64_t)sel[prob * p + j] * p + j] = 1.f;
+}
+
+__global__ void diag_sum_kernel(double *const *g, int l, double *out) {
+  const int prob = blockIdx.x;
+  double acc = 0.0;
+  for (int i = threadIdx.x; i < l; i += blockDim.x) acc += g[prob][(int64_t)i * l + i];
+  __shared__ double red[256];
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[prob] = red[0];
+}
+
+#define TSVD_BLAS(call)                                                        \
+  do {                                                                         \
+    cublasStatus_t s_ = (call);                                                \
+    if (s_ != CUBLAS_STATUS_SUCCESS)                                           \
+      return fail(TSVD_ERR_DEVICE, "cuBLAS status %d at %s:%d", (int)s_,       \
+                  __FILE__, __LINE__);                                         \
+  } while (0)
+
+// Buffers for up to `nprob` problems of n columns and W.sp rows.
+tsvd_status wide_reserve(FrpcaWork &W, int nprob, int n) {
+  const int nsrc = W.sp;
+  const size_t need = (size_t)nprob * nsrc * n;
+  if (!W.blas) {
+    cublasHandle_t h = nullptr;
+    TSVD_BLAS(cublasCreate(&h));
+    TSVD_BLAS(cublasSetMathMode(h, CUBLAS_PEDANTIC_MATH));  // fp32 products, no tf32
+    W.blas = h;
+  }
+  if (need <= W.wide_cap && nprob <= W.wide_nprob && n <= W.wide_n && W.wm) return TSVD_OK;
+  cudaFree(W.wm); cudaFree(W.wv); cudaFree(W.ww); cudaFree(W.wy); cudaFree(W.wy2);
+  cudaFree(W.wchol); cudaFree(W.wnorm);
+  W.wm = W.wv = W.ww = W.wy = W.wy2 = W.wnorm = nullptr;
+  W.wchol = nullptr;
+  W.wide_cap = 0;
+  TSVD_CUDA(cudaMalloc(&W.wm, need * sizeof(float)));
+  TSVD_CUDA(cudaMalloc(&W.wv, (size_t)nprob * n * 256 * sizeof(float)));
+  TSVD_CUDA(cudaMalloc(&W.ww, (size_t)nprob * n * 256 * sizeof(float)));
+  TSVD_CUDA(cudaMalloc(&W.wy, (size_t)nprob * nsrc * 256 * sizeof(float)));
+  TSVD_CUDA(cudaMalloc(&W.wy2, (size_t)nprob * nsrc * 256 * sizeof(float)));
+  TSVD_CUDA(cudaMalloc(&W.wchol, (size_t)nprob * 2 * 256 * 256 * sizeof(double)));
+  TSVD_CUDA(cudaMalloc(&W.wnorm, (size_t)nprob * n * sizeof(float)));
+  W.wide_cap = need;
+  W.wide_nprob = nprob;
+  W.wide_n = n;
+  return TSVD_OK;
+}
+
+// x[i] (rows x p, ld p) -> x[i] R^-1 into y[i], R from the compensated Gram;
+// energy (optional, host, nprob) receives trace(x^T x) = ||x||_F^2 per problem.
+tsvd_status orthonormalize(FrpcaWork &W, float *x, int64_t xstride, float *y, int rows, int p,
+                           int nprob, cudaStream_t st, double *energy) {
+  std::vector<float *> xs(nprob);
+  std::vector<double *> g(nprob);
+  std::vector<int32_t> rr(nprob, rows);
+  for (int i = 0; i < nprob; ++i) {
+    xs[i] = x + i * xstride;
+    g[i] = W.g + (int64_t)i * 256 * 256;
+  }
+  TSVD_CUDA(cudaStreamSynchronize(st));  // the pointer staging area is reused
+  PtrPack pk(W);
+  auto d_x = pk.add(xs);
+  auto d_g = pk.add(g);
+  const int32_t *d_rows = pk.add_int(rr);
+  TSVD_TRY(pk.upload(st));
+  TSVD_TRY(gram_batched((const float *const *)d_x, d_rows, rows, p, p, d_g, W.gram_work,
+                        W.gram_bytes, nprob, st));
+  if (energy) {
+    diag_sum_kernel<<<nprob, 256, 0, st>>>(d_g, p, W.sums);
+    TSVD_LAUNCH_CHECK();
+    TSVD_CUDA(cudaMemcpyAsync(energy, W.sums, sizeof(double) * nprob, cudaMemcpyDeviceToHost, st));
+  }
+  TSVD_TRY(chol_solve_wide_batched(d_g, W.wchol, x, y, rows, p, xstride, nprob, st));
+  TSVD_CUDA(cudaStreamSynchronize(st));
+  return TSVD_OK;
+}
+
+// Merge of h * d > 256 columns. The top-d singular triplets of M = [B_1..B_h]
+// (|S| x n) come from a p = min(256, n, |S|) dimensional basis V of M's
+// dominant right singular subspace, found by subspace iteration
+// (Y = M V, W = M^T Y, each product re-orthonormalized by CholeskyQR on a
+// compensated Gram), started from the p columns of M with the largest norms
+// and stopped when ||M V||_F^2 gains less than 1e-7 of itself. The result is
+// then the merge of the p columns of M V (compensated Gram + Jacobi), the
+// same arithmetic as a narrow merge. The products are plain fp32 GEMMs
+// (cuBLAS, pedantic math).
+tsvd_status merge_wide(FrpcaWork &W, const MergeProblem *probs, int nprob, int h, int nsrc,
+                       int root_mode, cudaStream_t st) {
+  const int d = W.d, n = h * d;
+  const int p = std::min(256, std::min(n, nsrc));
+  if (p < d) return fail(TSVD_ERR_INVALID, "merge: |S| = %d below rank d = %d", nsrc, d);
+  if (nsrc > W.sp) return fail(TSVD_ERR_INVALID, "merge: |S| = %d > %d", nsrc, W.sp);
+  TSVD_TRY(wide_reserve(W, std::max(nprob, W.nmax / h), n));
+  cublasHandle_t blas = (cublasHandle_t)W.blas;
+  TSVD_BLAS(cublasSetStream(blas, st));
+  const int64_t sm = (int64_t)nsrc * n, sv = (int64_t)n * p, sy = (int64_t)nsrc * p;
+  // M = [B_1 .. B_h], one |S| x n row-major matrix per problem
+  {
+    std::vector<const float *> ch((size_t)nprob * h);
+    std::vector<float *> m(nprob);
+    for (int i = 0; i < nprob; ++i) {
+      for (int c = 0; c < h; ++c) ch[(size_t)i * h + c] = probs[i].children[c];
+      m[i] = W.wm + i * sm;
+    }
+    TSVD_CUDA(cudaStreamSynchronize(st));
+    PtrPack pk(W);
+    auto d_ch = pk.add(ch);
+    auto d_m = pk.add(m);
+    TSVD_TRY(pk.upload(st));
+    concat_kernel<<<dim3(grid_for((int64_t)nsrc * n, 256, 4), nprob), 256, 0, st>>>(d_ch, h, d,
+                                                                                   nsrc, d_m);
+    TSVD_LAUNCH_CHECK();
+  }
+  // start: the p columns of M with the largest norms (the children's largest sigmas)
+  colnorm_kernel<<<dim3(ceil_div(n, 256), nprob), 256, 0, st>>>(W.wm, nsrc, n, W.wnorm);
+  TSVD_LAUNCH_CHECK();
+  std::vector<float> norms((size_t)nprob * n);
+  TSVD_CUDA(cudaMemcpyAsync(norms.data(), W.wnorm, sizeof(float) * norms.size(),
+                            cudaMemcpyDeviceToHost, st));
+  TSVD_CUDA(cudaStreamSynchronize(st));
+  std::vector<int32_t> sel((size_t)nprob * p);
+  for (int i = 0; i < nprob; ++i) {
+    std::vector<int32_t> idx(n);
+    for (int c = 0; c < n; ++c) idx[c] = c;
+    const float *nr = norms.data() + (size_t)i * n;
+    std::stable_sort(idx.begin(), idx.end(), [&](int32_t a, int32_t b) { return nr[a] > nr[b]; });
+    std::copy(idx.begin(), idx.begin() + p, sel.begin() + (size_t)i * p);
+  }
+  {
+    PtrPack pk(W);
+    const int32_t *d_sel = pk.add_int(sel);
+    TSVD_TRY(pk.upload(st));
+    select_basis_kernel<<<dim3(1, nprob), 256, 0, st>>>(d_sel, n, p, W.wv);
+    TSVD_LAUNCH_CHECK();
+    TSVD_CUDA(cudaStreamSynchronize(st));
+  }
+  const float one = 1.f, zero = 0.f;
+  std::vector<double> energy(nprob), prev(nprob, 0.0);
+  int it = 0;
+  for (; it < 40; ++it) {
+    // Y = M V: column-major, Y^T (p x |S|) = V^T (p x n) M^T (n x |S|)
+    TSVD_BLAS(cublasSgemmStridedBatched(blas, CUBLAS_OP_N, CUBLAS_OP_N, p, nsrc, n, &one, W.wv,
+                                        p, sv, W.wm, n, sm, &zero, W.wy, p, sy, nprob));
+    TSVD_TRY(orthonormalize(W, W.wy, sy, W.wy2, nsrc, p, nprob, st, energy.data()));
+    bool done = it > 0;
+    for (int i = 0; i < nprob; ++i)
+      if (!(energy[i] - prev[i] <= 1e-7 * energy[i])) done = false;
+    prev = energy;
+    if (done) break;
+    // W = M^T Yq: column-major, W^T (p x n) = Yq^T (p x |S|) M (|S| x n)
+    TSVD_BLAS(cublasSgemmStridedBatched(blas, CUBLAS_OP_N, CUBLAS_OP_T, p, n, nsrc, &one, W.wy2,
+                                        p, sy, W.wm, n, sm, &zero, W.ww, p, sv, nprob));
+    TSVD_TRY(orthonormalize(W, W.ww, sv, W.wv, n, p, nprob, st, nullptr));
+  }
+  W.wide_iters = it + 1;
+  // Rayleigh-Ritz: the narrow merge of the p columns of Z = M V
+  const int64_t RK = std::max<int64_t>(W.rows_max * kLp, (int64_t)W.sp * 256);
+  std::vector<float *> z(nprob);
+  for (int i = 0; i < nprob; ++i) z[i] = W.z + i * RK;
+  for (int i = 0; i < nprob; ++i)
+    TSVD_BLAS(cublasSgemm(blas, CUBLAS_OP_N, CUBLAS_OP_N, p, nsrc, n, &one, W.wv + i * sv, p,
+                          W.wm + i * sm, n, &zero, z[i], p));
+  return merge_finish(W, probs, nprob, p, nsrc, root_mode, z, st);
+}
+
+}  // namespace
+
+tsvd_status merge_batch(FrpcaWork &W, const MergeProblem *probs, int nprob, int h, int nsrc,
+                        int root_mode, cudaStream_t st) {
+  W.wide_iters = 0;
+  if (nprob == 0) return TSVD_OK;
+  const int d = W.d, n = h * d;
+  if (nprob > W.nmax) return fail(TSVD_ERR_INVALID, "merge: too many parents");
+  if (n > 256) return merge_wide(W, probs, nprob, h, nsrc, root_mode, st);
+  TSVD_CUDA(cudaStreamSynchronize(st));
+  // per-parent concatenation buffers inside the z area (sized for both uses)
+  const int64_t RK = std::max<int64_t>(W.rows_max * kLp, (int64_t)W.sp * 256);
+  std::vector<const float *> ch((size_t)nprob * h);
+  std::vector<float *> m(nprob);
+  for (int i = 0; i < nprob; ++i) {
+    for (int c = 0; c < h; ++c) ch[(size_t)i * h + c] = probs[i].children[c];
+    m[i] = W.z + i * RK;
+  }
+  {
+    PtrPack pk(W);
+    auto d_ch = pk.add(ch);
+    auto d_m = pk.add(m);
+    TSVD_TRY(pk.upload(st));
+    concat_kernel<<<dim3(grid_for((int64_t)nsrc * n, 256, 4), nprob), 256, 0, st>>>(d_ch, h, d,
+                                                                                   nsrc, d_m);
+    TSVD_LAUNCH_CHECK();
+  }
+  return merge_finish(W, probs, nprob, n, nsrc, root_mode, m, st);
 }
 
 tsvd_status lp_right_batch(FrpcaWork &W, const LpProblem *probs, int nprob, const float *u,

@@ -108,6 +108,12 @@ size_t gram_work_bytes(int max_rows, int l, int nprob);
 // CholeskyQR step: T[b] = R^{-1} from G[b] (upper triangular, l x kLp fp32).
 tsvd_status chol_inverse_batched(double *const *g, float *const *t, int l,
                                  int nprob, cudaStream_t st);
+// CholeskyQR step for l <= 256: factor G[b] = L L^T in fp64 (work: nprob x
+// (l*l + l) doubles), then y_b = x_b L^{-T} row by row (x, y: rows x l fp32,
+// ld l, problem b at offset b * stride). Directions whose pivot falls below
+// 1e-13 of the largest diagonal entry give zero columns.
+tsvd_status chol_solve_wide_batched(double *const *g, double *work, const float *x, float *y,
+                                    int rows, int l, int64_t stride, int nprob, cudaStream_t st);
 // Y[b] = X[b] * W[b] * diag(colscale[b]); writes fp32 (columns [n_out, ldy)
 // zeroed) and, when yhi/ylo are given, the fp16 split of Y * split_scale.
 tsvd_status apply_right_batched(const float *const *x, const int32_t *rows,

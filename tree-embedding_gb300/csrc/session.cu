@@ -218,6 +218,10 @@ extern "C" void tsvd_config_default(tsvd_config *c) {
 static tsvd_status session_alloc(tsvd_session *s) {
   const tsvd_config &c = s->cfg;
   TSVD_CUDA(cudaSetDevice(c.device));
+  // Launches are checked with cudaGetLastError: an error another component
+  // left in that slot (a library's handled failure, the caller's own code)
+  // must not be reported as ours.
+  cudaGetLastError();
   // The factor stream of a pipelined run gets the lowest priority: its
   // blocks fill the SMs the insert and push leave idle instead of delaying
   // the insert's short dependent kernels.
@@ -332,6 +336,7 @@ static void session_release(tsvd_session *s) {
       if (e) cudaEventDestroy(e);
   if (s->st) cudaStreamDestroy(s->st);
   if (s->st2) cudaStreamDestroy(s->st2);
+  cudaGetLastError();  // nothing from teardown may surface in a later launch check
 }
 
 extern "C" tsvd_status tsvd_session_create(const tsvd_config *cfg, tsvd_session **out) {
@@ -350,8 +355,8 @@ extern "C" tsvd_status tsvd_session_create(const tsvd_config *cfg, tsvd_session 
                 c.n_parts, c.hierarchy_n);
   if (c.rank_d < 1 || c.oversample < 0 || c.rank_d + c.oversample > kLp)
     return fail(TSVD_ERR_INVALID, "rank_d + oversample must be <= %d", kLp);
-  if ((int64_t)c.hierarchy_n * c.rank_d > 256)
-    return fail(TSVD_ERR_INVALID, "hierarchy_n * rank_d must be <= 256 (merge width)");
+  if (c.hierarchy_n > 16 || (int64_t)c.hierarchy_n * c.rank_d > 2048)
+    return fail(TSVD_ERR_INVALID, "need hierarchy_n <= 16 and hierarchy_n * rank_d <= 2048");
   if (c.passes_q < 1) return fail(TSVD_ERR_INVALID, "passes_q must be >= 1");
   if (c.transform < 0 || c.transform > 2 || c.dirty_rule < 0 || c.dirty_rule > 2)
     return fail(TSVD_ERR_INVALID, "bad transform or dirty rule");
@@ -621,6 +626,7 @@ static tsvd_status stage_merge(tsvd_session *s, FactorJob &job, cudaStream_t st)
     if (root) mode = s->cfg.root_scaling == TSVD_ROOT_U ? 2 : 1;
     TSVD_TRY(merge_batch(s->fw, probs.data(), (int)probs.size(), h, s->S, mode, st));
     job.stats.eig_sweeps_merge = std::max(job.stats.eig_sweeps_merge, s->fw.last_sweeps);
+    job.stats.merge_subspace_iters = std::max(job.stats.merge_subspace_iters, s->fw.wide_iters);
     job.stats.merged_nodes += (int)probs.size();
     if (root) {
       TSVD_CUDA(cudaMemcpyAsync(s->node_b(0), s->embedding, sizeof(float) * s->node_elems(),
@@ -767,6 +773,7 @@ static void finish_stats(tsvd_step_stats &st, cudaEvent_t *ea, cudaEvent_t *eb) 
 
 static tsvd_status step_device(tsvd_session *s, const int32_t *edges, bool on_device, int64_t m) {
   TSVD_CUDA(cudaSetDevice(s->cfg.device));
+  cudaGetLastError();  // not ours: see session_alloc
   bool skipped = false;
   TSVD_TRY(stage_front(s, edges, on_device, m, s->ev, &skipped));
   if (skipped) return TSVD_OK;
@@ -839,6 +846,7 @@ static tsvd_status run_snapshots(tsvd_session *s, const int32_t *edges, bool on_
                                  const int64_t *offsets, int32_t count, double *emb_out,
                                  tsvd_step_stats *stats_out) {
   TSVD_CUDA(cudaSetDevice(s->cfg.device));
+  cudaGetLastError();  // not ours: see session_alloc
   int64_t max_m = 0;
   for (int k = 0; k < count; ++k) {
     const int64_t m = offsets[k + 1] - offsets[k];
