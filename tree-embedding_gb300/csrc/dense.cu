@@ -596,14 +596,23 @@ struct JacobiArgs {
   float2 *log;        // [prob][JAC_MAX_SWEEPS][np-1][np/2]
   int32_t *sweeps;    // [prob]
   int32_t *rank;      // [prob][n]
+  int refine;         // 1: g is nearly diagonal (see jacobi_kernel)
+  const float *const *vinit;  // replay starts from these rows (null: identity)
 };
 
+// Refinement mode (a.refine): g = V^T G V for approximate eigenvectors V, so
+// its off-diagonal part is small. The diagonal is kept as an fp64 base
+// (dbase, fixed) plus an fp32 correction in the packed matrix, so the small
+// eigenvalues keep their relative accuracy: the rotation angle uses
+// (dbase_q - dbase_p) rounded once, and the updates only move the corrections.
 __global__ void __launch_bounds__(JAC_THREADS) jacobi_kernel(JacobiArgs a) {
   extern __shared__ __align__(16) float G[];  // packed upper triangle
   __shared__ float pc[128], ps[128], pt[128];
   __shared__ int pp[128], pq[128];
   __shared__ int rotated;
   __shared__ float dmax;
+  __shared__ double dbase[256];
+  const bool refine = a.refine != 0;
   const int n = a.n, np = n + (n & 1), P = np / 2;
   const int R = (P + 1) / 2;               // block-row groups
   const int Gs = (int)blockDim.x / R;      // threads per group (P <= 128: >= 16)
@@ -612,8 +621,9 @@ __global__ void __launch_bounds__(JAC_THREADS) jacobi_kernel(JacobiArgs a) {
   const double *Gin = a.g[prob];
   for (int idx = threadIdx.x; idx < n * n; idx += blockDim.x) {
     int i = idx / n, j = idx % n;
-    if (i <= j) G[packed(i, j)] = (float)Gin[idx];
+    if (i <= j) G[packed(i, j)] = (refine && i == j) ? 0.f : (float)Gin[idx];
   }
+  for (int i = threadIdx.x; i < n; i += blockDim.x) dbase[i] = refine ? Gin[(int64_t)i * n + i] : 0.0;
   float2 *log = a.log + (int64_t)prob * JAC_MAX_SWEEPS * (np - 1) * P;
   __syncthreads();
   int sweep = 0;
@@ -621,14 +631,16 @@ __global__ void __launch_bounds__(JAC_THREADS) jacobi_kernel(JacobiArgs a) {
     if (threadIdx.x == 0) {
       rotated = 0;
       float m = 0.f;
-      for (int i = 0; i < n; ++i) m = fmaxf(m, fabsf(G[packed(i, i)]));
+      for (int i = 0; i < n; ++i)
+        m = fmaxf(m, fabsf((float)(dbase[i] + (double)G[packed(i, i)])));
       dmax = m;
     }
     __syncthreads();
     // Rotate when the pair is coupled beyond fp32 rounding: relative to the
     // pair (Demmel-Veselic) and above the absolute noise floor eps * max|a_ii|
-    // that fp32 updates leave on every off-diagonal entry.
-    const float floor_abs = 2e-7f * dmax;
+    // that fp32 updates leave on every off-diagonal entry. In refinement mode
+    // the off-diagonal entries carry no such noise: only the relative test.
+    const float floor_abs = (refine ? 1e-14f : 2e-7f) * dmax;
     for (int t = 0; t < np - 1; ++t) {
       if (threadIdx.x < P) {
         const int k = threadIdx.x;
@@ -636,9 +648,11 @@ __global__ void __launch_bounds__(JAC_THREADS) jacobi_kernel(JacobiArgs a) {
         int p = min(x, y), q = max(x, y);
         float c = 1.f, s = 0.f, tt = 0.f;
         if (q < n) {
-          float app = G[packed(p, p)], aqq = G[packed(q, q)], apq = G[packed(p, q)];
+          const float cp = G[packed(p, p)], cq = G[packed(q, q)], apq = G[packed(p, q)];
+          const float app = (float)(dbase[p] + (double)cp), aqq = (float)(dbase[q] + (double)cq);
           if (fabsf(apq) > floor_abs && fabsf(apq) > 1e-7f * sqrtf(fabsf(app) * fabsf(aqq))) {
-            float tau = (aqq - app) / (2.f * apq);
+            const float diff = refine ? (float)(dbase[q] - dbase[p]) + (cq - cp) : aqq - app;
+            float tau = diff / (2.f * apq);
             float sg = tau >= 0.f ? 1.f : -1.f;
             tt = sg / (fabsf(tau) + sqrtf(1.f + tau * tau));
             c = rsqrtf(1.f + tt * tt);
@@ -700,14 +714,14 @@ __global__ void __launch_bounds__(JAC_THREADS) jacobi_kernel(JacobiArgs a) {
   // eigenvalues and their descending rank
   float *lam = a.lambda[prob];
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
-    float li = G[packed(i, i)];
+    const double li = dbase[i] + (double)G[packed(i, i)];
     int r = 0;
     for (int j = 0; j < n; ++j) {
-      float lj = G[packed(j, j)];
+      const double lj = dbase[j] + (double)G[packed(j, j)];
       r += (lj > li) || (lj == li && j < i);
     }
     a.rank[prob * n + i] = r;
-    lam[r] = li;
+    lam[r] = (float)li;
   }
 }
 
@@ -730,9 +744,10 @@ __global__ void __launch_bounds__(256) jacobi_replay_kernel(JacobiArgs a, float 
   const int nr = min(REPLAY_ROWS, n - r0);
   if (nr <= 0) return;
   float2 *lb = reinterpret_cast<float2 *>(sv + ((REPLAY_ROWS * n + 1) & ~1));
+  const float *vin = a.vinit ? a.vinit[prob] : nullptr;
   for (int i = threadIdx.x; i < REPLAY_ROWS * n; i += blockDim.x) {
     int rr = i / n, cc = i % n;
-    sv[i] = (rr < nr && r0 + rr == cc) ? 1.f : 0.f;
+    sv[i] = rr >= nr ? 0.f : vin ? vin[(int64_t)(r0 + rr) * n + cc] : (r0 + rr == cc ? 1.f : 0.f);
   }
   const float2 *log = a.log + (int64_t)prob * JAC_MAX_SWEEPS * (np - 1) * P;
   const int rounds = a.sweeps[prob] * (np - 1);
@@ -965,6 +980,110 @@ __global__ void trsm_rows_kernel(const float *__restrict__ x, float *__restrict_
   }
 }
 
+// Shifted Cholesky in fp32 for the basis of a subspace iteration: K + s I =
+// L L^T with s = shift * trace(K) / l, so no direction is dropped and the
+// result R^{-1} = L^{-T} makes a well-conditioned (not exactly orthonormal)
+// basis. One block per problem, packed lower triangle in shared memory; L
+// goes out packed (row i at i(i+1)/2). K: l x l fp32, problem b at b * l * l.
+__global__ void __launch_bounds__(1024) chol_shift_kernel(const float *__restrict__ K,
+                                                          float *__restrict__ Lout, int l,
+                                                          float shift) {
+  extern __shared__ float Lp[];  // l (l + 1) / 2
+  __shared__ float tr;
+  const float *Kb = K + (int64_t)blockIdx.x * l * l;
+  float *Lb = Lout + (int64_t)blockIdx.x * l * (l + 1) / 2;
+  for (int t = threadIdx.x; t < l * (l + 1) / 2; t += blockDim.x) {
+    int i = (int)((sqrtf(8.f * t + 1.f) - 1.f) * 0.5f);
+    while ((i + 1) * (i + 2) / 2 <= t) ++i;
+    while (i * (i + 1) / 2 > t) --i;
+    const int j = t - i * (i + 1) / 2;
+    Lp[t] = Kb[(int64_t)i * l + j];
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float acc = 0.f;
+    for (int i = 0; i < l; ++i) acc += Lp[i * (i + 1) / 2 + i];
+    tr = fmaxf(acc, FLT_MIN) * shift / (float)l;
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < l; i += blockDim.x) Lp[i * (i + 1) / 2 + i] += tr;
+  __syncthreads();
+  for (int k = 0; k < l; ++k) {
+    const int kk = k * (k + 1) / 2 + k;
+    if (threadIdx.x == 0) Lp[kk] = sqrtf(fmaxf(Lp[kk], tr));
+    __syncthreads();
+    const float piv = Lp[kk];
+    for (int i = k + 1 + threadIdx.x; i < l; i += blockDim.x) Lp[i * (i + 1) / 2 + k] /= piv;
+    __syncthreads();
+    const int n = l - k - 1;
+    for (int t = threadIdx.x; t < n * n; t += blockDim.x) {
+      const int i = k + 1 + t / n, j = k + 1 + t % n;
+      if (j <= i) Lp[i * (i + 1) / 2 + j] -= Lp[i * (i + 1) / 2 + k] * Lp[j * (j + 1) / 2 + k];
+    }
+    __syncthreads();
+  }
+  for (int t = threadIdx.x; t < l * (l + 1) / 2; t += blockDim.x) Lb[t] = Lp[t];
+}
+
+// y = x L^{-T}, one warp per row: y_j = (x_j - sum_{k<j} y_k L[j][k]) / L[j][j]
+// with the dot product split over the lanes; L packed in shared memory, the
+// row's y in the warp's shared slice. x, y: rows x l, problem b at b * stride.
+__global__ void __launch_bounds__(1024) trsm_warp_kernel(const float *__restrict__ x,
+                                                         float *__restrict__ y,
+                                                         const float *__restrict__ Lpk, int rows,
+                                                         int l, int64_t stride) {
+  extern __shared__ float sm[];
+  float *Lp = sm;                                   // l (l + 1) / 2
+  float *ys = sm + ((l * (l + 1) / 2 + 3) & ~3);    // [warps][l]
+  const int prob = blockIdx.y;
+  const float *Lb = Lpk + (int64_t)prob * l * (l + 1) / 2;
+  for (int t = threadIdx.x; t < l * (l + 1) / 2; t += blockDim.x) Lp[t] = Lb[t];
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  float *yw = ys + warp * l;
+  for (int r = blockIdx.x * nwarps + warp; r < rows; r += gridDim.x * nwarps) {
+    const float *xr = x + prob * stride + (int64_t)r * l;
+    float *yr = y + prob * stride + (int64_t)r * l;
+    for (int j = 0; j < l; ++j) {
+      const float *Lj = Lp + j * (j + 1) / 2;
+      float part = 0.f;
+      for (int k = lane; k < j; k += 32) part = fmaf(yw[k], Lj[k], part);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(kFull, part, o);
+      const float v = (xr[j] - part) / Lj[j];
+      if (lane == 0) yw[j] = v;
+      __syncwarp();
+    }
+    for (int j = lane; j < l; j += 32) yr[j] = yw[j];
+    __syncwarp();
+  }
+}
+
+tsvd_status chol_shift_solve_batched(const float *K, float *Lpk, const float *x, float *y,
+                                     int rows, int l, int64_t stride, float shift, int nprob,
+                                     cudaStream_t st) {
+  if (nprob == 0) return TSVD_OK;
+  if (l > 256 || l < 1) return fail(TSVD_ERR_INVALID, "chol shift: l=%d", l);
+  const size_t csm = (size_t)l * (l + 1) / 2 * sizeof(float);
+  const size_t tsm = (((size_t)l * (l + 1) / 2 + 3) & ~(size_t)3) * sizeof(float) +
+                     (size_t)32 * l * sizeof(float);
+  static size_t ccur = 0, tcur = 0;
+  if (csm > 48 * 1024 && csm > ccur) {
+    TSVD_TRY(set_smem((const void *)chol_shift_kernel, csm));
+    ccur = csm;
+  }
+  if (tsm > 48 * 1024 && tsm > tcur) {
+    TSVD_TRY(set_smem((const void *)trsm_warp_kernel, tsm));
+    tcur = tsm;
+  }
+  chol_shift_kernel<<<nprob, 1024, csm, st>>>(K, Lpk, l, shift);
+  TSVD_LAUNCH_CHECK();
+  const int blocks = (int)std::min<int64_t>(ceil_div(rows, 32), 2 * sm_count() / std::max(nprob, 1) + 1);
+  trsm_warp_kernel<<<dim3(blocks, nprob), 1024, tsm, st>>>(x, y, Lpk, rows, l, stride);
+  TSVD_LAUNCH_CHECK();
+  return TSVD_OK;
+}
+
 tsvd_status chol_solve_wide_batched(double *const *g, double *work, const float *x, float *y,
                                     int rows, int l, int64_t stride, int nprob, cudaStream_t st) {
   if (nprob == 0) return TSVD_OK;
@@ -1006,7 +1125,7 @@ size_t jacobi_work_bytes(int n, int nprob) {
 
 tsvd_status jacobi_eig_batched(double *const *g, int n, float *const *lambda, float *const *v,
                                int nprob, void *work, size_t work_bytes, cudaStream_t st,
-                               int *sweeps_out) {
+                               int *sweeps_out, int refine, const float *const *vinit) {
   if (nprob == 0) return TSVD_OK;
   if (n > 256 || n < 2) return fail(TSVD_ERR_INVALID, "jacobi: n=%d", n);
   if (jacobi_work_bytes(n, nprob) > work_bytes) return fail(TSVD_ERR_INVALID, "jacobi: work");
@@ -1021,6 +1140,8 @@ tsvd_status jacobi_eig_batched(double *const *g, int n, float *const *lambda, fl
   a.sweeps = (int32_t *)w;
   w += round_up((size_t)nprob * sizeof(int32_t), 256);
   a.rank = (int32_t *)w;
+  a.refine = refine;
+  a.vinit = vinit;
   const int P = np / 2;
   size_t smem = (size_t)n * (n + 1) / 2 * sizeof(float);
   static size_t cur = 0;

@@ -214,6 +214,14 @@ tsvd_status frpca_work_alloc(FrpcaWork &W, int nmax, int64_t rows_max, int sp, i
   TSVD_CUDA(cudaMallocHost(&W.hptr, W.ptr_slots * sizeof(void *)));
   TSVD_CUDA(cudaMalloc(&W.dint, W.ptr_slots * sizeof(int32_t)));
   TSVD_CUDA(cudaMallocHost(&W.hint, W.ptr_slots * sizeof(int32_t)));
+  for (double **p : {&W.dv, &W.dt, &W.dh})
+    TSVD_CUDA(cudaMalloc(p, (size_t)nmax * 256 * 256 * sizeof(double)));
+  {
+    std::vector<double *> hp(nmax);
+    for (int i = 0; i < nmax; ++i) hp[i] = W.dh + (int64_t)i * 256 * 256;
+    TSVD_CUDA(cudaMalloc(&W.dh_ptrs, sizeof(double *) * nmax));
+    TSVD_CUDA(cudaMemcpy(W.dh_ptrs, hp.data(), sizeof(double *) * nmax, cudaMemcpyHostToDevice));
+  }
   return TSVD_OK;
 }
 
@@ -223,10 +231,84 @@ void frpca_work_free(FrpcaWork &W) {
   cudaFree(W.colscale); cudaFree(W.sums); cudaFree(W.gram_work); cudaFree(W.jac_work); cudaFree(W.dptr);
   cudaFreeHost(W.hptr); cudaFree(W.dint); cudaFreeHost(W.hint);
   cudaFree(W.wm); cudaFree(W.wv); cudaFree(W.ww); cudaFree(W.wy); cudaFree(W.wy2);
-  cudaFree(W.wchol); cudaFree(W.wnorm);
+  cudaFree(W.wchol); cudaFree(W.wnorm); cudaFree(W.wk);
+  cudaFree(W.dv); cudaFree(W.dt); cudaFree(W.dh); cudaFree(W.dh_ptrs);
   if (W.blas) cublasDestroy((cublasHandle_t)W.blas);
   cudaGetLastError();  // the launch checks read this slot: leave nothing from teardown in it
   W = FrpcaWork();
+}
+
+#define TSVD_BLAS(call)                                                        \
+  do {                                                                         \
+    cublasStatus_t s_ = (call);                                                \
+    if (s_ != CUBLAS_STATUS_SUCCESS)                                           \
+      return fail(TSVD_ERR_DEVICE, "cuBLAS status %d at %s:%d", (int)s_,       \
+                  __FILE__, __LINE__);                                         \
+  } while (0)
+
+namespace {
+
+__global__ void widen_kernel(const float *__restrict__ v, double *__restrict__ out, int64_t count,
+                             int64_t stride_in, int64_t stride_out) {
+  const int prob = blockIdx.y;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < count;
+       i += (int64_t)gridDim.x * blockDim.x)
+    out[prob * stride_out + i] = v[prob * stride_in + i];
+}
+
+// C = op(A) B for n x n row-major fp64 matrices, problem z at offset z * S;
+// op(A) = A (trans_a 0) or A^T (1). 16 x 16 output tiles, k staged in shared
+// memory.
+__global__ void __launch_bounds__(256) dgemm_small_kernel(const double *__restrict__ A,
+                                                          const double *__restrict__ B,
+                                                          double *__restrict__ C, int n, int64_t S,
+                                                          int trans_a) {
+  __shared__ double sa[16][17], sb[16][17];
+  const int z = blockIdx.z, ty = threadIdx.x / 16, tx = threadIdx.x % 16;
+  const int i = blockIdx.y * 16 + ty, j = blockIdx.x * 16 + tx;
+  const double *Az = A + z * S, *Bz = B + z * S;
+  double acc = 0.0;
+  for (int k0 = 0; k0 < n; k0 += 16) {
+    const int ka = k0 + tx, kb = k0 + ty;
+    // sa[ty][tx] = op(A)[i][k0 + tx]
+    sa[ty][tx] = (i < n && ka < n) ? (trans_a ? Az[(int64_t)ka * n + i] : Az[(int64_t)i * n + ka])
+                                   : 0.0;
+    sb[ty][tx] = (kb < n && j < n) ? Bz[(int64_t)kb * n + j] : 0.0;
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < 16; ++k) acc = fma(sa[ty][k], sb[k][tx], acc);
+    __syncthreads();
+  }
+  if (i < n && j < n) C[z * S + (int64_t)i * n + j] = acc;
+}
+
+}  // namespace
+
+// Eigenpairs of the Grams G[i] = W.g + i 256^2 (n x n fp64) to the accuracy
+// the fp64 Gram carries. The fp32 Jacobi's absolute error, a few eps_32 times
+// the largest eigenvalue, is a large relative error on the small ones (the
+// Gram squares the spread of the singular values), so its eigenvectors V
+// (W.v) are refined: H = V^T G V in fp64 (nearly diagonal), a Jacobi on H
+// that carries the diagonal in fp64, its rotations replayed onto V. lam / v:
+// pointer arrays to W.lambda / W.v of each problem.
+tsvd_status eig_refined(FrpcaWork &W, double *const *d_g, int n, float *const *d_lam,
+                        float *const *d_v, int nprob, cudaStream_t st) {
+  TSVD_TRY(jacobi_eig_batched(d_g, n, d_lam, d_v, nprob, W.jac_work, W.jac_bytes, st,
+                              &W.last_sweeps));
+  const int64_t S = 256 * 256;
+  widen_kernel<<<dim3(grid_for((int64_t)n * n, 256, 1), nprob), 256, 0, st>>>(W.v, W.dv,
+                                                                            (int64_t)n * n, S, S);
+  TSVD_LAUNCH_CHECK();
+  // T = G V, H = V^T T (fp64)
+  const dim3 grid(ceil_div(n, 16), ceil_div(n, 16), nprob);
+  dgemm_small_kernel<<<grid, 256, 0, st>>>(W.g, W.dv, W.dt, n, S, 0);
+  TSVD_LAUNCH_CHECK();
+  dgemm_small_kernel<<<grid, 256, 0, st>>>(W.dv, W.dt, W.dh, n, S, 1);
+  TSVD_LAUNCH_CHECK();
+  // the rotations are replayed onto V in place (each replay block reads its
+  // rows before writing them)
+  return jacobi_eig_batched(W.dh_ptrs, n, d_lam, d_v, nprob, W.jac_work, W.jac_bytes, st,
+                            &W.last_refine_sweeps, 1, (const float *const *)d_v);
 }
 
 tsvd_status frpca_batch(FrpcaWork &W, const FrpcaProblem *probs, int nprob, int q, uint64_t seed,
@@ -323,8 +405,7 @@ tsvd_status frpca_batch(FrpcaWork &W, const FrpcaProblem *probs, int nprob, int 
   // eigSVD of Z = A^T Q (frpca.c:99-136): Gram, eigenpairs, top-d.
   TSVD_TRY(gram_batched((const float *const *)d_z, d_nc, max_nc, l, kLp, d_g, W.gram_work,
                         W.gram_bytes, nprob, st));
-  TSVD_TRY(jacobi_eig_batched(d_g, l, d_lam, d_v, nprob, W.jac_work, W.jac_bytes, st,
-                              &W.last_sweeps));
+  TSVD_TRY(eig_refined(W, d_g, l, d_lam, d_v, nprob, st));
   double *d_sum2 = W.sums;
   sigma_kernel<<<nprob, 128, 0, st>>>((const float *const *)d_lam, d, d_cs, d_csi, d_sout, d_sum2);
   TSVD_LAUNCH_CHECK();
@@ -380,8 +461,7 @@ tsvd_status merge_finish(FrpcaWork &W, const MergeProblem *probs, int nprob, int
   TSVD_TRY(pk.upload(st));
   TSVD_TRY(gram_batched((const float *const *)d_m, d_rows, nsrc, n, n, d_g, W.gram_work,
                         W.gram_bytes, nprob, st));
-  TSVD_TRY(jacobi_eig_batched(d_g, n, d_lam, d_v, nprob, W.jac_work, W.jac_bytes, st,
-                              &W.last_sweeps));
+  TSVD_TRY(eig_refined(W, d_g, n, d_lam, d_v, nprob, st));
   merge_scale_kernel<<<nprob, 128, 0, st>>>((const float *const *)d_lam, d, root_mode, d_cs,
                                             d_sout);
   TSVD_LAUNCH_CHECK();
@@ -429,13 +509,8 @@ __global__ void diag_sum_kernel(double *const *g, int l, double *out) {
   if (threadIdx.x == 0) out[prob] = red[0];
 }
 
-#define TSVD_BLAS(call)                                                        \
-  do {                                                                         \
-    cublasStatus_t s_ = (call);                                                \
-    if (s_ != CUBLAS_STATUS_SUCCESS)                                           \
-      return fail(TSVD_ERR_DEVICE, "cuBLAS status %d at %s:%d", (int)s_,       \
-                  __FILE__, __LINE__);                                         \
-  } while (0)
+
+constexpr int64_t kWideK = 256 * 256 + 256 * 257 / 2;  // fp32 Gram + packed factor
 
 // Buffers for up to `nprob` problems of n columns and W.sp rows.
 tsvd_status wide_reserve(FrpcaWork &W, int nprob, int n) {
@@ -444,13 +519,13 @@ tsvd_status wide_reserve(FrpcaWork &W, int nprob, int n) {
   if (!W.blas) {
     cublasHandle_t h = nullptr;
     TSVD_BLAS(cublasCreate(&h));
-    TSVD_BLAS(cublasSetMathMode(h, CUBLAS_PEDANTIC_MATH));  // fp32 products, no tf32
     W.blas = h;
+    TSVD_BLAS(cublasSetMathMode(h, CUBLAS_PEDANTIC_MATH));  // fp32 products, no tf32
   }
   if (need <= W.wide_cap && nprob <= W.wide_nprob && n <= W.wide_n && W.wm) return TSVD_OK;
   cudaFree(W.wm); cudaFree(W.wv); cudaFree(W.ww); cudaFree(W.wy); cudaFree(W.wy2);
-  cudaFree(W.wchol); cudaFree(W.wnorm);
-  W.wm = W.wv = W.ww = W.wy = W.wy2 = W.wnorm = nullptr;
+  cudaFree(W.wchol); cudaFree(W.wnorm); cudaFree(W.wk);
+  W.wm = W.wv = W.ww = W.wy = W.wy2 = W.wnorm = W.wk = nullptr;
   W.wchol = nullptr;
   W.wide_cap = 0;
   TSVD_CUDA(cudaMalloc(&W.wm, need * sizeof(float)));
@@ -460,6 +535,7 @@ tsvd_status wide_reserve(FrpcaWork &W, int nprob, int n) {
   TSVD_CUDA(cudaMalloc(&W.wy2, (size_t)nprob * nsrc * 256 * sizeof(float)));
   TSVD_CUDA(cudaMalloc(&W.wchol, (size_t)nprob * 2 * 256 * 256 * sizeof(double)));
   TSVD_CUDA(cudaMalloc(&W.wnorm, (size_t)nprob * n * sizeof(float)));
+  TSVD_CUDA(cudaMalloc(&W.wk, (size_t)nprob * kWideK * sizeof(float)));
   W.wide_cap = need;
   W.wide_nprob = nprob;
   W.wide_n = n;
@@ -556,22 +632,48 @@ tsvd_status merge_wide(FrpcaWork &W, const MergeProblem *probs, int nprob, int h
   }
   const float one = 1.f, zero = 0.f;
   std::vector<double> energy(nprob), prev(nprob, 0.0);
+  // x (rows x p, row-major, problem stride xs) -> y: fp32 Gram (cuBLAS; problem
+  // i at W.wk + i p p), shifted fp32 Cholesky (packed factors after all the
+  // Grams), triangular solve.
+  const int64_t kp = (int64_t)p * p;
+  auto cheap_basis = [&](const float *x, int64_t xs, float *y, int rows) -> tsvd_status {
+    // K = x^T x: column-major K (p x p) = (x^T) (x^T)^T with x^T (p x rows, ld p)
+    TSVD_BLAS(cublasSgemmStridedBatched(blas, CUBLAS_OP_N, CUBLAS_OP_T, p, p, rows, &one, x, p,
+                                        xs, x, p, xs, &zero, W.wk, p, kp, nprob));
+    TSVD_TRY(chol_shift_solve_batched(W.wk, W.wk + nprob * kp, x, y, rows, p, xs, 1e-6f, nprob,
+                                      st));
+    return TSVD_OK;
+  };
   int it = 0;
   for (; it < 40; ++it) {
     // Y = M V: column-major, Y^T (p x |S|) = V^T (p x n) M^T (n x |S|)
     TSVD_BLAS(cublasSgemmStridedBatched(blas, CUBLAS_OP_N, CUBLAS_OP_N, p, nsrc, n, &one, W.wv,
                                         p, sv, W.wm, n, sm, &zero, W.wy, p, sy, nprob));
-    TSVD_TRY(orthonormalize(W, W.wy, sy, W.wy2, nsrc, p, nprob, st, energy.data()));
-    bool done = it > 0;
+    TSVD_TRY(cheap_basis(W.wy, sy, W.wy2, nsrc));
+    // ||M V||_F^2 = trace(Y^T Y), from the diagonal of the Gram just formed
+    std::vector<float> diag((size_t)nprob * p);
     for (int i = 0; i < nprob; ++i)
-      if (!(energy[i] - prev[i] <= 1e-7 * energy[i])) done = false;
+      TSVD_CUDA(cudaMemcpy2DAsync(diag.data() + (size_t)i * p, sizeof(float),
+                                  W.wk + i * kp, (p + 1) * sizeof(float), sizeof(float), p,
+                                  cudaMemcpyDeviceToHost, st));
+    TSVD_CUDA(cudaStreamSynchronize(st));
+    bool done = it > 0;
+    for (int i = 0; i < nprob; ++i) {
+      double e = 0.0;
+      for (int j = 0; j < p; ++j) e += diag[(size_t)i * p + j];
+      energy[i] = e;
+      if (!(energy[i] - prev[i] <= 1e-6 * energy[i])) done = false;
+    }
     prev = energy;
     if (done) break;
     // W = M^T Yq: column-major, W^T (p x n) = Yq^T (p x |S|) M (|S| x n)
     TSVD_BLAS(cublasSgemmStridedBatched(blas, CUBLAS_OP_N, CUBLAS_OP_T, p, n, nsrc, &one, W.wy2,
                                         p, sy, W.wm, n, sm, &zero, W.ww, p, sv, nprob));
-    TSVD_TRY(orthonormalize(W, W.ww, sv, W.wv, n, p, nprob, st, nullptr));
+    TSVD_TRY(cheap_basis(W.ww, sv, W.wv, n));
   }
+  // one accurate CholeskyQR pass: an orthonormal V to working precision
+  TSVD_CUDA(cudaMemcpyAsync(W.ww, W.wv, sizeof(float) * nprob * sv, cudaMemcpyDeviceToDevice, st));
+  TSVD_TRY(orthonormalize(W, W.ww, sv, W.wv, n, p, nprob, st, nullptr));
   W.wide_iters = it + 1;
   // Rayleigh-Ritz: the narrow merge of the p columns of Z = M V
   const int64_t RK = std::max<int64_t>(W.rows_max * kLp, (int64_t)W.sp * 256);

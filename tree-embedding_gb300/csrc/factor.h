@@ -28,14 +28,18 @@ struct FrpcaWork {
   int32_t *dint = nullptr; // device int area (row counts, block ids)
   int32_t *hint = nullptr;
   int last_sweeps = 0;
-  // merges wider than 256 columns (allocated on first use)
   void *blas = nullptr;     // cublasHandle_t
+  double *dv = nullptr, *dt = nullptr, *dh = nullptr;  // [nmax][256*256] eigen refinement
+  double **dh_ptrs = nullptr;  // device: dh + i 256^2 for each problem i
+  int last_refine_sweeps = 0;
+  // merges wider than 256 columns (allocated on first use)
   float *wm = nullptr;      // [nprob][|S|][n] the concatenated children
   float *wv = nullptr;      // [nprob][n][256] basis of the right singular subspace
   float *ww = nullptr;      // [nprob][n][256] M^T Y before normalization
   float *wy = nullptr;      // [nprob][|S|][256] M V, then its orthonormal basis
   float *wy2 = nullptr;
   double *wchol = nullptr;  // [nprob][2][256][256] Cholesky factors
+  float *wk = nullptr;      // [nprob][256*256 + 256*257/2] fp32 Gram + packed factor
   float *wnorm = nullptr;   // [nprob][n] column norms of M
   size_t wide_cap = 0;      // problems x n x |S| the buffers hold
   int wide_nprob = 0, wide_n = 0;

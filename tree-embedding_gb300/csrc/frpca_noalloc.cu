@@ -64,6 +64,8 @@ constexpr size_t kUB = al((size_t)kNaMaxRows * kNaMaxK * 4);
 constexpr size_t kVoutB = al((size_t)kNaMaxUsedCols * kNaMaxK * 4);
 constexpr size_t kSigB = al(kNaMaxK * 4);
 constexpr size_t kMiscB = al(16);
+constexpr size_t kRefB = al((size_t)kNaMaxL * kNaMaxL * 8);  // eigen refinement (fp64)
+constexpr size_t kHpB = al(8);                                // device pointer to dh
 
 constexpr size_t kOffAt = 0;
 constexpr size_t kOffXhi = kOffAt + kAtB;
@@ -91,7 +93,11 @@ constexpr size_t kOffU = kOffCmap + kCmapB;
 constexpr size_t kOffVout = kOffU + kUB;
 constexpr size_t kOffSig = kOffVout + kVoutB;
 constexpr size_t kOffMisc = kOffSig + kSigB;
-constexpr size_t kNoallocScratchBytes = kOffMisc + kMiscB;
+constexpr size_t kOffDv = kOffMisc + kMiscB;
+constexpr size_t kOffDt = kOffDv + kRefB;
+constexpr size_t kOffDh = kOffDt + kRefB;
+constexpr size_t kOffHp = kOffDh + kRefB;
+constexpr size_t kNoallocScratchBytes = kOffHp + kHpB;
 
 __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocScratchBytes];
 
@@ -182,6 +188,9 @@ tsvd_status scratch_for_current_device(unsigned char **out) {
     if (e != cudaSuccess || !p)
       return fail(TSVD_ERR_DEVICE, "cudaGetSymbolAddress(g_noalloc_scratch): %s",
                   cudaGetErrorString(e));
+    // the refinement's pointer array (one problem) never changes: set it now
+    double *dh = (double *)((unsigned char *)p + kOffDh);
+    TSVD_CUDA(cudaMemcpy((unsigned char *)p + kOffHp, &dh, sizeof(dh), cudaMemcpyHostToDevice));
     g_dev_scratch[dev] = (unsigned char *)p;
   }
   *out = g_dev_scratch[dev];
@@ -287,6 +296,10 @@ extern "C" tsvd_status tsvd_frpca_noalloc(int32_t nrows, int32_t ncols, int64_t 
     W.ptr_slots = kPtrSlots;
     W.dint = (int32_t *)(base + kOffInt);
     W.hint = g_hint;
+    W.dv = (double *)(base + kOffDv);
+    W.dt = (double *)(base + kOffDt);
+    W.dh = (double *)(base + kOffDh);
+    W.dh_ptrs = (double **)(base + kOffHp);
     FrpcaProblem P;
     P.block = 0;
     P.at = (const __half *)(base + kOffAt);

@@ -114,6 +114,13 @@ tsvd_status chol_inverse_batched(double *const *g, float *const *t, int l,
 // 1e-13 of the largest diagonal entry give zero columns.
 tsvd_status chol_solve_wide_batched(double *const *g, double *work, const float *x, float *y,
                                     int rows, int l, int64_t stride, int nprob, cudaStream_t st);
+// Cheap step of a subspace iteration (l <= 256): K[b] (l x l fp32, at b l l)
+// + shift * trace/l * I = L L^T in fp32, Lpk (packed, nprob x l(l+1)/2) gets
+// L, y_b = x_b L^{-T}. Keeps every direction; the basis is well-conditioned,
+// not exactly orthonormal.
+tsvd_status chol_shift_solve_batched(const float *K, float *Lpk, const float *x, float *y,
+                                     int rows, int l, int64_t stride, float shift, int nprob,
+                                     cudaStream_t st);
 // Y[b] = X[b] * W[b] * diag(colscale[b]); writes fp32 (columns [n_out, ldy)
 // zeroed) and, when yhi/ylo are given, the fp16 split of Y * split_scale.
 tsvd_status apply_right_batched(const float *const *x, const int32_t *rows,
@@ -125,10 +132,15 @@ tsvd_status apply_right_batched(const float *const *x, const int32_t *rows,
 // Two-sided cyclic Jacobi on G[b] (n x n fp64 in, fp32 work): eigenvalues
 // (descending) and eigenvectors V[b] (n x n row-major fp32, column j is the
 // eigenvector of lambda[j]).
+// refine = 1: g[b] = V^T G V for approximate eigenvectors V (nearly
+// diagonal); the diagonal is carried in fp64 (see jacobi_kernel) and the
+// rotations are replayed onto vinit[b] (V, n x n row-major), so v[b] = V R.
+// v may alias vinit.
 tsvd_status jacobi_eig_batched(double *const *g, int n, float *const *lambda,
                                float *const *v, int nprob, void *work,
                                size_t work_bytes, cudaStream_t st,
-                               int *sweeps_out);
+                               int *sweeps_out, int refine = 0,
+                               const float *const *vinit = nullptr);
 size_t jacobi_work_bytes(int n, int nprob);
 
 }  // namespace tsvd
