@@ -114,6 +114,15 @@ tsvd_status tsvd_frpca_noalloc(int32_t nrows, int32_t ncols, int64_t nnz,
                                int32_t k, int32_t q, uint64_t seed, double *U,
                                double *S, double *V);
 
+/* The tree merge's SVD on one dense matrix: replaces dense_sub_svd_function
+ * (Code/Tree_u_NC.cpp:238-262) over truncated_singular_value_decomposition
+ * (Code/matrix_vector_functions_intel_mkl.c:1259-1300). M: rows x cols,
+ * column-major (the reference's mat); US (rows x d, column-major) = U_d
+ * diag(s_d), sigma: s_d descending. d <= min(rows, cols, 144), cols <= 2048.
+ * Host pointers; device memory is allocated and freed inside the call. */
+tsvd_status tsvd_merge_svd(int32_t rows, int32_t cols, const double *M, int32_t d, double *US,
+                           double *sigma);
+
 /* ------------------------------------------------------------------------- */
 /* Session: device graph store + PPR store + block factors + merge tree.      */
 /* ------------------------------------------------------------------------- */

@@ -497,3 +497,35 @@ def test_host_reserve_matches_device_reserve():
                 s.step(e)
             emb[host] = s.embedding()
     assert gram_rel_err(emb[True], emb[False]) < 3e-2
+
+
+def _cos_cols(X, Y):
+    return np.abs(np.sum(X * Y, 0)) / (np.linalg.norm(X, axis=0) * np.linalg.norm(Y, axis=0))
+
+
+def test_merge_svd_matches_reference_golden():
+    """tsvd_merge_svd (the tree merge on one matrix) against the reference's
+    own dense_sub_svd_function output (tests/golden/ref_merge.npz, LAPACK
+    gesvd through its truncated_singular_value_decomposition)."""
+    import os
+    z = np.load(os.path.join(os.path.dirname(__file__), "golden", "ref_merge.npz"))
+    US, sig = T.merge_svd(z["M"], int(z["d"]))
+    assert np.allclose(sig, z["sigma"], rtol=1e-5)
+    assert (1 - _cos_cols(US, z["US"])).max() < 1e-5
+
+
+@pytest.mark.parametrize("rows,cols,d,top,bottom", [(600, 256, 128, 1e3, 1e-1), (400, 512, 64, 1e2, 1.0)])
+def test_merge_svd_wide_spread(rows, cols, d, top, bottom):
+    """Singular values spread over four orders of magnitude (the Gram squares
+    that to eight): the eigen-solve's fp64 refinement keeps every kept value
+    within 1e-4 of an exact SVD. 512 columns go through the wide merge's
+    subspace iteration."""
+    rng = np.random.default_rng(rows + cols)
+    Q = np.linalg.qr(rng.standard_normal((rows, min(rows, cols))))[0]
+    Vt = np.linalg.qr(rng.standard_normal((cols, min(rows, cols))))[0].T
+    s = np.geomspace(top, bottom, min(rows, cols))
+    M = (Q * s) @ Vt
+    US, sig = T.merge_svd(M, d)
+    U0, S0, _ = np.linalg.svd(M.astype(np.float32).astype(np.float64), full_matrices=False)
+    assert np.allclose(sig, S0[:d], rtol=1e-4), np.abs(sig / S0[:d] - 1).max()
+    assert (1 - _cos_cols(US, U0[:, :d] * S0[:d])).max() < 1e-4

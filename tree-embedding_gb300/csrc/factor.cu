@@ -580,16 +580,15 @@ tsvd_status orthonormalize(FrpcaWork &W, float *x, int64_t xstride, float *y, in
 // then the merge of the p columns of M V (compensated Gram + Jacobi), the
 // same arithmetic as a narrow merge. The products are plain fp32 GEMMs
 // (cuBLAS, pedantic math).
+tsvd_status merge_wide_core(FrpcaWork &W, const MergeProblem *probs, int nprob, int n, int nsrc,
+                            int root_mode, cudaStream_t st);
+
 tsvd_status merge_wide(FrpcaWork &W, const MergeProblem *probs, int nprob, int h, int nsrc,
                        int root_mode, cudaStream_t st) {
   const int d = W.d, n = h * d;
-  const int p = std::min(256, std::min(n, nsrc));
-  if (p < d) return fail(TSVD_ERR_INVALID, "merge: |S| = %d below rank d = %d", nsrc, d);
   if (nsrc > W.sp) return fail(TSVD_ERR_INVALID, "merge: |S| = %d > %d", nsrc, W.sp);
   TSVD_TRY(wide_reserve(W, std::max(nprob, W.nmax / h), n));
-  cublasHandle_t blas = (cublasHandle_t)W.blas;
-  TSVD_BLAS(cublasSetStream(blas, st));
-  const int64_t sm = (int64_t)nsrc * n, sv = (int64_t)n * p, sy = (int64_t)nsrc * p;
+  const int64_t sm = (int64_t)nsrc * n;
   // M = [B_1 .. B_h], one |S| x n row-major matrix per problem
   {
     std::vector<const float *> ch((size_t)nprob * h);
@@ -607,6 +606,20 @@ tsvd_status merge_wide(FrpcaWork &W, const MergeProblem *probs, int nprob, int h
                                                                                    nsrc, d_m);
     TSVD_LAUNCH_CHECK();
   }
+  return merge_wide_core(W, probs, nprob, n, nsrc, root_mode, st);
+}
+
+// The wide merge of the n-column matrices already in W.wm (problem i at
+// i |S| n, row-major |S| x n).
+tsvd_status merge_wide_core(FrpcaWork &W, const MergeProblem *probs, int nprob, int n, int nsrc,
+                            int root_mode, cudaStream_t st) {
+  const int d = W.d;
+  const int p = std::min(256, std::min(n, nsrc));
+  if (p < d) return fail(TSVD_ERR_INVALID, "merge: %d rows or columns, below rank d = %d",
+                         std::min(n, nsrc), d);
+  cublasHandle_t blas = (cublasHandle_t)W.blas;
+  TSVD_BLAS(cublasSetStream(blas, st));
+  const int64_t sm = (int64_t)nsrc * n, sv = (int64_t)n * p, sy = (int64_t)nsrc * p;
   // start: the p columns of M with the largest norms (the children's largest sigmas)
   colnorm_kernel<<<dim3(ceil_div(n, 256), nprob), 256, 0, st>>>(W.wm, nsrc, n, W.wnorm);
   TSVD_LAUNCH_CHECK();
@@ -686,6 +699,22 @@ tsvd_status merge_wide(FrpcaWork &W, const MergeProblem *probs, int nprob, int h
 }
 
 }  // namespace
+
+tsvd_status merge_matrix(FrpcaWork &W, const float *m_host, int rows, int cols, float *out,
+                         float *sigma_out, cudaStream_t st) {
+  if (rows > W.sp) return fail(TSVD_ERR_INVALID, "merge: %d rows > %d", rows, W.sp);
+  MergeProblem prob{};
+  prob.out = out;
+  prob.sigma_out = sigma_out;
+  if (cols > 256) {
+    TSVD_TRY(wide_reserve(W, 1, cols));
+    TSVD_CUDA(cudaMemcpyAsync(W.wm, m_host, sizeof(float) * rows * cols, cudaMemcpyHostToDevice,
+                              st));
+    return merge_wide_core(W, &prob, 1, cols, rows, 0, st);
+  }
+  TSVD_CUDA(cudaMemcpyAsync(W.z, m_host, sizeof(float) * rows * cols, cudaMemcpyHostToDevice, st));
+  return merge_finish(W, &prob, 1, cols, rows, 0, std::vector<float *>{W.z}, st);
+}
 
 tsvd_status merge_batch(FrpcaWork &W, const MergeProblem *probs, int nprob, int h, int nsrc,
                         int root_mode, cudaStream_t st) {

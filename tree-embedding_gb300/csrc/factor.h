@@ -74,6 +74,12 @@ struct MergeProblem {
 
 // Truncated SVD of [B_1 ... B_h] for every problem; out = U_d * diag(s_d) * f(s_d)
 // with f = 1 (inner node), s^-1/2 (root, U sqrt(S)) or s^-1 (root, U).
+// The merge of one ready matrix: m_host (rows x cols row-major fp32, host);
+// out (rows x d, device) = U_d diag(s_d), sigma_out (d, device) = s_d. W
+// sized by frpca_work_alloc with sp >= rows.
+tsvd_status merge_matrix(FrpcaWork &W, const float *m_host, int rows, int cols, float *out,
+                         float *sigma_out, cudaStream_t st);
+
 tsvd_status merge_batch(FrpcaWork &W, const MergeProblem *probs, int nprob, int h, int nsrc,
                         int root_mode, cudaStream_t st);
 

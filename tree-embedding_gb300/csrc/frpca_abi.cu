@@ -185,3 +185,44 @@ extern "C" void frPCA(mat_csr *A, mat **U, mat **S, mat **V, int k, int q) {
     std::memcpy(Vm->d + (size_t)j * Vm->nrows, v.data() + (size_t)src * n, sizeof(double) * n);
   }
 }
+
+// dense_sub_svd_function (Code/Tree_u_NC.cpp:238-262) over
+// truncated_singular_value_decomposition (matrix_vector_functions_intel_mkl.c
+// :1259-1300): US = U_d diag(s_d) of the dense rows x cols matrix M
+// (column-major, as the reference's mat), sigma = s_d descending. The tree
+// merge's own path: compensated Gram, Jacobi refined in fp64, and for more
+// than 256 columns the subspace iteration of the wide merge.
+extern "C" tsvd_status tsvd_merge_svd(int32_t rows, int32_t cols, const double *M, int32_t d,
+                                      double *US, double *sigma) {
+  if (rows < 1 || cols < 1 || !M || !US || !sigma) return fail(TSVD_ERR_INVALID, "merge_svd: bad arguments");
+  if (d < 1 || d > std::min(rows, cols) || d > kLp || cols > 2048 || (cols > 256 && std::min(rows, 256) < d))
+    return fail(TSVD_ERR_INVALID, "merge_svd: d = %d for %d x %d (d <= %d, cols <= 2048)", d, rows,
+                cols, kLp);
+  std::vector<float> m((size_t)rows * cols);  // row-major fp32, as the merge keeps factors
+  for (int32_t j = 0; j < cols; ++j)
+    for (int32_t i = 0; i < rows; ++i) m[(size_t)i * cols + j] = (float)M[(size_t)j * rows + i];
+  const int sp = (int)round_up(rows, kRowPad);
+  DevBuf<float> dout, dsig;
+  TSVD_TRY(dout.alloc((size_t)rows * d));
+  TSVD_TRY(dsig.alloc(d));
+  cudaStream_t st;
+  TSVD_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+  FrpcaWork W;
+  tsvd_status s1 = frpca_work_alloc(W, 1, rows, sp, std::min(kLp, d + 5), d);
+  std::vector<float> hu((size_t)rows * d), hs(d);
+  if (s1 == TSVD_OK) s1 = merge_matrix(W, m.data(), rows, cols, dout.p, dsig.p, st);
+  if (s1 == TSVD_OK) {
+    cudaMemcpyAsync(hu.data(), dout.p, sizeof(float) * hu.size(), cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(hs.data(), dsig.p, sizeof(float) * d, cudaMemcpyDeviceToHost, st);
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) s1 = fail(TSVD_ERR_DEVICE, "merge_svd: %s", cudaGetErrorString(e));
+  }
+  frpca_work_free(W);
+  cudaStreamDestroy(st);
+  if (s1 != TSVD_OK) return s1;
+  for (int32_t j = 0; j < d; ++j) {
+    sigma[j] = hs[j];
+    for (int32_t i = 0; i < rows; ++i) US[(size_t)j * rows + i] = hu[(size_t)i * d + j];
+  }
+  return TSVD_OK;
+}

@@ -87,6 +87,8 @@ _SIGS = {
     "tsvd_frpca_noalloc": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.c_int64, _i64p,
                                           _i32p, _f64p, ctypes.c_int32, ctypes.c_int32,
                                           ctypes.c_int32, ctypes.c_uint64, _f64p, _f64p, _f64p]),
+    "tsvd_merge_svd": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, _f64p, ctypes.c_int32,
+                                      _f64p, _f64p]),
     "tsvd_config_default": (None, [ctypes.POINTER(Config)]),
     "tsvd_session_create": (ctypes.c_int, [ctypes.POINTER(Config), ctypes.POINTER(_vp)]),
     "tsvd_session_destroy": (ctypes.c_int, [_vp]),
@@ -228,6 +230,17 @@ def frpca(csr_indptr, csr_indices, csr_data, shape, k, q, seed=20231, index_base
     _check(fn(m, n, len(va), _p(rp, _i64p), _p(ci, _i32p), _p(va, _f64p), index_base, k, q,
               seed, _p(U, _f64p), _p(S, _f64p), _p(V, _f64p)))
     return U.T.copy(), S, V.T.copy()
+
+
+def merge_svd(M, d):
+    """tsvd_merge_svd: (U_d diag(s_d) (rows x d), s_d) of a dense matrix."""
+    M = np.asfortranarray(M, dtype=np.float64)
+    rows, cols = M.shape
+    US = np.zeros((rows, d), np.float64, order="F")
+    sig = np.zeros(d, np.float64)
+    _check(lib().tsvd_merge_svd(rows, cols, M.ctypes.data_as(_f64p), d, US.ctypes.data_as(_f64p),
+                                _p(sig, _f64p)))
+    return US, sig
 
 
 # ----------------------------------------------------------------- session
