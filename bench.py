@@ -432,7 +432,8 @@ def main():
             "ms_materialize_kernel_mean": float(np.mean([s["ms_materialize_kernel"] for s in res["stages"]])),
             "dirty_blocks_mean": float(np.mean([s["dirty_blocks"] for s in res["stages"]])),
             "eig_sweeps_merge_max": int(max(s["eig_sweeps_merge"] for s in res["stages"])),
-            "merge_subspace_iters_max": int(max(s["merge_subspace_iters"] for s in res["stages"]))}
+            "merge_subspace_iters_max": int(max(s["merge_subspace_iters"] for s in res["stages"])),
+            "eig_refine_sweeps_max": int(max(s["eig_refine_sweeps"] for s in res["stages"]))}
     line["roofline"] = push_roofline(res["stages"])
     if "e2e_ms" in res:
         line["e2e"] = {"value": edges_all / (res["e2e_ms"] / 1e3), "unit": "edge updates/s",

@@ -233,6 +233,8 @@ typedef struct tsvd_step_stats {
   int32_t eig_sweeps_merge; /* Jacobi sweeps of the merges (max over levels)      */
   int32_t merge_subspace_iters; /* subspace iterations of merges wider than 256  */
                             /* columns (max over levels; 0 for narrow merges)    */
+  int32_t eig_refine_sweeps;/* sweeps of the fp64 refinement Jacobi (max, all     */
+                            /* eigen-solves of the snapshot)                     */
 } tsvd_step_stats;
 tsvd_status tsvd_session_last_stats(tsvd_session *s, tsvd_step_stats *out);
 

@@ -593,6 +593,7 @@ static tsvd_status stage_factorize(tsvd_session *s, FactorJob &job, cudaStream_t
   std::vector<double> ssum(nf);
   TSVD_TRY(frpca_batch(s->fw, probs.data(), nf, s->q, s->cfg.seed, s->S, st, ssum.data()));
   job.stats.eig_sweeps_frpca = s->fw.last_sweeps;
+  job.stats.eig_refine_sweeps = std::max(job.stats.eig_refine_sweeps, s->fw.last_refine_sweeps);
   // Residual ||A - U S V^T||_F = sqrt(||A||^2 - sum sigma^2) for an orthonormal
   // basis (the reference forms the dense product, Tree_u_NC.cpp:158-204).
   if (job.iter >= s->cfg.lazy_update_start_iter - 1)
@@ -627,6 +628,7 @@ static tsvd_status stage_merge(tsvd_session *s, FactorJob &job, cudaStream_t st)
     TSVD_TRY(merge_batch(s->fw, probs.data(), (int)probs.size(), h, s->S, mode, st));
     job.stats.eig_sweeps_merge = std::max(job.stats.eig_sweeps_merge, s->fw.last_sweeps);
     job.stats.merge_subspace_iters = std::max(job.stats.merge_subspace_iters, s->fw.wide_iters);
+    job.stats.eig_refine_sweeps = std::max(job.stats.eig_refine_sweeps, s->fw.last_refine_sweeps);
     job.stats.merged_nodes += (int)probs.size();
     if (root) {
       TSVD_CUDA(cudaMemcpyAsync(s->node_b(0), s->embedding, sizeof(float) * s->node_elems(),

@@ -60,7 +60,7 @@ class StepStats(ctypes.Structure):
         ("ms_push_kernels", ctypes.c_double), ("ms_materialize_kernel", ctypes.c_double),
         ("push_item_edges", ctypes.c_int64), ("ms_lp", ctypes.c_double),
         ("eig_sweeps_frpca", ctypes.c_int32), ("eig_sweeps_merge", ctypes.c_int32),
-        ("merge_subspace_iters", ctypes.c_int32),
+        ("merge_subspace_iters", ctypes.c_int32), ("eig_refine_sweeps", ctypes.c_int32),
     ]
 
     def as_dict(self):
