@@ -637,12 +637,16 @@ __global__ void __launch_bounds__(JAC_THREADS) jacobi_kernel(JacobiArgs a) {
     }
     __syncthreads();
     // Rotate when the pair is coupled: relative to the pair (Demmel-Veselic)
-    // and above an absolute floor. The first pass only has to bring the
-    // eigenvectors close (1e-6 of the pair, 1e-6 of max|a_ii|), the fp64
-    // refinement does the rest: there the off-diagonal entries are already
-    // small, and the floor (1e-11 of max|a_ii|) sits above the fp32 rounding
-    // its own rotations leave, so the tiny eigenvalues' pairs cannot cycle.
-    const float floor_abs = (refine ? 1e-11f : 1e-6f) * dmax;
+    // and above an absolute floor. The first pass only resolves the couplings
+    // above 1e-5 of max|a_ii| (a few sweeps: the Grams of merges and of
+    // frPCA's Z are nearly diagonal at that scale); it settles in fp32 the
+    // strong couplings whose small eigenvalues come from cancellation, which
+    // H = V^T G V then recomputes in fp64. The refinement does the rest: the
+    // eigenvalues span 1e-7 of the largest, so below 1e-4 of it most pairs are
+    // still coupled. Its floor (1e-11 of max|a_ii|) sits above the fp32
+    // rounding its own rotations leave, so the tiny eigenvalues' pairs cannot
+    // cycle.
+    const float floor_abs = (refine ? 1e-11f : 1e-5f) * dmax;
     const float rel_tol = refine ? 1e-7f : 1e-6f;
     for (int t = 0; t < np - 1; ++t) {
       if (threadIdx.x < P) {
