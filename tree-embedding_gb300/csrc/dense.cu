@@ -12,13 +12,17 @@
 //  chol_inverse_batched / apply_right_batched : CholeskyQR2 normalization,
 //    replacing LUfraction (Code/frpca.c:4-41); the span of the basis, which
 //    is all the power iteration keeps, is the same.
-//  jacobi_eig_batched : two-sided cyclic Jacobi on the packed Gram in shared
-//    memory, replacing LAPACKE_dsyevd (frpca.c:102) and the Gram route to
-//    LAPACKE_dgesvd (..._mkl.c:1278) for the merge.
+//  jacobi_eig_batched : two-sided cyclic Jacobi on the Gram, its rows spread
+//    over the shared memory of a thread-block cluster, replacing
+//    LAPACKE_dsyevd (frpca.c:102) and the Gram route to LAPACKE_dgesvd
+//    (..._mkl.c:1278) for the merge.
 #include <algorithm>
 #include <cfloat>
 
+#include <cooperative_groups.h>
+
 #include "internal.h"
+#include "jacobi_sched.h"
 
 namespace tsvd {
 
@@ -574,20 +578,7 @@ __global__ void __launch_bounds__(APPLY_THREADS) apply_right_kernel(ApplyArgs a)
 // ------------------------------------------------------------------ Jacobi
 constexpr int JAC_THREADS = 1024;
 constexpr int JAC_MAX_SWEEPS = 30;
-
-__device__ __forceinline__ int packed(int i, int j) {  // i <= j
-  return j * (j + 1) / 2 + i;
-}
-__device__ __forceinline__ int pk(int i, int j) { return i <= j ? packed(i, j) : packed(j, i); }
-
-// Player at circle position `pos` (<= np-1) in round `t` (< np-1) of a
-// round-robin over np players.
-__device__ __forceinline__ int circle_player(int pos, int t, int np) {
-  if (pos == 0) return 0;
-  int x = pos - 1 + t;
-  if (x >= np - 1) x -= np - 1;
-  return x + 1;
-}
+constexpr int kJacMaxCluster = 8;  // CTAs per eigenproblem (portable cluster size)
 
 struct JacobiArgs {
   double *const *g;
@@ -596,138 +587,270 @@ struct JacobiArgs {
   float2 *log;        // [prob][JAC_MAX_SWEEPS][np-1][np/2]
   int32_t *sweeps;    // [prob]
   int32_t *rank;      // [prob][n]
-  int refine;         // 1: g is nearly diagonal (see jacobi_kernel)
+  int refine;         // 1: the diagonal is carried in fp64 (see jacobi_kernel)
   const float *const *vinit;  // replay starts from these rows (null: identity)
 };
 
-// Refinement mode (a.refine): g = V^T G V for approximate eigenvectors V, so
-// its off-diagonal part is small. The diagonal is kept as an fp64 base
-// (dbase, fixed) plus an fp32 correction in the packed matrix, so the small
-// eigenvalues keep their relative accuracy: the rotation angle uses
-// (dbase_q - dbase_p) rounded once, and the updates only move the corrections.
-__global__ void __launch_bounds__(JAC_THREADS) jacobi_kernel(JacobiArgs a) {
-  extern __shared__ __align__(16) float G[];  // packed upper triangle
-  __shared__ float pc[128], ps[128], pt[128];
-  __shared__ int pp[128], pq[128];
-  __shared__ int rotated;
-  __shared__ float dmax;
-  __shared__ double dbase[256];
-  const bool refine = a.refine != 0;
-  const int n = a.n, np = n + (n & 1), P = np / 2;
-  const int R = (P + 1) / 2;               // block-row groups
-  const int Gs = (int)blockDim.x / R;      // threads per group (P <= 128: >= 16)
-  const int r = (int)threadIdx.x / Gs, jg = (int)threadIdx.x % Gs;
-  const int prob = blockIdx.x;
-  const double *Gin = a.g[prob];
-  for (int idx = threadIdx.x; idx < n * n; idx += blockDim.x) {
-    int i = idx / n, j = idx % n;
-    if (i <= j) G[packed(i, j)] = (refine && i == j) ? 0.f : (float)Gin[idx];
+// Shared-memory layout of one CTA of jacobi_kernel (C CTAs per problem).
+struct JacobiSmem {
+  int n, np, P, L, nbuf;
+  size_t off_dbase, off_lam, off_rows, off_pc, off_ps, off_pt, off_diag, off_coup, off_top,
+      off_bot, off_flag, bytes;
+  __host__ __device__ JacobiSmem(int n_, int C) {
+    n = n_;
+    np = n + (n & 1);
+    P = np / 2;
+    L = (P + C - 1) / C;
+    nbuf = 2 * L + 4;  // the rows of the owned slots' players, mailboxes [2 parities][L, R]
+    size_t o = 0;
+    off_dbase = o; o += (size_t)np * sizeof(double);
+    off_lam = o; o += (size_t)np * sizeof(double);
+    off_rows = o; o += (size_t)nbuf * np * sizeof(float);
+    off_pc = o; o += (size_t)P * sizeof(float);
+    off_ps = o; o += (size_t)P * sizeof(float);
+    off_pt = o; o += (size_t)P * sizeof(float);
+    off_diag = o; o += (size_t)2 * np * sizeof(float);  // [parity][player]
+    off_coup = o; o += (size_t)2 * P * sizeof(float);   // [parity][slot]
+    off_top = o; o += (size_t)2 * L * sizeof(int);      // two map pairs (renamed each round)
+    off_bot = o; o += (size_t)2 * L * sizeof(int);
+    off_flag = o; o += (size_t)(JAC_MAX_SWEEPS + 1) * sizeof(int);
+    bytes = (o + 15) & ~(size_t)15;
   }
-  for (int i = threadIdx.x; i < n; i += blockDim.x) dbase[i] = refine ? Gin[(int64_t)i * n + i] : 0.0;
+};
+
+// One symmetric eigenproblem per thread-block cluster of C CTAs: cyclic
+// two-sided Jacobi in the round-robin order of circle_player (np/2 disjoint
+// pairs per round, np - 1 rounds per sweep). CTA c owns the pair slots
+// [c L, c L + L) and holds the full rows (indexed by player, so a warp's
+// lanes touch consecutive words) of the two players of each owned slot.
+// A round: every CTA applies all of the round's rotations to its rows, 2 x 2
+// block by block (G <- J_k1^T G J_k2, each entry summed in an order that is
+// the same for its transposed twin, so the two copies of an entry that
+// different CTAs hold stay equal); then the schedule advances: each CTA
+// passes one row to each neighbour (into the neighbour's mailbox, in
+// distributed shared memory) and broadcasts, for every row it holds, the
+// diagonal entry and the coupling to the row's next partner; after the one
+// cluster barrier of the round, each CTA renames its rows (circle_arrivals,
+// circle_next) and computes all rotations of the next round itself, from the
+// same values in the same order, so every CTA has the same rotations without
+// a second exchange. Mailboxes and broadcast values alternate between two
+// buffers by round parity, so a fast CTA never overwrites what a slow one
+// has yet to read.
+//
+// Rotate when the pair is coupled: relative to the pair (Demmel-Veselic) and
+// above an absolute floor. The first pass only resolves the couplings above
+// 1e-5 of max|a_ii| (a few sweeps: the Grams of merges and of frPCA's Z are
+// nearly diagonal at that scale); it settles in fp32 the strong couplings
+// whose small eigenvalues come from cancellation, which H = V^T G V then
+// recomputes in fp64. Refinement mode (a.refine): g = H, the diagonal is kept
+// as an fp64 base (dbase, fixed) plus an fp32 correction in the rows, so the
+// small eigenvalues keep their relative accuracy: the rotation angle uses
+// (dbase_q - dbase_p) rounded once, and the updates only move the
+// corrections. The eigenvalues span 1e-7 of the largest, so below 1e-4 of it
+// most pairs are still coupled; the refinement's floor (1e-11 of max|a_ii|)
+// sits above the fp32 rounding its own rotations leave, so the tiny
+// eigenvalues' pairs cannot cycle.
+__global__ void __launch_bounds__(JAC_THREADS) jacobi_kernel(JacobiArgs a) {
+  namespace cg = cooperative_groups;
+  cg::cluster_group cluster = cg::this_cluster();
+  extern __shared__ __align__(16) unsigned char jsm[];
+  const int C = (int)cluster.num_blocks(), crank = (int)cluster.block_rank();
+  const JacobiSmem lay(a.n, C);
+  const int n = lay.n, np = lay.np, P = lay.P, L = lay.L;
+  double *dbase = reinterpret_cast<double *>(jsm + lay.off_dbase);
+  double *lam_all = reinterpret_cast<double *>(jsm + lay.off_lam);
+  float *rows = reinterpret_cast<float *>(jsm + lay.off_rows);
+  float *pc = reinterpret_cast<float *>(jsm + lay.off_pc);
+  float *ps = reinterpret_cast<float *>(jsm + lay.off_ps);
+  float *pt = reinterpret_cast<float *>(jsm + lay.off_pt);
+  float *diag = reinterpret_cast<float *>(jsm + lay.off_diag);  // [2][np]
+  float *coup = reinterpret_cast<float *>(jsm + lay.off_coup);  // [2][P]
+  int *const top_m = reinterpret_cast<int *>(jsm + lay.off_top);  // [2][L]
+  int *const bot_m = reinterpret_cast<int *>(jsm + lay.off_bot);
+  int *flag = reinterpret_cast<int *>(jsm + lay.off_flag);  // [sweep]: some pair rotated
+  int *top = top_m, *bot = bot_m;  // the current maps: slot s0+i -> row buffers
+  const bool refine = a.refine != 0;
+  const int prob = blockIdx.x / C;
+  const int s0 = crank * L, nloc = min(P, s0 + L) - s0;  // >= 1 (host)
+  const double *Gin = a.g[prob];
   float2 *log = a.log + (int64_t)prob * JAC_MAX_SWEEPS * (np - 1) * P;
+  // at every sweep start slot k holds players k (top) and np-1-k (bottom)
+  auto player_of = [&](int i) { return (i & 1) ? np - 1 - (s0 + i / 2) : s0 + i / 2; };
+  auto row_of = [&](int i) { return rows + (size_t)((i & 1) ? bot[i / 2] : top[i / 2]) * np; };
+  for (int i = threadIdx.x; i < nloc; i += blockDim.x) {
+    top[i] = 2 * i;
+    bot[i] = 2 * i + 1;
+  }
+  for (int i = threadIdx.x; i < np; i += blockDim.x) {
+    dbase[i] = (refine && i < n) ? Gin[(int64_t)i * n + i] : 0.0;
+    diag[i] = (!refine && i < n) ? (float)Gin[(int64_t)i * n + i] : 0.f;
+  }
+  for (int k = threadIdx.x; k < P; k += blockDim.x) {  // round 0 pairs (k, np-1-k)
+    const int q = np - 1 - k;
+    coup[k] = q < n ? (float)Gin[(int64_t)k * n + q] : 0.f;
+  }
+  for (int i = threadIdx.x; i <= JAC_MAX_SWEEPS; i += blockDim.x) flag[i] = 0;
+  for (int idx = threadIdx.x; idx < 2 * nloc * np; idx += blockDim.x) {
+    const int b = idx / np, col = idx % np, x = player_of(b);
+    float v = 0.f;
+    if (x < n && col < n && !(refine && x == col)) v = (float)Gin[(int64_t)x * n + col];
+    rows[(size_t)b * np + col] = v;
+  }
   __syncthreads();
-  int sweep = 0;
-  for (; sweep < JAC_MAX_SWEEPS; ++sweep) {
-    if (threadIdx.x == 0) {
-      rotated = 0;
-      float m = 0.f;
-      for (int i = 0; i < n; ++i)
-        m = fmaxf(m, fabsf((float)(dbase[i] + (double)G[packed(i, i)])));
-      dmax = m;
+  // Rotations of round t (of sweep `sw`, global round g) for every slot, from
+  // the broadcast values of parity `par`; threads < P.
+  float dmax = 0.f;  // max|a_ii| at the start of the sweep (threads of the first warps)
+  auto sweep_dmax = [&](int par) {
+    float m = 0.f;
+    for (int x = threadIdx.x & 31; x < n; x += 32)
+      m = fmaxf(m, fabsf((float)(dbase[x] + (double)diag[par * np + x])));
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    return m;
+  };
+  auto rotations = [&](int t, int sw, int g, int par) {
+    const int k = threadIdx.x;
+    const int x = circle_player(k, t, np), y = circle_player(np - 1 - k, t, np);
+    const int p = min(x, y), q = max(x, y);
+    float c = 1.f, s = 0.f, tt = 0.f;
+    if (q < n) {
+      const float cp = diag[par * np + p], cq = diag[par * np + q], apq = coup[par * P + k];
+      const float app = (float)(dbase[p] + (double)cp), aqq = (float)(dbase[q] + (double)cq);
+      const float floor_abs = (refine ? 1e-11f : 1e-5f) * dmax;
+      const float rel_tol = refine ? 1e-7f : 1e-6f;
+      if (fabsf(apq) > floor_abs && fabsf(apq) > rel_tol * sqrtf(fabsf(app) * fabsf(aqq))) {
+        const float diff = refine ? (float)(dbase[q] - dbase[p]) + (cq - cp) : aqq - app;
+        float tau = diff / (2.f * apq);
+        float sg = tau >= 0.f ? 1.f : -1.f;
+        tt = sg / (fabsf(tau) + sqrtf(1.f + tau * tau));
+        c = rsqrtf(1.f + tt * tt);
+        s = tt * c;
+        flag[sw] = 1;
+      }
+    }
+    pc[k] = c;
+    ps[k] = s;
+    pt[k] = tt;
+    if (k >= s0 && k < s0 + nloc) log[(int64_t)g * P + k] = make_float2(c, s);
+  };
+  if ((int)threadIdx.x < ((P + 31) & ~31)) dmax = sweep_dmax(0);
+  if ((int)threadIdx.x < P) rotations(0, 0, 0, 0);
+  __syncthreads();
+  int sweeps_done = JAC_MAX_SWEEPS;
+  for (int g = 0;; ++g) {
+    const int t = g % (np - 1);
+    // every rotation applied to the owned rows: block (owned slot k1, slot k2)
+    for (int e = threadIdx.x; e < nloc * P; e += blockDim.x) {
+      const int kl = e / P, k1 = s0 + kl, k2 = e - kl * P;
+      const float s1v = ps[k1], s2v = ps[k2];
+      if (s1v == 0.f && s2v == 0.f) continue;
+      const int x1 = circle_player(k1, t, np), y1 = circle_player(np - 1 - k1, t, np);
+      const int p1 = min(x1, y1), q1 = max(x1, y1);
+      float *rp = rows + (size_t)(x1 < y1 ? top[kl] : bot[kl]) * np;
+      float *rq = rows + (size_t)(x1 < y1 ? bot[kl] : top[kl]) * np;
+      if (k2 == k1) {  // the rotation's own 2 x 2 block
+        const float t1 = pt[k1];
+        if (q1 < n && t1 != 0.f) {
+          const float apq = rp[q1];
+          rp[p1] -= t1 * apq;
+          rq[q1] += t1 * apq;
+          rp[q1] = 0.f;
+          rq[p1] = 0.f;
+        }
+        continue;
+      }
+      const int x2 = circle_player(k2, t, np), y2 = circle_player(np - 1 - k2, t, np);
+      const int p2 = min(x2, y2), q2 = max(x2, y2);
+      const float c1 = pc[k1], c2 = pc[k2];
+      const float cc = __fmul_rn(c1, c2), cs = __fmul_rn(c1, s2v), sc = __fmul_rn(s1v, c2),
+                  ss = __fmul_rn(s1v, s2v);
+      const float b00 = rp[p2], b01 = rp[q2], b10 = rq[p2], b11 = rq[q2];
+      // J1^T B J2 with J = [[c, s], [-s, c]]; the twin block (k2, k1) sums
+      // the same four products in the same pairs
+      rp[p2] = __fsub_rn(__fadd_rn(__fmul_rn(cc, b00), __fmul_rn(ss, b11)),
+                         __fadd_rn(__fmul_rn(cs, b01), __fmul_rn(sc, b10)));
+      rp[q2] = __fsub_rn(__fadd_rn(__fmul_rn(cs, b00), __fmul_rn(cc, b01)),
+                         __fadd_rn(__fmul_rn(ss, b10), __fmul_rn(sc, b11)));
+      rq[p2] = __fsub_rn(__fadd_rn(__fmul_rn(sc, b00), __fmul_rn(cc, b10)),
+                         __fadd_rn(__fmul_rn(ss, b01), __fmul_rn(cs, b11)));
+      rq[q2] = __fadd_rn(__fadd_rn(__fmul_rn(ss, b00), __fmul_rn(cc, b11)),
+                         __fadd_rn(__fmul_rn(sc, b01), __fmul_rn(cs, b10)));
     }
     __syncthreads();
-    // Rotate when the pair is coupled: relative to the pair (Demmel-Veselic)
-    // and above an absolute floor. The first pass only resolves the couplings
-    // above 1e-5 of max|a_ii| (a few sweeps: the Grams of merges and of
-    // frPCA's Z are nearly diagonal at that scale); it settles in fp32 the
-    // strong couplings whose small eigenvalues come from cancellation, which
-    // H = V^T G V then recomputes in fp64. The refinement does the rest: the
-    // eigenvalues span 1e-7 of the largest, so below 1e-4 of it most pairs are
-    // still coupled. Its floor (1e-11 of max|a_ii|) sits above the fp32
-    // rounding its own rotations leave, so the tiny eigenvalues' pairs cannot
-    // cycle.
-    const float floor_abs = (refine ? 1e-11f : 1e-5f) * dmax;
-    const float rel_tol = refine ? 1e-7f : 1e-6f;
-    for (int t = 0; t < np - 1; ++t) {
-      if (threadIdx.x < P) {
-        const int k = threadIdx.x;
-        int x = circle_player(k, t, np), y = circle_player(np - 1 - k, t, np);
-        int p = min(x, y), q = max(x, y);
-        float c = 1.f, s = 0.f, tt = 0.f;
-        if (q < n) {
-          const float cp = G[packed(p, p)], cq = G[packed(q, q)], apq = G[packed(p, q)];
-          const float app = (float)(dbase[p] + (double)cp), aqq = (float)(dbase[q] + (double)cq);
-          if (fabsf(apq) > floor_abs && fabsf(apq) > rel_tol * sqrtf(fabsf(app) * fabsf(aqq))) {
-            const float diff = refine ? (float)(dbase[q] - dbase[p]) + (cq - cp) : aqq - app;
-            float tau = diff / (2.f * apq);
-            float sg = tau >= 0.f ? 1.f : -1.f;
-            tt = sg / (fabsf(tau) + sqrtf(1.f + tau * tau));
-            c = rsqrtf(1.f + tt * tt);
-            s = tt * c;
-            rotated = 1;
-          }
-        }
-        pp[k] = p; pq[k] = q; pc[k] = c; ps[k] = s; pt[k] = tt;
-        log[((int64_t)sweep * (np - 1) + t) * P + k] = make_float2(c, s);
+    // the next round: position j -> j - 1 (j >= 2), 1 -> np - 1, 0 stays
+    const int g1 = g + 1, t1 = g1 % (np - 1), sw1 = g1 / (np - 1), par = g1 & 1;
+    float *mbox = rows + (size_t)(2 * L + 2 * par) * np;  // [from left, from right]
+    if (P >= 2) {  // hand-over: first owned top row left, last owned bottom row right
+      if (crank > 0) {
+        const float *src = rows + (size_t)top[0] * np;
+        float *dst = cluster.map_shared_rank(mbox, crank - 1) + np;
+        for (int i = threadIdx.x; i < np; i += blockDim.x) dst[i] = src[i];
       }
-      __syncthreads();
-      // G <- J^T G J, 2x2 block by 2x2 block; each entry belongs to one block.
-      // Thread group r owns the block rows k1 = r and k1 = P-1-r (P+1 blocks
-      // together, so the groups are balanced) and loads their rotations once.
-      if (r < R) {
-        const int ra = r, rb = P - 1 - r;
-        const int na = P - ra, ntot = ra == rb ? na : na + r + 1;
-        const int pa_ = pp[ra], qa = pq[ra], pb_ = pp[rb], qb = pq[rb];
-        const float ca = pc[ra], sa = ps[ra], ta = pt[ra];
-        const float cb = pc[rb], sb = ps[rb], tb = pt[rb];
-        for (int e = jg; e < ntot; e += Gs) {
-          const bool first = e < na;
-          const int k2 = first ? ra + e : rb + (e - na);
-          const int p1 = first ? pa_ : pb_, q1 = first ? qa : qb;
-          const float c1 = first ? ca : cb, s1 = first ? sa : sb, t1 = first ? ta : tb;
-          if (k2 == (first ? ra : rb)) {  // diagonal block: the rotation's own pair
-            if (q1 < n && t1 != 0.f) {
-              const float apq = G[packed(p1, q1)];
-              G[packed(p1, p1)] -= t1 * apq;
-              G[packed(q1, q1)] += t1 * apq;
-              G[packed(p1, q1)] = 0.f;
-            }
-            continue;
-          }
-          const float c2 = pc[k2], s2 = ps[k2];
-          if (s1 == 0.f && s2 == 0.f) continue;
-          const int p2 = pp[k2], q2 = pq[k2];
-          const bool hq1 = q1 < n, hq2 = q2 < n;
-          float b00 = G[pk(p1, p2)];
-          float b01 = hq2 ? G[pk(p1, q2)] : 0.f;
-          float b10 = hq1 ? G[pk(q1, p2)] : 0.f;
-          float b11 = (hq1 && hq2) ? G[pk(q1, q2)] : 0.f;
-          float t00 = c1 * b00 - s1 * b10, t01 = c1 * b01 - s1 * b11;
-          float t10 = s1 * b00 + c1 * b10, t11 = s1 * b01 + c1 * b11;
-          G[pk(p1, p2)] = t00 * c2 - t01 * s2;
-          if (hq2) G[pk(p1, q2)] = t00 * s2 + t01 * c2;
-          if (hq1) G[pk(q1, p2)] = t10 * c2 - t11 * s2;
-          if (hq1 && hq2) G[pk(q1, q2)] = t10 * s2 + t11 * c2;
-        }
+      if (crank < C - 1) {
+        const float *src = rows + (size_t)bot[nloc - 1] * np;
+        float *dst = cluster.map_shared_rank(mbox, crank + 1);
+        for (int i = threadIdx.x; i < np; i += blockDim.x) dst[i] = src[i];
       }
-      __syncthreads();
     }
-    const int any_rotation = rotated;
-    __syncthreads();  // everyone has read `rotated` before thread 0 resets it
-    if (!any_rotation) break;
+    // each held row's diagonal, and its coupling to its next partner (sent by
+    // the lower-numbered of the two), to every CTA
+    for (int i = threadIdx.x; i < 2 * nloc; i += blockDim.x) {
+      const int k = s0 + i / 2, pos = (i & 1) ? np - 1 - k : k;
+      const int x = circle_player(pos, t, np);
+      const float *row = rows + (size_t)((i & 1) ? bot[i / 2] : top[i / 2]) * np;
+      const int pos1 = pos == 0 ? 0 : (pos == 1 ? np - 1 : pos - 1);
+      const int k1 = min(pos1, np - 1 - pos1), y = circle_player(np - 1 - pos1, t1, np);
+      const float dv = row[x];
+      const bool send_c = x < y;
+      const float cv = (send_c && y < n) ? row[y] : 0.f;
+      for (int r = 0; r < C; ++r) {
+        cluster.map_shared_rank(diag, r)[par * np + x] = dv;
+        if (send_c) cluster.map_shared_rank(coup, r)[par * P + k1] = cv;
+      }
+    }
+    cluster.sync();
+    if (P >= 2) {  // rename into the other map pair; arrived rows take the freed buffers
+      int dl, dr;
+      circle_arrivals(top, bot, s0, nloc, P, &dl, &dr);
+      int *ntop = top == top_m ? top_m + L : top_m, *nbot = bot == bot_m ? bot_m + L : bot_m;
+      for (int i = threadIdx.x; i < nloc; i += blockDim.x)
+        circle_next(top, bot, s0, nloc, P, i, dl, dr, &ntop[i], &nbot[i]);
+      for (int i = threadIdx.x; i < np; i += blockDim.x) {
+        if (dl >= 0) rows[(size_t)dl * np + i] = mbox[i];
+        if (dr >= 0) rows[(size_t)dr * np + i] = mbox[np + i];
+      }
+      top = ntop;
+      bot = nbot;
+    }
+    if (t1 == 0) {  // sweep boundary: stop after a sweep without rotations
+      __syncthreads();
+      if (!flag[sw1 - 1] || sw1 == JAC_MAX_SWEEPS) {  // the same in every CTA
+        sweeps_done = sw1;
+        break;
+      }
+      if ((int)threadIdx.x < ((P + 31) & ~31)) dmax = sweep_dmax(par);
+    }
+    if ((int)threadIdx.x < P) rotations(t1, sw1, g1, par);
+    __syncthreads();
   }
-  const int done = min(sweep + 1, JAC_MAX_SWEEPS);
-  if (threadIdx.x == 0) a.sweeps[prob] = done;
-  // eigenvalues and their descending rank
+  if (crank == 0 && threadIdx.x == 0) a.sweeps[prob] = sweeps_done;
+  // eigenvalues to every CTA of the cluster, then each ranks its own players
+  for (int i = threadIdx.x; i < 2 * nloc; i += blockDim.x) {
+    const int x = player_of(i);
+    const double lx = dbase[x] + (double)row_of(i)[x];
+    for (int r = 0; r < C; ++r) cluster.map_shared_rank(lam_all, r)[x] = lx;
+  }
+  cluster.sync();  // the last access to another CTA's shared memory is above
   float *lam = a.lambda[prob];
-  for (int i = threadIdx.x; i < n; i += blockDim.x) {
-    const double li = dbase[i] + (double)G[packed(i, i)];
+  for (int i = threadIdx.x; i < 2 * nloc; i += blockDim.x) {
+    const int x = player_of(i);
+    if (x >= n) continue;
+    const double li = lam_all[x];
     int r = 0;
     for (int j = 0; j < n; ++j) {
-      const double lj = dbase[j] + (double)G[packed(j, j)];
-      r += (lj > li) || (lj == li && j < i);
+      const double lj = lam_all[j];
+      r += (lj > li) || (lj == li && j < x);
     }
-    a.rank[prob * n + i] = r;
+    a.rank[prob * n + x] = r;
     lam[r] = (float)li;
   }
 }
@@ -1150,14 +1273,30 @@ tsvd_status jacobi_eig_batched(double *const *g, int n, float *const *lambda, fl
   a.refine = refine;
   a.vinit = vinit;
   const int P = np / 2;
-  size_t smem = (size_t)n * (n + 1) / 2 * sizeof(float);
-  static size_t cur = 0;
-  if (smem > cur) {
-    TSVD_TRY(set_smem((const void *)jacobi_kernel, smem));
-    cur = smem;
-  }
-  jacobi_kernel<<<nprob, JAC_THREADS, smem, st>>>(a);
-  TSVD_LAUNCH_CHECK();
+  // CTAs per problem: as many as keep the whole batch within one wave of
+  // clusters (up to 8), at least as many as the rows need for shared memory,
+  // and no CTA without a slot
+  const size_t smem_cap = 200 * 1024;
+  int C = 1;
+  while (C < kJacMaxCluster && (int64_t)nprob * 2 * C <= sm_count()) C *= 2;
+  while (C < kJacMaxCluster && JacobiSmem(n, C).bytes > smem_cap) C *= 2;
+  while (C > 1 && (C - 1) * JacobiSmem(n, C).L >= P) C /= 2;
+  const size_t smem = JacobiSmem(n, C).bytes;
+  if (smem > smem_cap) return fail(TSVD_ERR_INVALID, "jacobi: n=%d needs %zu B per CTA", n, smem);
+  TSVD_TRY(set_smem((const void *)jacobi_kernel, smem));
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)(nprob * C));
+  cfg.blockDim = dim3(JAC_THREADS);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = (unsigned)C;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  TSVD_CUDA(cudaLaunchKernelEx(&cfg, jacobi_kernel, a));
   const size_t rsmem = (size_t)((REPLAY_ROWS * n + 1) & ~1) * sizeof(float) +
                        (size_t)2 * REPLAY_CHUNK * P * sizeof(float2);
   static size_t rcur = 0;
