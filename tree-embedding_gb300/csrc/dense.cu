@@ -807,7 +807,7 @@ __global__ void __launch_bounds__(JAC_THREADS) jacobi_kernel(JacobiArgs a) {
         if (send_c) cluster.map_shared_rank(coup, r)[par * P + k1] = cv;
       }
     }
-    cluster.sync();
+    if (C > 1) cluster.sync(); else __syncthreads();  // a one-CTA barrier is 8x cheaper
     if (P >= 2) {  // rename into the other map pair; arrived rows take the freed buffers
       int dl, dr;
       circle_arrivals(top, bot, s0, nloc, P, &dl, &dr);
@@ -839,7 +839,7 @@ __global__ void __launch_bounds__(JAC_THREADS) jacobi_kernel(JacobiArgs a) {
     const double lx = dbase[x] + (double)row_of(i)[x];
     for (int r = 0; r < C; ++r) cluster.map_shared_rank(lam_all, r)[x] = lx;
   }
-  cluster.sync();  // the last access to another CTA's shared memory is above
+  if (C > 1) cluster.sync(); else __syncthreads();  // the last remote access is above
   float *lam = a.lambda[prob];
   for (int i = threadIdx.x; i < 2 * nloc; i += blockDim.x) {
     const int x = player_of(i);
