@@ -311,7 +311,13 @@ def test_session_matches_oracle_pipeline(directed, n, sources, parts, h, d):
                 tie = np.abs(lhs - kw["delta"] * np.sqrt(2) * o.norm) <= 1e-3 * o.norm
             assert np.array_equal(info["dirty"][~tie], o.dirty[~tie])
             if tie.any():
-                continue  # a near-tie decision may legitimately differ
+                # a near-tie decision may legitimately differ; when one does,
+                # the two sides accept different block matrices from here on
+                # (norm_diff is taken against the last accepted one), so
+                # later snapshots are no longer comparable
+                if not np.array_equal(info["dirty"][tie], o.dirty[tie]):
+                    break
+                continue
             assert st["factorized_blocks"] == len(o.last_factorized)
             for b in o.last_factorized:
                 _, sg = s.tree_factor(s.leaf_start + b)

@@ -672,6 +672,7 @@ __global__ void __launch_bounds__(JAC_THREADS) jacobi_kernel(JacobiArgs a) {
   const bool refine = a.refine != 0;
   const int prob = blockIdx.x / C;
   const int s0 = crank * L, nloc = min(P, s0 + L) - s0;  // >= 1 (host)
+  const int cgroups = (int)blockDim.x / P;  // >= 8 (P <= 128)
   const double *Gin = a.g[prob];
   float2 *log = a.log + (int64_t)prob * JAC_MAX_SWEEPS * (np - 1) * P;
   // at every sweep start slot k holds players k (top) and np-1-k (bottom)
@@ -738,42 +739,49 @@ __global__ void __launch_bounds__(JAC_THREADS) jacobi_kernel(JacobiArgs a) {
   int sweeps_done = JAC_MAX_SWEEPS;
   for (int g = 0;; ++g) {
     const int t = g % (np - 1);
-    // every rotation applied to the owned rows: block (owned slot k1, slot k2)
-    for (int e = threadIdx.x; e < nloc * P; e += blockDim.x) {
-      const int kl = e / P, k1 = s0 + kl, k2 = e - kl * P;
-      const float s1v = ps[k1], s2v = ps[k2];
-      if (s1v == 0.f && s2v == 0.f) continue;
-      const int x1 = circle_player(k1, t, np), y1 = circle_player(np - 1 - k1, t, np);
-      const int p1 = min(x1, y1), q1 = max(x1, y1);
-      float *rp = rows + (size_t)(x1 < y1 ? top[kl] : bot[kl]) * np;
-      float *rq = rows + (size_t)(x1 < y1 ? bot[kl] : top[kl]) * np;
-      if (k2 == k1) {  // the rotation's own 2 x 2 block
-        const float t1 = pt[k1];
-        if (q1 < n && t1 != 0.f) {
-          const float apq = rp[q1];
-          rp[p1] -= t1 * apq;
-          rq[q1] += t1 * apq;
-          rp[q1] = 0.f;
-          rq[p1] = 0.f;
-        }
-        continue;
-      }
+    // every rotation applied to the owned rows, 2 x 2 block (owned slot k1,
+    // slot k2) by block: a thread keeps one column slot k2 for the round and
+    // walks the owned slots (groups of P threads; the column pair's players
+    // and rotation are loaded once)
+    if ((int)threadIdx.x < cgroups * P) {
+      const int k2 = (int)threadIdx.x % P;
       const int x2 = circle_player(k2, t, np), y2 = circle_player(np - 1 - k2, t, np);
       const int p2 = min(x2, y2), q2 = max(x2, y2);
-      const float c1 = pc[k1], c2 = pc[k2];
-      const float cc = __fmul_rn(c1, c2), cs = __fmul_rn(c1, s2v), sc = __fmul_rn(s1v, c2),
-                  ss = __fmul_rn(s1v, s2v);
-      const float b00 = rp[p2], b01 = rp[q2], b10 = rq[p2], b11 = rq[q2];
-      // J1^T B J2 with J = [[c, s], [-s, c]]; the twin block (k2, k1) sums
-      // the same four products in the same pairs
-      rp[p2] = __fsub_rn(__fadd_rn(__fmul_rn(cc, b00), __fmul_rn(ss, b11)),
-                         __fadd_rn(__fmul_rn(cs, b01), __fmul_rn(sc, b10)));
-      rp[q2] = __fsub_rn(__fadd_rn(__fmul_rn(cs, b00), __fmul_rn(cc, b01)),
-                         __fadd_rn(__fmul_rn(ss, b10), __fmul_rn(sc, b11)));
-      rq[p2] = __fsub_rn(__fadd_rn(__fmul_rn(sc, b00), __fmul_rn(cc, b10)),
-                         __fadd_rn(__fmul_rn(ss, b01), __fmul_rn(cs, b11)));
-      rq[q2] = __fadd_rn(__fadd_rn(__fmul_rn(ss, b00), __fmul_rn(cc, b11)),
-                         __fadd_rn(__fmul_rn(sc, b01), __fmul_rn(cs, b10)));
+      const float c2 = pc[k2], s2v = ps[k2];
+      for (int kl = (int)threadIdx.x / P; kl < nloc; kl += cgroups) {
+        const int k1 = s0 + kl;
+        const float s1v = ps[k1];
+        if (s1v == 0.f && s2v == 0.f) continue;
+        const int x1 = circle_player(k1, t, np), y1 = circle_player(np - 1 - k1, t, np);
+        const int p1 = min(x1, y1), q1 = max(x1, y1);
+        float *rp = rows + (x1 < y1 ? top[kl] : bot[kl]) * np;
+        float *rq = rows + (x1 < y1 ? bot[kl] : top[kl]) * np;
+        if (k2 == k1) {  // the rotation's own 2 x 2 block
+          const float t1 = pt[k1];
+          if (q1 < n && t1 != 0.f) {
+            const float apq = rp[q1];
+            rp[p1] -= t1 * apq;
+            rq[q1] += t1 * apq;
+            rp[q1] = 0.f;
+            rq[p1] = 0.f;
+          }
+          continue;
+        }
+        const float c1 = pc[k1];
+        const float cc = __fmul_rn(c1, c2), cs = __fmul_rn(c1, s2v), sc = __fmul_rn(s1v, c2),
+                    ss = __fmul_rn(s1v, s2v);
+        const float b00 = rp[p2], b01 = rp[q2], b10 = rq[p2], b11 = rq[q2];
+        // J1^T B J2 with J = [[c, s], [-s, c]]; the twin block (k2, k1) sums
+        // the same four products in the same pairs
+        rp[p2] = __fsub_rn(__fadd_rn(__fmul_rn(cc, b00), __fmul_rn(ss, b11)),
+                           __fadd_rn(__fmul_rn(cs, b01), __fmul_rn(sc, b10)));
+        rp[q2] = __fsub_rn(__fadd_rn(__fmul_rn(cs, b00), __fmul_rn(cc, b01)),
+                           __fadd_rn(__fmul_rn(ss, b10), __fmul_rn(sc, b11)));
+        rq[p2] = __fsub_rn(__fadd_rn(__fmul_rn(sc, b00), __fmul_rn(cc, b10)),
+                           __fadd_rn(__fmul_rn(ss, b01), __fmul_rn(cs, b11)));
+        rq[q2] = __fadd_rn(__fadd_rn(__fmul_rn(ss, b00), __fmul_rn(cc, b11)),
+                           __fadd_rn(__fmul_rn(sc, b01), __fmul_rn(cs, b10)));
+      }
     }
     __syncthreads();
     // the next round: position j -> j - 1 (j >= 2), 1 -> np - 1, 0 stays
