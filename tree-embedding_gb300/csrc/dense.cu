@@ -579,6 +579,8 @@ __global__ void __launch_bounds__(APPLY_THREADS) apply_right_kernel(ApplyArgs a)
 constexpr int JAC_THREADS = 1024;
 constexpr int JAC_MAX_SWEEPS = 30;
 constexpr int kJacMaxCluster = 8;  // CTAs per eigenproblem (portable cluster size)
+constexpr int kJacRotBase = 512;   // first thread computing rotations (P <= 128 of them)
+constexpr int kJacSendBase = 768;  // first thread broadcasting (2 L <= 256 rows)
 
 struct JacobiArgs {
   double *const *g;
@@ -700,7 +702,7 @@ __global__ void __launch_bounds__(JAC_THREADS) jacobi_kernel(JacobiArgs a) {
   __syncthreads();
   // Rotations of round t (of sweep `sw`, global round g) for every slot, from
   // the broadcast values of parity `par`; threads < P.
-  float dmax = 0.f;  // max|a_ii| at the start of the sweep (threads of the first warps)
+  float dmax = 0.f;  // max|a_ii| at the start of the sweep (rotation warps)
   auto sweep_dmax = [&](int par) {
     float m = 0.f;
     for (int x = threadIdx.x & 31; x < n; x += 32)
@@ -708,8 +710,7 @@ __global__ void __launch_bounds__(JAC_THREADS) jacobi_kernel(JacobiArgs a) {
     for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
     return m;
   };
-  auto rotations = [&](int t, int sw, int g, int par) {
-    const int k = threadIdx.x;
+  auto rotations = [&](int k, int t, int sw, int g, int par) {
     const int x = circle_player(k, t, np), y = circle_player(np - 1 - k, t, np);
     const int p = min(x, y), q = max(x, y);
     float c = 1.f, s = 0.f, tt = 0.f;
@@ -733,8 +734,11 @@ __global__ void __launch_bounds__(JAC_THREADS) jacobi_kernel(JacobiArgs a) {
     pt[k] = tt;
     if (k >= s0 && k < s0 + nloc) log[(int64_t)g * P + k] = make_float2(c, s);
   };
-  if ((int)threadIdx.x < ((P + 31) & ~31)) dmax = sweep_dmax(0);
-  if ((int)threadIdx.x < P) rotations(0, 0, 0, 0);
+  // the rotations are computed by warps 16-19 and the broadcast sent by warps
+  // 24-31, while warps 0-7 move rows, so the phases of a round overlap
+  const int rt = (int)threadIdx.x - kJacRotBase, bt = (int)threadIdx.x - kJacSendBase;
+  if (rt >= 0 && rt < ((P + 31) & ~31)) dmax = sweep_dmax(0);
+  if (rt >= 0 && rt < P) rotations(rt, 0, 0, 0, 0);
   __syncthreads();
   int sweeps_done = JAC_MAX_SWEEPS;
   for (int g = 0;; ++g) {
@@ -801,7 +805,7 @@ __global__ void __launch_bounds__(JAC_THREADS) jacobi_kernel(JacobiArgs a) {
     }
     // each held row's diagonal, and its coupling to its next partner (sent by
     // the lower-numbered of the two), to every CTA
-    for (int i = threadIdx.x; i < 2 * nloc; i += blockDim.x) {
+    for (int i = bt; i >= 0 && i < 2 * nloc; i += JAC_THREADS - kJacSendBase) {
       const int k = s0 + i / 2, pos = (i & 1) ? np - 1 - k : k;
       const int x = circle_player(pos, t, np);
       const float *row = rows + (size_t)((i & 1) ? bot[i / 2] : top[i / 2]) * np;
@@ -835,9 +839,9 @@ __global__ void __launch_bounds__(JAC_THREADS) jacobi_kernel(JacobiArgs a) {
         sweeps_done = sw1;
         break;
       }
-      if ((int)threadIdx.x < ((P + 31) & ~31)) dmax = sweep_dmax(par);
+      if (rt >= 0 && rt < ((P + 31) & ~31)) dmax = sweep_dmax(par);
     }
-    if ((int)threadIdx.x < P) rotations(t1, sw1, g1, par);
+    if (rt >= 0 && rt < P) rotations(rt, t1, sw1, g1, par);
     __syncthreads();
   }
   if (crank == 0 && threadIdx.x == 0) a.sweeps[prob] = sweeps_done;
