@@ -520,6 +520,26 @@ def test_merge_svd_matches_reference_golden():
     assert (1 - _cos_cols(US, z["US"])).max() < 1e-5
 
 
+@pytest.mark.parametrize("cols", [2, 3, 17, 64, 133, 255])
+def test_merge_svd_sizes_and_cluster_splits(cols):
+    """One eigenproblem spread over the CTAs of a cluster, at the sizes where
+    the split changes: 2 columns (one pair, one CTA, nobody moves), 3 (a
+    dummy player, two CTAs of one slot), 17 (two CTAs of 5 and 4 slots), 64
+    (eight CTAs of 4 slots), 133 (eight CTAs of 9 slots, the last with 4; a
+    dummy player), 255 (eight CTAs of 16 slots, a dummy player). Singular
+    values and vectors against an exact SVD."""
+    rng = np.random.default_rng(cols)
+    rows = 300
+    Q = np.linalg.qr(rng.standard_normal((rows, cols)))[0]
+    Vt = np.linalg.qr(rng.standard_normal((cols, cols)))[0].T
+    M = (Q * np.geomspace(1e2, 1e-1, cols)) @ Vt
+    d = min(cols, 16)
+    US, sig = T.merge_svd(M, d)
+    U0, S0, _ = np.linalg.svd(M.astype(np.float32).astype(np.float64), full_matrices=False)
+    assert np.allclose(sig, S0[:d], rtol=1e-4), np.abs(sig / S0[:d] - 1).max()
+    assert (1 - _cos_cols(US, U0[:, :d] * S0[:d])).max() < 1e-4
+
+
 @pytest.mark.parametrize("rows,cols,d,top,bottom", [(600, 256, 128, 1e3, 1e-1), (400, 512, 64, 1e2, 1.0)])
 def test_merge_svd_wide_spread(rows, cols, d, top, bottom):
     """Singular values spread over four orders of magnitude (the Gram squares
