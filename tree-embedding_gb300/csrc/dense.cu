@@ -5,8 +5,10 @@
 //      csr_matrix_{,transpose_}matrix_mult, ..._ext.c:364-398),
 //    with A stored once per block as A^T in half precision (vertex-major, the
 //    layout the PPR state has) and the skinny operand split into hi + lo
-//    halves so that it keeps ~22 significant bits. Tensor cores (mma.sync
-//    m16n8k16, fp32 accumulate), cp.async 3-stage pipeline.
+//    halves so that it keeps ~22 significant bits. 5th-generation tensor
+//    cores: tcgen05.mma kind::f16 into a tensor-memory accumulator (fp32),
+//    operands staged by a 4-stage cp.async pipeline, stages recycled on the
+//    MMAs' mbarrier.
 //  gram_batched : X^T X with error-free products and compensated sums per
 //    row chunk, chunks summed in fp64 (Code/frpca.c:101, cblas_dgemm TN).
 //  chol_inverse_batched / apply_right_batched : CholeskyQR2 normalization,
@@ -44,40 +46,63 @@ template <int N>
 __device__ __forceinline__ void cp_async_wait() {
   asm volatile("cp.async.wait_group %0;\n" ::"n"(N));
 }
-__device__ __forceinline__ void ldsm_x4(uint32_t &r0, uint32_t &r1, uint32_t &r2, uint32_t &r3,
-                                        const void *p) {
-  asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
-               : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
-               : "r"(smem_u32(p)));
-}
-__device__ __forceinline__ void ldsm_x4_t(uint32_t &r0, uint32_t &r1, uint32_t &r2, uint32_t &r3,
-                                          const void *p) {
-  asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];\n"
-               : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
-               : "r"(smem_u32(p)));
-}
-__device__ __forceinline__ void ldsm_x2_t(uint32_t &r0, uint32_t &r1, const void *p) {
-  asm volatile("ldmatrix.sync.aligned.m8n8.x2.trans.shared.b16 {%0,%1}, [%2];\n"
-               : "=r"(r0), "=r"(r1)
-               : "r"(smem_u32(p)));
-}
-__device__ __forceinline__ void mma16816(float *c, const uint32_t *a, uint32_t b0, uint32_t b1) {
-  asm volatile(
-      "mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
-      "{%8,%9}, {%0,%1,%2,%3};\n"
-      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
-      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+// ------------------------------------------------------------------ GEMM tiles
+// The two frPCA products run on the 5th-generation tensor cores: one CTA
+// computes two 128 x 144 fp32 tiles in tensor memory (TMEM) with tcgen05.mma
+// kind::f16, issued by one thread; operand tiles are staged in shared memory
+// by cp.async in the no-swizzle core-matrix layout (8 rows x 16 bytes per
+// core matrix; LBO = distance between core matrices adjacent along K, SBO =
+// along M/N). A (the block, fp16) is K-major in the backward product
+// (A^T rows, k contiguous) and MN-major in the forward one; the skinny
+// operand (fp16 hi and lo halves, [k][144]) is MN-major in both, so every
+// operand row is copied from global memory as 16-byte pieces, unchanged.
+// A CTA computes MH = 2 row tiles of BM = 128 (two accumulators in TMEM, at
+// columns 0 and 256), so each staged tile of the skinny operand, which every
+// row tile re-reads from L2, serves 256 rows.
+constexpr int BM = 128, MH = 2, BN = kLp, BK = 64, STAGES = 3, GEMM_THREADS = 128;
+constexpr int kCoreBytes = 128;                       // one 8 x 16-byte core matrix
+constexpr int kKBlockStride = kCoreBytes;             // LBO: next 8 values of K
+constexpr int kRowBlockStride = (BK / 8) * kCoreBytes;  // SBO: next 8 rows (M or N)
+constexpr int SA_BYTES = (BM / 8) * kRowBlockStride;  // 16 KB per row tile
+constexpr int SB_BYTES = (BN / 8) * kRowBlockStride;  // 18 KB
+constexpr int STAGE_BYTES = MH * SA_BYTES + 2 * SB_BYTES;
+constexpr size_t kGemmSmem = (size_t)STAGES * STAGE_BYTES + 1024;  // + barriers, TMEM slot
+constexpr int kTmemCols = 512;                        // MH accumulators, 256 columns apart
+constexpr int kAccStride = 256;
+static_assert(BN % 16 == 0 && BN <= 256, "tcgen05.mma with M = 128 needs N % 16 == 0, N <= 256");
+
+// Counts waits that ran out (a kernel that gives up skips its tile and
+// frees its tensor memory; the host turns a non-zero count into an error).
+__device__ int g_umma_timeouts = 0;
+
+__device__ __forceinline__ uint64_t umma_smem_desc(uint32_t saddr) {
+  uint64_t d = (uint64_t)((saddr >> 4) & 0x3FFFu);
+  d |= (uint64_t)((kKBlockStride >> 4) & 0x3FFF) << 16;
+  d |= (uint64_t)((kRowBlockStride >> 4) & 0x3FFF) << 32;
+  d |= (uint64_t)1 << 46;  // descriptor version of tcgen05; base offset 0, no swizzle
+  return d;
 }
 
-// ------------------------------------------------------------------ GEMM tiles
-constexpr int BM = 128, BN = kLp, BK = 32, STAGES = 3, GEMM_THREADS = 256;
-constexpr int WN_TILES = 9;            // 72 columns per warp = 9 n8 tiles
-constexpr int SB_LD = BN + 8;          // 152 halves
-constexpr int SA_FWD_LD = BM + 8;      // 136 halves (rows = k)
-constexpr int SA_BWD_LD = BK + 8;      // 40 halves (rows = m)
-constexpr int SA_FWD_ELEMS = BK * SA_FWD_LD;
-constexpr int SA_BWD_ELEMS = BM * SA_BWD_LD;
-constexpr int SB_ELEMS = BK * SB_LD;
+// kind::f16 instruction descriptor: fp32 accumulator, fp16 A and B, A K-major
+// (0) or MN-major (1), B MN-major, N = BN, M = BM.
+__host__ __device__ constexpr uint32_t umma_idesc(int a_mn) {
+  return (1u << 4) | ((uint32_t)a_mn << 15) | (1u << 16) | ((uint32_t)(BN >> 3) << 17) |
+         ((uint32_t)(BM >> 4) << 24);
+}
+
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+  for (int it = 0; it < (1 << 24); ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        "selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
 
 struct GemmArgs {
   const __half *const *at;
@@ -90,225 +115,195 @@ struct GemmArgs {
   int splits;  // fwd split-K
 };
 
-// Load the skinny operand tile rows [k0, k0+BK) (all BN columns) of hi and lo.
-__device__ __forceinline__ void load_b_tile(__half *sb_hi, __half *sb_lo, const __half *bhi,
-                                            const __half *blo, int k0, int krows) {
-  constexpr int CHUNKS = BK * (BN / 8);  // 16-byte chunks per operand tile
-  for (int c = threadIdx.x; c < 2 * CHUNKS; c += GEMM_THREADS) {
-    int which = c / CHUNKS, cc = c % CHUNKS;
-    int row = cc / (BN / 8), col = (cc % (BN / 8)) * 8;
-    bool valid = k0 + row < krows && (which == 0 || blo != nullptr);
-    const __half *src = (which ? blo : bhi);
-    const __half *g = valid ? src + (int64_t)(k0 + row) * BN + col : bhi;
-    __half *s = (which ? sb_lo : sb_hi) + row * SB_LD + col;
-    cp_async16(s, g, valid);
-  }
-}
-
-// Fragments of 9 n8-tiles starting at column nbase for k16 step ks.
-__device__ __forceinline__ void load_b_frags(uint32_t (*b)[2], const __half *sb, int ks,
-                                             int nbase) {
-  const int lane = threadIdx.x & 31;
-  const int j = lane >> 3, r = lane & 7;
-#pragma unroll
-  for (int t = 0; t < 4; ++t) {
-    const __half *p = sb + (ks + (j & 1) * 8 + r) * SB_LD + nbase + (2 * t + (j >> 1)) * 8;
-    ldsm_x4_t(b[2 * t][0], b[2 * t][1], b[2 * t + 1][0], b[2 * t + 1][1], p);
-  }
-  const __half *p = sb + (ks + (j & 1) * 8 + r) * SB_LD + nbase + 8 * 8;
-  ldsm_x2_t(b[8][0], b[8][1], p);
-}
-
-__device__ __forceinline__ void store_acc(float (*acc)[WN_TILES][4], float *out, int m_base,
-                                          int nbase, int mrows, bool atomic, float scale) {
-  const int lane = threadIdx.x & 31, g = lane >> 2, t4 = lane & 3;
-#pragma unroll
-  for (int mt = 0; mt < 2; ++mt)
-#pragma unroll
-    for (int nt = 0; nt < WN_TILES; ++nt)
-#pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        int row = m_base + mt * 16 + g + h * 8;
-        if (row >= mrows) continue;
-        int col = nbase + nt * 8 + 2 * t4;
-        float v0 = acc[mt][nt][2 * h] * scale, v1 = acc[mt][nt][2 * h + 1] * scale;
-        float *o = out + (int64_t)row * BN + col;
-        if (atomic) {
-          atomicAdd(o, v0);
-          atomicAdd(o + 1, v1);
-        } else {
-          *reinterpret_cast<float2 *>(o) = make_float2(v0, v1);
-        }
-      }
-}
-
-// Y (Sp x BN) [+]= A (Sp x nc) * B (nc x BN); A given as A^T [nc][lda].
-__global__ void __launch_bounds__(GEMM_THREADS) gemm_fwd_kernel(GemmArgs a) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  __half *sA = reinterpret_cast<__half *>(smem_raw);
-  __half *sBh = sA + STAGES * SA_FWD_ELEMS;
-  __half *sBl = sBh + STAGES * SB_ELEMS;
+// FWD: Y (Sp x BN) [+]= A (Sp x nc) * X (nc x BN), A given as A^T [nc][lda].
+// BWD: Z (nc x BN) = A^T (nc x Sp) * Y (Sp x BN).
+// The skinny operand is hi (+ lo), both accumulated into the same tile.
+template <bool FWD>
+__global__ void __launch_bounds__(GEMM_THREADS, 1) umma_gemm_kernel(GemmArgs a) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  unsigned char *stage_base = smem_raw;
+  uint64_t *bars = reinterpret_cast<uint64_t *>(smem_raw + (size_t)STAGES * STAGE_BYTES);
+  uint32_t *tslot = reinterpret_cast<uint32_t *>(bars + STAGES);
   const int prob = blockIdx.z;
   const int nc = a.ncols[prob];
-  const __half *at = a.at[prob];
-  const __half *bhi = a.bhi[prob];
-  const __half *blo = a.blo ? a.blo[prob] : nullptr;
-  const int m0 = blockIdx.x * BM;
-  const int nk_total = (nc + BK - 1) / BK;
+  const int m0 = blockIdx.x * (BM * MH);
+  const int mrows = FWD ? a.lda : nc;  // rows of the output
+  if (m0 >= mrows) return;
+  const int nk_total = FWD ? (nc + BK - 1) / BK : a.lda / BK;
   const int per = (nk_total + a.splits - 1) / a.splits;
   const int kt0 = blockIdx.y * per, kt1 = min(nk_total, kt0 + per);
   if (kt0 >= kt1) return;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int wm = warp & 3, wn = warp >> 2;
+  const int krows = FWD ? nc : a.lda;  // valid K
+  const __half *at = a.at[prob];
+  const __half *bhi = a.bhi[prob];
+  const __half *blo = a.blo ? a.blo[prob] : nullptr;
+  const int tid = threadIdx.x, warp = tid >> 5;
 
-  auto load_a = [&](int stage, int kt) {
-    __half *s = sA + stage * SA_FWD_ELEMS;
+  // Operand tiles of stage `st` for K tile kt, as 16-byte pieces. Eight
+  // consecutive lanes fill the eight 16-byte rows of one core matrix (one
+  // shared-memory wavefront, no bank conflicts); four such groups of a warp
+  // read four adjacent pieces of the same global row (64 contiguous bytes).
+  auto load_stage = [&](int st, int kt) {
+    // the MH row tiles' A operands are adjacent: row block mb of the CTA at
+    // mb * SBO (tile mb / 16 starts at SA_BYTES * (mb / 16))
+    unsigned char *sa = stage_base + (size_t)st * STAGE_BYTES;
+    unsigned char *sbh = sa + MH * SA_BYTES, *sbl = sbh + SB_BYTES;
     const int k0 = kt * BK;
-    for (int c = threadIdx.x; c < BK * (BM / 8); c += GEMM_THREADS) {
-      int row = c / (BM / 8), col = (c % (BM / 8)) * 8;
-      bool valid = k0 + row < nc;
-      const __half *g = valid ? at + (int64_t)(k0 + row) * a.lda + m0 + col : at;
-      cp_async16(s + row * SA_FWD_LD + col, g, valid);
+    if (FWD) {  // A MN-major: piece (k, rows mb*8..+7) = A^T[k0 + k][m0 + mb*8 ..]
+      for (int c = tid; c < BK * (MH * BM / 8); c += GEMM_THREADS) {
+        const int kq = c & 7, mbq = (c >> 3) & 3, rest = c >> 5;
+        const int k = (rest & 7) * 8 + kq, mb = (rest >> 3) * 4 + mbq;
+        const bool valid = k0 + k < krows && m0 + mb * 8 < a.lda;
+        const __half *g = valid ? at + (int64_t)(k0 + k) * a.lda + m0 + mb * 8 : at;
+        cp_async16(sa + mb * kRowBlockStride + k * 16, g, valid);
+      }
+    } else {  // A K-major: piece (row m, k = kb*8..+7) = A^T[m0 + m][k0 + kb*8 ..]
+      for (int c = tid; c < MH * BM * (BK / 8); c += GEMM_THREADS) {
+        const int mq = c & 7, kb = (c >> 3) & 7, m = (c >> 6) * 8 + mq;
+        const bool valid = m0 + m < nc;
+        const __half *g = valid ? at + (int64_t)(m0 + m) * a.lda + k0 + kb * 8 : at;
+        cp_async16(sa + (m >> 3) * kRowBlockStride + kb * kKBlockStride + mq * 16, g, valid);
+      }
+    }
+    // skinny operand MN-major: piece (k, columns nb*8..+7) = B[k0 + k][nb*8 ..]
+    constexpr int kPieces = BK * (BN / 8);
+    for (int c = tid; c < 2 * kPieces; c += GEMM_THREADS) {
+      const int which = c >= kPieces, cc = c - which * kPieces;
+      const int kq = cc & 7, rest = cc >> 3;
+      const int nb = rest % (BN / 8), k = (rest / (BN / 8)) * 8 + kq;
+      const __half *src = which ? blo : bhi;
+      const bool valid = k0 + k < krows && src != nullptr;
+      const __half *g = valid ? src + (int64_t)(k0 + k) * BN + nb * 8 : bhi;
+      cp_async16((which ? sbl : sbh) + nb * kRowBlockStride + k * 16, g, valid);
     }
   };
-  auto load_stage = [&](int stage, int kt) {
-    load_a(stage, kt);
-    load_b_tile(sBh + stage * SB_ELEMS, sBl + stage * SB_ELEMS, bhi, blo, kt * BK, nc);
-  };
 
-  float acc[2][WN_TILES][4];
-#pragma unroll
-  for (int i = 0; i < 2; ++i)
-#pragma unroll
-    for (int j = 0; j < WN_TILES; ++j)
-#pragma unroll
-      for (int k = 0; k < 4; ++k) acc[i][j][k] = 0.f;
-
+  if (tid == 0)
+    for (int s = 0; s < STAGES; ++s)
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(bars + s)));
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(
+                     smem_u32(tslot)),
+                 "n"(kTmemCols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::);
+  }
   for (int s = 0; s < STAGES - 1; ++s) {
     if (kt0 + s < kt1) load_stage(s, kt0 + s);
     cp_async_commit();
   }
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+  const uint32_t tmem = *tslot;
+  constexpr uint32_t idesc = umma_idesc(FWD ? 1 : 0);
+  // every decision below is the same in all threads (__syncthreads_and), so
+  // no thread leaves the loop while another waits at its barrier
+  bool ok = true;
+  int issued = 0;  // K tiles whose MMAs were issued
   for (int kt = kt0; kt < kt1; ++kt) {
+    const int i = kt - kt0, st = i % STAGES;
     cp_async_wait<STAGES - 2>();
-    __syncthreads();
-    int nxt = kt + STAGES - 1;
-    if (nxt < kt1) load_stage((nxt - kt0) % STAGES, nxt);
-    cp_async_commit();
-    const int st = (kt - kt0) % STAGES;
-    const __half *cA = sA + st * SA_FWD_ELEMS;
-    const __half *cBh = sBh + st * SB_ELEMS;
-    const __half *cBl = sBl + st * SB_ELEMS;
-#pragma unroll
-    for (int ks = 0; ks < BK; ks += 16) {
-      uint32_t af[2][4];
-      const int j = lane >> 3, r = lane & 7;
-#pragma unroll
-      for (int mt = 0; mt < 2; ++mt) {
-        const __half *p = cA + (ks + (j >> 1) * 8 + r) * SA_FWD_LD + wm * 32 + mt * 16 + (j & 1) * 8;
-        ldsm_x4_t(af[mt][0], af[mt][1], af[mt][2], af[mt][3], p);
-      }
-      uint32_t bf[WN_TILES][2];
-      load_b_frags(bf, cBh, ks, wn * 72);
-#pragma unroll
-      for (int mt = 0; mt < 2; ++mt)
-#pragma unroll
-        for (int nt = 0; nt < WN_TILES; ++nt) mma16816(acc[mt][nt], af[mt], bf[nt][0], bf[nt][1]);
-      if (blo) {
-        load_b_frags(bf, cBl, ks, wn * 72);
-#pragma unroll
-        for (int mt = 0; mt < 2; ++mt)
-#pragma unroll
-          for (int nt = 0; nt < WN_TILES; ++nt)
-            mma16816(acc[mt][nt], af[mt], bf[nt][0], bf[nt][1]);
-      }
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");  // copies -> tensor core reads
+    if (!__syncthreads_and(ok)) {
+      ok = false;
+      break;
     }
+    if (tid == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+      const uint32_t sa = smem_u32(stage_base + (size_t)st * STAGE_BYTES);
+      const uint32_t sbh = sa + MH * SA_BYTES, sbl = sbh + SB_BYTES;
+#pragma unroll
+      for (int ks = 0; ks < BK / 16; ++ks) {
+        const uint64_t bdh = umma_smem_desc(sbh + ks * 2 * kKBlockStride);
+        const uint64_t bdl = umma_smem_desc(sbl + ks * 2 * kKBlockStride);
+        const uint32_t acc0 = (i > 0 || ks > 0) ? 1u : 0u;
+#pragma unroll
+        for (int h = 0; h < MH; ++h) {
+          const uint64_t ad = umma_smem_desc(sa + h * SA_BYTES + ks * 2 * kKBlockStride);
+          const uint32_t td = tmem + (uint32_t)(h * kAccStride);
+          asm volatile(
+              "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+              "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(td),
+              "l"(ad), "l"(bdh), "r"(idesc), "r"(acc0));
+          if (blo)
+            asm volatile(
+                "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+                "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(td),
+                "l"(ad), "l"(bdl), "r"(idesc), "r"(1u));
+        }
+      }
+      asm volatile(
+          "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+              smem_u32(bars + st))
+          : "memory");
+    }
+    issued = i + 1;
+    // refill the stage the previous tile's MMAs read, once they are done
+    const int nxt = kt + STAGES - 1;
+    if (nxt < kt1) {
+      if (i >= 1) {
+        const int pi = i - 1;
+        ok = mbar_wait(smem_u32(bars + pi % STAGES), (uint32_t)((pi / STAGES) & 1));
+      }
+      if (ok) load_stage((nxt - kt0) % STAGES, nxt);
+    }
+    cp_async_commit();
   }
+  // the last commit covers every MMA issued before it; wait for it even
+  // after a timeout, so no MMA still writes the tensor memory freed below
+  bool done = issued == 0;
+  if (issued > 0) {
+    const int li = issued - 1;
+    done = mbar_wait(smem_u32(bars + li % STAGES), (uint32_t)((li / STAGES) & 1));
+  }
+  ok = __syncthreads_and(ok && done);
   cp_async_wait<0>();
-  store_acc(acc, a.out[prob], m0 + wm * 32, wn * 72, a.lda, a.splits > 1, a.scale);
-}
-
-// Z (nc x BN) = A^T (nc x Sp) * B (Sp x BN); A^T [nc][lda].
-__global__ void __launch_bounds__(GEMM_THREADS) gemm_bwd_kernel(GemmArgs a) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  __half *sA = reinterpret_cast<__half *>(smem_raw);
-  __half *sBh = sA + STAGES * SA_BWD_ELEMS;
-  __half *sBl = sBh + STAGES * SB_ELEMS;
-  const int prob = blockIdx.z;
-  const int nc = a.ncols[prob];
-  const int m0 = blockIdx.x * BM;
-  if (m0 >= nc) return;
-  const __half *at = a.at[prob];
-  const __half *bhi = a.bhi[prob];
-  const __half *blo = a.blo ? a.blo[prob] : nullptr;
-  const int nk = a.lda / BK;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int wm = warp & 3, wn = warp >> 2;
-
-  auto load_stage = [&](int stage, int kt) {
-    __half *s = sA + stage * SA_BWD_ELEMS;
-    const int k0 = kt * BK;
-    for (int c = threadIdx.x; c < BM * (BK / 8); c += GEMM_THREADS) {
-      int row = c / (BK / 8), col = (c % (BK / 8)) * 8;
-      bool valid = m0 + row < nc;
-      const __half *g = valid ? at + (int64_t)(m0 + row) * a.lda + k0 + col : at;
-      cp_async16(s + row * SA_BWD_LD + col, g, valid);
-    }
-    load_b_tile(sBh + stage * SB_ELEMS, sBl + stage * SB_ELEMS, bhi, blo, k0, a.lda);
-  };
-
-  float acc[2][WN_TILES][4];
+  asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+  if (!ok) {
+    if ((tid & 31) == 0) atomicAdd(&g_umma_timeouts, 1);
+  } else {
+    // epilogue: warp w reads TMEM lanes 32w..32w+31 of accumulator h = output
+    // rows m0 + 128 h + 32 w + lane
+    float *out = a.out[prob];
+    const bool atomic = FWD && a.splits > 1;
+#pragma unroll 1
+    for (int h = 0; h < MH; ++h) {
+      const int row = m0 + h * BM + warp * 32 + (tid & 31);
+#pragma unroll 1
+      for (int c0 = 0; c0 < BN; c0 += 16) {
+        uint32_t v[16];
+        const uint32_t ta =
+            tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(h * kAccStride + c0);
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
+            "%14,%15}, [%16];\n"
+            : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+              "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]),
+              "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+            : "r"(ta));
+        asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+        if (row < mrows) {
+          float *o = out + (int64_t)row * BN + c0;
+          if (atomic) {
 #pragma unroll
-  for (int i = 0; i < 2; ++i)
+            for (int j = 0; j < 16; ++j) atomicAdd(o + j, __uint_as_float(v[j]) * a.scale);
+          } else {
 #pragma unroll
-    for (int j = 0; j < WN_TILES; ++j)
-#pragma unroll
-      for (int k = 0; k < 4; ++k) acc[i][j][k] = 0.f;
-
-  for (int s = 0; s < STAGES - 1; ++s) {
-    if (s < nk) load_stage(s, s);
-    cp_async_commit();
-  }
-  for (int kt = 0; kt < nk; ++kt) {
-    cp_async_wait<STAGES - 2>();
-    __syncthreads();
-    int nxt = kt + STAGES - 1;
-    if (nxt < nk) load_stage(nxt % STAGES, nxt);
-    cp_async_commit();
-    const int st = kt % STAGES;
-    const __half *cA = sA + st * SA_BWD_ELEMS;
-    const __half *cBh = sBh + st * SB_ELEMS;
-    const __half *cBl = sBl + st * SB_ELEMS;
-#pragma unroll
-    for (int ks = 0; ks < BK; ks += 16) {
-      uint32_t af[2][4];
-      const int j = lane >> 3, r = lane & 7;
-#pragma unroll
-      for (int mt = 0; mt < 2; ++mt) {
-        const __half *p = cA + (wm * 32 + mt * 16 + (j & 1) * 8 + r) * SA_BWD_LD + ks + (j >> 1) * 8;
-        ldsm_x4(af[mt][0], af[mt][1], af[mt][2], af[mt][3], p);
-      }
-      uint32_t bf[WN_TILES][2];
-      load_b_frags(bf, cBh, ks, wn * 72);
-#pragma unroll
-      for (int mt = 0; mt < 2; ++mt)
-#pragma unroll
-        for (int nt = 0; nt < WN_TILES; ++nt) mma16816(acc[mt][nt], af[mt], bf[nt][0], bf[nt][1]);
-      if (blo) {
-        load_b_frags(bf, cBl, ks, wn * 72);
-#pragma unroll
-        for (int mt = 0; mt < 2; ++mt)
-#pragma unroll
-          for (int nt = 0; nt < WN_TILES; ++nt)
-            mma16816(acc[mt][nt], af[mt], bf[nt][0], bf[nt][1]);
+            for (int j = 0; j < 16; j += 4)
+              *reinterpret_cast<float4 *>(o + j) = make_float4(
+                  __uint_as_float(v[j]) * a.scale, __uint_as_float(v[j + 1]) * a.scale,
+                  __uint_as_float(v[j + 2]) * a.scale, __uint_as_float(v[j + 3]) * a.scale);
+          }
+        }
       }
     }
   }
-  cp_async_wait<0>();
-  store_acc(acc, a.out[prob], m0 + wm * 32, wn * 72, nc, false, a.scale);
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem),
+                 "n"(kTmemCols));
 }
-
-constexpr size_t kFwdSmem = (size_t)STAGES * (SA_FWD_ELEMS + 2 * SB_ELEMS) * sizeof(__half);
-constexpr size_t kBwdSmem = (size_t)STAGES * (SA_BWD_ELEMS + 2 * SB_ELEMS) * sizeof(__half);
 
 // ------------------------------------------------------------------ Gram
 // Error-free product + TwoSum accumulation (Ogita, Rump, Oishi, "Accurate sum
@@ -967,16 +962,13 @@ static tsvd_status set_smem(const void *fn, size_t bytes) {
 tsvd_status gemm_fwd(const GemmBatch &gb, const __half *const *xhi, const __half *const *xlo,
                      float *const *y, float *y_base, size_t y_bytes, int sp, int max_nc,
                      float inv_xscale, cudaStream_t st) {
-  static bool init = false;
-  if (!init) {
-    TSVD_TRY(set_smem((const void *)gemm_fwd_kernel, kFwdSmem));
-    init = true;
-  }
   if (gb.nprob == 0) return TSVD_OK;
-  const int mtiles = sp / BM;
+  if (sp % BM != 0) return fail(TSVD_ERR_INVALID, "gemm_fwd: Sp = %d not a multiple of %d", sp, BM);
+  TSVD_TRY(set_smem((const void *)umma_gemm_kernel<true>, kGemmSmem));
+  const int mtiles = (int)ceil_div(sp, BM * MH);
   int splits = 1;
   int64_t base_ctas = (int64_t)mtiles * gb.nprob;
-  int64_t target = 2ll * sm_count();
+  int64_t target = sm_count();  // one CTA per SM (shared memory)
   if (base_ctas < target)
     splits = (int)std::min<int64_t>(ceil_div(target, base_ctas),
                                     std::max<int64_t>(1, ceil_div(max_nc, 1024)));
@@ -984,23 +976,33 @@ tsvd_status gemm_fwd(const GemmBatch &gb, const __half *const *xhi, const __half
   if (splits > 1) TSVD_CUDA(cudaMemsetAsync(y_base, 0, y_bytes, st));
   GemmArgs a{gb.at, gb.ncols, gb.lda, xhi, xlo, y, inv_xscale, splits};
   dim3 grid(mtiles, splits, gb.nprob);
-  gemm_fwd_kernel<<<grid, GEMM_THREADS, kFwdSmem, st>>>(a);
+  umma_gemm_kernel<true><<<grid, GEMM_THREADS, kGemmSmem, st>>>(a);
   TSVD_LAUNCH_CHECK();
   return TSVD_OK;
 }
 
 tsvd_status gemm_bwd(const GemmBatch &gb, const __half *const *yhi, const __half *const *ylo,
                      float *const *z, int sp, int max_nc, float inv_yscale, cudaStream_t st) {
-  static bool init = false;
-  if (!init) {
-    TSVD_TRY(set_smem((const void *)gemm_bwd_kernel, kBwdSmem));
-    init = true;
-  }
   if (gb.nprob == 0 || max_nc == 0) return TSVD_OK;
+  if (sp % BK != 0) return fail(TSVD_ERR_INVALID, "gemm_bwd: Sp = %d not a multiple of %d", sp, BK);
+  TSVD_TRY(set_smem((const void *)umma_gemm_kernel<false>, kGemmSmem));
   GemmArgs a{gb.at, gb.ncols, sp, yhi, ylo, z, inv_yscale, 1};
-  dim3 grid((unsigned)ceil_div(max_nc, BM), 1, gb.nprob);
-  gemm_bwd_kernel<<<grid, GEMM_THREADS, kBwdSmem, st>>>(a);
+  dim3 grid((unsigned)ceil_div(max_nc, BM * MH), 1, gb.nprob);
+  umma_gemm_kernel<false><<<grid, GEMM_THREADS, kGemmSmem, st>>>(a);
   TSVD_LAUNCH_CHECK();
+  return TSVD_OK;
+}
+
+tsvd_status gemm_check(cudaStream_t st) {
+  int h = 0;
+  TSVD_CUDA(cudaMemcpyFromSymbolAsync(&h, g_umma_timeouts, sizeof(int), 0, cudaMemcpyDeviceToHost, st));
+  TSVD_CUDA(cudaStreamSynchronize(st));
+  if (h != 0) {
+    const int zero = 0;
+    TSVD_CUDA(cudaMemcpyToSymbolAsync(g_umma_timeouts, &zero, sizeof(int), 0, cudaMemcpyHostToDevice, st));
+    TSVD_CUDA(cudaStreamSynchronize(st));
+    return fail(TSVD_ERR_TIMEOUT, "tensor-core GEMM: %d warps gave up waiting for their MMAs", h);
+  }
   return TSVD_OK;
 }
 

@@ -429,7 +429,7 @@ tsvd_status frpca_batch(FrpcaWork &W, const FrpcaProblem *probs, int nprob, int 
   TSVD_CUDA(cudaStreamSynchronize(st));
   if (sum_sigma2)
     for (int i = 0; i < nprob; ++i) sum_sigma2[i] = hs[i];
-  return TSVD_OK;
+  return gemm_check(st);
 }
 
 namespace {
@@ -772,7 +772,8 @@ tsvd_status lp_right_batch(FrpcaWork &W, const LpProblem *probs, int nprob, cons
   const int32_t *d_nc = pk.add_int(nc);
   TSVD_TRY(pk.upload(st));
   GemmBatch gb{d_at, d_nc, W.sp, nprob};
-  return gemm_bwd(gb, d_yhi, d_ylo, d_z, W.sp, max_nc, 1.f / kSplitScale, st);
+  TSVD_TRY(gemm_bwd(gb, d_yhi, d_ylo, d_z, W.sp, max_nc, 1.f / kSplitScale, st));
+  return gemm_check(st);
 }
 
 }  // namespace tsvd

@@ -98,6 +98,9 @@ tsvd_status gemm_fwd(const GemmBatch &gb, const __half *const *xhi,
 tsvd_status gemm_bwd(const GemmBatch &gb, const __half *const *yhi,
                      const __half *const *ylo, float *const *z, int sp,
                      int max_nc, float inv_yscale, cudaStream_t st);
+// Non-zero if a tensor-core GEMM gave up waiting for its MMAs since the last
+// check (a bounded wait ran out); synchronizes the stream.
+tsvd_status gemm_check(cudaStream_t st);
 
 // G[b] (l x l fp64) = X[b]^T X[b], X row-major [rows_b][ld] fp32.
 tsvd_status gram_batched(const float *const *x, const int32_t *rows, int max_rows,
