@@ -48,7 +48,7 @@ __device__ __forceinline__ void cp_async_wait() {
 }
 // ------------------------------------------------------------------ GEMM tiles
 // The two frPCA products run on the 5th-generation tensor cores: one CTA
-// computes two 128 x 144 fp32 tiles in tensor memory (TMEM) with tcgen05.mma
+// computes three 128 x 144 fp32 tiles in tensor memory (TMEM) with tcgen05.mma
 // kind::f16, issued by one thread; operand tiles are staged in shared memory
 // by cp.async in the no-swizzle core-matrix layout (8 rows x 16 bytes per
 // core matrix; LBO = distance between core matrices adjacent along K, SBO =
@@ -56,10 +56,12 @@ __device__ __forceinline__ void cp_async_wait() {
 // (A^T rows, k contiguous) and MN-major in the forward one; the skinny
 // operand (fp16 hi and lo halves, [k][144]) is MN-major in both, so every
 // operand row is copied from global memory as 16-byte pieces, unchanged.
-// A CTA computes MH = 2 row tiles of BM = 128 (two accumulators in TMEM, at
-// columns 0 and 256), so each staged tile of the skinny operand, which every
-// row tile re-reads from L2, serves 256 rows.
-constexpr int BM = 128, MH = 2, BN = kLp, BK = 64, STAGES = 3, GEMM_THREADS = 128;
+// A CTA computes MH = 3 row tiles of BM = 128 (three accumulators in TMEM,
+// 160 columns apart), so each staged tile of the skinny operand, which every
+// row tile re-reads from L2, serves 384 rows; K advances 32 at a time through
+// five stages.
+constexpr int BM = 128, MH = 3, BN = kLp, BK = 32, STAGES = 5, GEMM_THREADS = 128;
+constexpr int kKB = BK / 8;  // core matrices along K per stage
 constexpr int kCoreBytes = 128;                       // one 8 x 16-byte core matrix
 constexpr int kKBlockStride = kCoreBytes;             // LBO: next 8 values of K
 constexpr int kRowBlockStride = (BK / 8) * kCoreBytes;  // SBO: next 8 rows (M or N)
@@ -67,8 +69,10 @@ constexpr int SA_BYTES = (BM / 8) * kRowBlockStride;  // 16 KB per row tile
 constexpr int SB_BYTES = (BN / 8) * kRowBlockStride;  // 18 KB
 constexpr int STAGE_BYTES = MH * SA_BYTES + 2 * SB_BYTES;
 constexpr size_t kGemmSmem = (size_t)STAGES * STAGE_BYTES + 1024;  // + barriers, TMEM slot
-constexpr int kTmemCols = 512;                        // MH accumulators, 256 columns apart
-constexpr int kAccStride = 256;
+constexpr int kTmemCols = 512;                        // MH accumulators, kAccStride apart
+constexpr int kAccStride = 160;
+static_assert(MH * kAccStride <= kTmemCols && kAccStride >= BN, "accumulators fit in TMEM");
+static_assert(kKB == 4 || kKB == 8, "load mappings assume 4 or 8 core matrices along K");
 static_assert(BN % 16 == 0 && BN <= 256, "tcgen05.mma with M = 128 needs N % 16 == 0, N <= 256");
 
 // Counts waits that ran out (a kernel that gives up skips its tile and
@@ -152,14 +156,14 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1) umma_gemm_kernel(GemmArgs a) 
     if (FWD) {  // A MN-major: piece (k, rows mb*8..+7) = A^T[k0 + k][m0 + mb*8 ..]
       for (int c = tid; c < BK * (MH * BM / 8); c += GEMM_THREADS) {
         const int kq = c & 7, mbq = (c >> 3) & 3, rest = c >> 5;
-        const int k = (rest & 7) * 8 + kq, mb = (rest >> 3) * 4 + mbq;
+        const int k = (rest % kKB) * 8 + kq, mb = (rest / kKB) * 4 + mbq;
         const bool valid = k0 + k < krows && m0 + mb * 8 < a.lda;
         const __half *g = valid ? at + (int64_t)(k0 + k) * a.lda + m0 + mb * 8 : at;
         cp_async16(sa + mb * kRowBlockStride + k * 16, g, valid);
       }
     } else {  // A K-major: piece (row m, k = kb*8..+7) = A^T[m0 + m][k0 + kb*8 ..]
       for (int c = tid; c < MH * BM * (BK / 8); c += GEMM_THREADS) {
-        const int mq = c & 7, kb = (c >> 3) & 7, m = (c >> 6) * 8 + mq;
+        const int mq = c & 7, kb = (c >> 3) % kKB, m = ((c >> 3) / kKB) * 8 + mq;
         const bool valid = m0 + m < nc;
         const __half *g = valid ? at + (int64_t)(m0 + m) * a.lda + k0 + kb * 8 : at;
         cp_async16(sa + (m >> 3) * kRowBlockStride + kb * kKBlockStride + mq * 16, g, valid);
