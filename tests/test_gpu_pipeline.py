@@ -195,6 +195,25 @@ def _random_lowrank_csr(m, n, rank, density, seed):
     return sp.csr_matrix(D)
 
 
+def test_frpca_abi_block_sized():
+    """A 3000 x 12000 block at 10 % density, rank 128, q = 6: the products
+    run over several 384-row tiles and hundreds of 32-deep K stages of the
+    tensor-core GEMM in both directions. Against the oracle's frPCA on the
+    same Omega."""
+    m, n, k, q = 3000, 12000, 128, 6
+    A = _random_lowrank_csr(m, n, 400, 0.1, seed=4)
+    U, S, V = T.frpca(A.indptr, A.indices, A.data, A.shape, k, q, seed=91)
+    omega = gaussian_matrix(91, 0, n, k + 5)
+    Uo, So, _ = oracle_frpca(A.toarray(), k, q, omega=omega)
+    So = So[::-1]
+    Uo = Uo[:, ::-1]
+    assert np.allclose(S, So, rtol=1e-3, atol=1e-6 * So[0]), np.abs(S / So - 1).max()
+    j = gap_index(So, k)
+    assert j > 0
+    assert max_principal_sine(U[:, :j], Uo[:, :j]) < 1e-2
+    assert np.abs(U.T @ U - np.eye(k)).max() < 1e-3
+
+
 def test_frpca_abi_matches_oracle():
     m, n, k, q = 300, 2000, 32, 6
     A = _random_lowrank_csr(m, n, 80, 0.3, seed=1)
