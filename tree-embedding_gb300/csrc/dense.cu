@@ -499,8 +499,19 @@ __global__ void __launch_bounds__(CHOL_THREADS) chol_inverse_kernel(double *cons
 }
 
 // ------------------------------------------------------------------ X * W
-constexpr int APPLY_ROWS = 32;
+// Y = X W diag(colscale) (rows x n_out, written up to ldy <= 144 columns,
+// zero past n_out), optionally split into fp16 hi/lo. Register tiles: 256
+// threads as 16 x 16, each thread 4 rows x 9 columns (c = tx + 16 j) of a
+// 64-row tile; per k one float4 of X (the tile is staged transposed) and
+// nine loads of W feed 36 FMAs. A CTA walks a contiguous range of
+// (problem, row tile) items and restages W only when the problem changes.
+// X may alias Y (in-place CholeskyQR): a tile is read whole before it is
+// written.
+constexpr int APPLY_RT = 64;          // rows per tile
 constexpr int APPLY_THREADS = 256;
+constexpr int APPLY_CJ = 9;           // columns per thread
+constexpr int APPLY_WLD = 16 * APPLY_CJ;  // 144: staged W row
+constexpr int APPLY_XLD = APPLY_RT + 4;   // transposed X tile row (16-byte aligned)
 struct ApplyArgs {
   const float *const *x;
   const int32_t *rows;
@@ -514,58 +525,72 @@ struct ApplyArgs {
   __half *const *yhi;
   __half *const *ylo;
   float split_scale;
+  int tiles;  // row tiles per problem (of the largest)
+  int nprob;
 };
 
 __global__ void __launch_bounds__(APPLY_THREADS) apply_right_kernel(ApplyArgs a) {
   extern __shared__ __align__(16) float sm[];
-  float *sw = sm;                          // [n_in][n_out]
-  float *sx = sm + a.n_in * a.n_out;       // [APPLY_ROWS][n_in]
-  const int prob = blockIdx.y;
-  const int rows = a.rows[prob];
-  const float *W = a.w[prob];
-  const float *cs = a.colscale ? a.colscale[prob] : nullptr;
-  for (int i = threadIdx.x; i < a.n_in * a.n_out; i += blockDim.x) {
-    int r = i / a.n_out, c = i % a.n_out;
-    sw[i] = W[(int64_t)r * a.ldw + c] * (cs ? cs[c] : 1.f);
-  }
-  const float *X = a.x[prob];
-  float *Y = a.y[prob];
-  __half *Yh = a.yhi ? a.yhi[prob] : nullptr;
-  __half *Yl = a.ylo ? a.ylo[prob] : nullptr;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  for (int r0 = blockIdx.x * APPLY_ROWS; r0 < rows; r0 += gridDim.x * APPLY_ROWS) {
-    __syncthreads();
-    for (int i = threadIdx.x; i < APPLY_ROWS * a.n_in; i += blockDim.x) {
-      int rr = i / a.n_in, cc = i % a.n_in;
-      sx[i] = r0 + rr < rows ? X[(int64_t)(r0 + rr) * a.ldx + cc] : 0.f;
+  float *sw = sm;                               // [n_in][APPLY_WLD]
+  float *sxt = sm + a.n_in * APPLY_WLD;         // [n_in][APPLY_XLD] (X tile transposed)
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  const int64_t items = (int64_t)a.nprob * a.tiles;
+  const int64_t per = (items + gridDim.x - 1) / gridDim.x;
+  const int64_t i0 = blockIdx.x * per, i1 = min(items, i0 + per);
+  int cur = -1;
+  for (int64_t it = i0; it < i1; ++it) {
+    const int prob = (int)(it / a.tiles), r0 = (int)(it % a.tiles) * APPLY_RT;
+    const int rows = a.rows[prob];
+    if (r0 >= rows) continue;  // the same for every thread
+    __syncthreads();           // the previous tile is written out
+    if (prob != cur) {
+      const float *W = a.w[prob];
+      const float *cs = a.colscale ? a.colscale[prob] : nullptr;
+      for (int i = threadIdx.x; i < a.n_in * APPLY_WLD; i += blockDim.x) {
+        const int r = i / APPLY_WLD, c = i % APPLY_WLD;
+        sw[i] = c < a.n_out ? W[(int64_t)r * a.ldw + c] * (cs ? cs[c] : 1.f) : 0.f;
+      }
+      cur = prob;
+    }
+    const float *X = a.x[prob];
+    for (int i = threadIdx.x; i < APPLY_RT * a.n_in; i += blockDim.x) {
+      const int rr = i / a.n_in, k = i % a.n_in;
+      sxt[k * APPLY_XLD + rr] = r0 + rr < rows ? X[(int64_t)(r0 + rr) * a.ldx + k] : 0.f;
     }
     __syncthreads();
-    // warp w handles rows w, w+8, w+16, w+24; lane handles columns lane+32q
-    for (int rr = warp; rr < APPLY_ROWS; rr += APPLY_THREADS / 32) {
-      const int row = r0 + rr;
-      if (row >= rows) break;
-      float acc[8];
+    float acc[4][APPLY_CJ];
 #pragma unroll
-      for (int q = 0; q < 8; ++q) acc[q] = 0.f;
-      const float *xr = sx + rr * a.n_in;
-      for (int k = 0; k < a.n_in; ++k) {
-        float xv = xr[k];
-        const float *wr = sw + k * a.n_out;
+    for (int r = 0; r < 4; ++r)
 #pragma unroll
-        for (int q = 0; q < 8; ++q) {
-          int c = lane + 32 * q;
-          if (c < a.n_out) acc[q] = fmaf(xv, wr[c], acc[q]);
-        }
+      for (int j = 0; j < APPLY_CJ; ++j) acc[r][j] = 0.f;
+    for (int k = 0; k < a.n_in; ++k) {
+      const float4 xv = *reinterpret_cast<const float4 *>(sxt + k * APPLY_XLD + ty * 4);
+      const float *wr = sw + k * APPLY_WLD + tx;
+#pragma unroll
+      for (int j = 0; j < APPLY_CJ; ++j) {
+        const float wv = wr[16 * j];
+        acc[0][j] = fmaf(xv.x, wv, acc[0][j]);
+        acc[1][j] = fmaf(xv.y, wv, acc[1][j]);
+        acc[2][j] = fmaf(xv.z, wv, acc[2][j]);
+        acc[3][j] = fmaf(xv.w, wv, acc[3][j]);
       }
+    }
+    float *Y = a.y[prob];
+    __half *Yh = a.yhi ? a.yhi[prob] : nullptr;
+    __half *Yl = a.ylo ? a.ylo[prob] : nullptr;
 #pragma unroll
-      for (int q = 0; q < 8; ++q) {
-        int c = lane + 32 * q;
+    for (int r = 0; r < 4; ++r) {
+      const int row = r0 + ty * 4 + r;
+      if (row >= rows) continue;
+#pragma unroll
+      for (int j = 0; j < APPLY_CJ; ++j) {
+        const int c = tx + 16 * j;
         if (c >= a.ldy) continue;
-        float v = c < a.n_out ? acc[q] : 0.f;
+        const float v = acc[r][j];  // zero past n_out (W staged as zero there)
         Y[(int64_t)row * a.ldy + c] = v;
         if (Yh) {
-          float sv = v * a.split_scale;
-          __half h = __float2half_rn(sv);
+          const float sv = v * a.split_scale;
+          const __half h = __float2half_rn(sv);
           Yh[(int64_t)row * a.ldy + c] = h;
           Yl[(int64_t)row * a.ldy + c] = __float2half_rn(sv - __half2float(h));
         }
@@ -1249,17 +1274,17 @@ tsvd_status apply_right_batched(const float *const *x, const int32_t *rows, int 
                                 __half *const *yhi, __half *const *ylo, float split_scale,
                                 int nprob, cudaStream_t st) {
   if (nprob == 0 || max_rows == 0) return TSVD_OK;
-  if (n_out > 256 || ldy > 256 || n_in > 256)
-    return fail(TSVD_ERR_INVALID, "apply_right: sizes %d %d", n_in, n_out);
-  size_t smem = ((size_t)n_in * n_out + (size_t)APPLY_ROWS * n_in) * sizeof(float);
-  static size_t cur = 0;
-  if (smem > cur) {
-    TSVD_TRY(set_smem((const void *)apply_right_kernel, smem));
-    cur = smem;
-  }
-  ApplyArgs a{x, rows, ldx, w, ldw, n_in, n_out, colscale, y, ldy, yhi, ylo, split_scale};
-  int gx = (int)std::min<int64_t>(ceil_div(max_rows, APPLY_ROWS), 4ll * sm_count());
-  apply_right_kernel<<<dim3(gx, nprob), APPLY_THREADS, smem, st>>>(a);
+  if (n_out > APPLY_WLD || ldy > APPLY_WLD || n_in > 256 || n_in < 1)
+    return fail(TSVD_ERR_INVALID, "apply_right: sizes %d %d %d", n_in, n_out, ldy);
+  const size_t smem = (size_t)n_in * (APPLY_WLD + APPLY_XLD) * sizeof(float);
+  TSVD_TRY(set_smem((const void *)apply_right_kernel, smem));
+  const int tiles = (int)ceil_div(max_rows, APPLY_RT);
+  const int per_sm = std::max(1, (int)((227 * 1024) / (smem + 1024)));
+  const int64_t items = (int64_t)tiles * nprob;
+  const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(items, (int64_t)sm_count() * per_sm));
+  ApplyArgs a{x, rows, ldx, w, ldw, n_in, n_out, colscale, y, ldy, yhi, ylo, split_scale, tiles,
+              nprob};
+  apply_right_kernel<<<grid, APPLY_THREADS, smem, st>>>(a);
   TSVD_LAUNCH_CHECK();
   return TSVD_OK;
 }
