@@ -328,8 +328,8 @@ __device__ __forceinline__ void comp_add(Comp &acc, float a, float b) {
 constexpr int GRAM_MIN_ROWS = 128;    // rows per CTA at least (one fp64 partial per chunk)
 constexpr int GRAM_MAX_CHUNKS = 2048;  // chunks over all problems (bounds the work buffer)
 constexpr int GRAM_SUB = 32;      // rows staged in smem at a time
-constexpr int GRAM_THREADS = 512;
-constexpr int GRAM_TPT = 2;       // 4x4 output tiles per thread
+constexpr int GRAM_THREADS = 256;
+constexpr int GRAM_TPT = 1;       // 4x4 output tiles per thread (79 registers: 3 CTAs per SM)
 constexpr int GRAM_TILES_PER_CTA = GRAM_THREADS * GRAM_TPT;
 constexpr int GRAM_LMAX = 256;
 
