@@ -1324,21 +1324,39 @@ tsvd_status jacobi_eig_batched(double *const *g, int n, float *const *lambda, fl
   while (C < kJacMaxCluster && (int64_t)nprob * 2 * C <= sm_count()) C *= 2;
   while (C < kJacMaxCluster && JacobiSmem(n, C).bytes > smem_cap) C *= 2;
   while (C > 1 && (C - 1) * JacobiSmem(n, C).L >= P) C /= 2;
-  const size_t smem = JacobiSmem(n, C).bytes;
-  if (smem > smem_cap) return fail(TSVD_ERR_INVALID, "jacobi: n=%d needs %zu B per CTA", n, smem);
-  TSVD_TRY(set_smem((const void *)jacobi_kernel, smem));
+  int cmin = 1;
+  while (cmin < kJacMaxCluster && JacobiSmem(n, cmin).bytes > smem_cap) cmin *= 2;
   cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3((unsigned)(nprob * C));
-  cfg.blockDim = dim3(JAC_THREADS);
-  cfg.dynamicSmemBytes = smem;
-  cfg.stream = st;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeClusterDimension;
-  attr[0].val.clusterDim.x = (unsigned)C;
   attr[0].val.clusterDim.y = 1;
   attr[0].val.clusterDim.z = 1;
+  cfg.blockDim = dim3(JAC_THREADS);
+  cfg.stream = st;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
+  auto configure = [&](int c) -> tsvd_status {
+    cfg.gridDim = dim3((unsigned)(nprob * c));
+    cfg.dynamicSmemBytes = JacobiSmem(n, c).bytes;
+    attr[0].val.clusterDim.x = (unsigned)c;
+    return set_smem((const void *)jacobi_kernel, cfg.dynamicSmemBytes);
+  };
+  // a cluster must fit in one GPC: fewer CTAs per problem when the batch's
+  // clusters would not all be resident at once (a second wave doubles the
+  // time, as 16 clusters of 8 did)
+  while (C > cmin) {
+    TSVD_TRY(configure(C));
+    int active = 0;
+    if (cudaOccupancyMaxActiveClusters(&active, (const void *)jacobi_kernel, &cfg) != cudaSuccess) {
+      cudaGetLastError();
+      break;
+    }
+    if (active >= nprob) break;
+    C /= 2;
+  }
+  TSVD_TRY(configure(C));
+  if (cfg.dynamicSmemBytes > smem_cap)
+    return fail(TSVD_ERR_INVALID, "jacobi: n=%d needs %zu B per CTA", n, cfg.dynamicSmemBytes);
   TSVD_CUDA(cudaLaunchKernelEx(&cfg, jacobi_kernel, a));
   const size_t rsmem = (size_t)((REPLAY_ROWS * n + 1) & ~1) * sizeof(float) +
                        (size_t)2 * REPLAY_CHUNK * P * sizeof(float2);
