@@ -15,7 +15,7 @@ int main() {
   int bad = 0, cases = 0;
   for (int np = 4; np <= 260; np += 2) {
     const int P = np / 2;
-    for (int C = 1; C <= 8; ++C) {
+    for (int C = 1; C <= 16; ++C) {
       const int L = (P + C - 1) / C;
       if ((C - 1) * L >= P) continue;  // the kernel's launcher never picks this C
       ++cases;

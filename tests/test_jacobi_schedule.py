@@ -2,7 +2,7 @@
 thread-block cluster and passes rows between neighbours as the round-robin
 schedule advances. The hand-over logic (tree-embedding_gb300/csrc/
 jacobi_sched.h) is host/device code; this compiles it for the host and checks
-it against the schedule for every even size up to 260 and 1-8 CTAs."""
+it against the schedule for every even size up to 260 and 1-16 CTAs."""
 import os
 import shutil
 import subprocess
