@@ -132,12 +132,6 @@ __global__ void expand_edges_kernel(const int32_t *__restrict__ e, int64_t m, in
   }
 }
 
-__global__ void f32_to_f64_kernel(const float *in, double *out, int64_t n) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x)
-    out[i] = (double)in[i];
-}
-
 // One warp per (source i, vertex j) pair: U_b[row(i)] . V[j] in fp64, times
 // the degree product when asked; invalid pairs set *bad.
 __global__ void lp_score_kernel(const int32_t *__restrict__ pairs, int64_t m,
