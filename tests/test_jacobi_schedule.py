@@ -14,7 +14,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, '..', 'tree-embedding_gb300', 'csrc')
 
 
-def test_circle_rename_follows_schedule():
+def test_row_handover_follows_schedule():
     cxx = shutil.which('g++') or shutil.which('c++')
     if cxx is None:
         pytest.skip('no host C++ compiler')
