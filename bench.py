@@ -3,10 +3,28 @@
 A step is one snapshot refresh of the named workload: insert the delta's
 edges, refresh + push PPR (forward and reverse for directed graphs), log
 transform + lazy test of every column block, frPCA of the dirty blocks, merge
-of their ancestors. The first snapshot (half the edges, pushed from scratch)
-is set-up and is not timed; the timed steps are later, dynamic snapshots.
+of their ancestors. The first snapshot (pushed from scratch) is set-up and is
+not timed; the timed steps are later, dynamic snapshots. The default workload
+is the precision configuration's graph (directed R-MAT, N = 6,216,199,
+M = 177,862,656, |S| = 3000, 128 blocks, d = 128) refreshed by 1 %-insertion
+snapshots (1.78M edges each) after a 70 % first snapshot.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+`value` is inserted edges per second with every delta resident in HBM before
+the timed region; `e2e` is the same metric through tsvd_session_step with the
+deltas in pinned host memory (copied in every step) and the |S| x d embedding
+read back every step, on the deltas that follow the timed ones in the same
+session (at most K of them). p50/p99 are per-snapshot latencies.
+
+--impl reference times the reference's own CPU code for the path on the host
+cores (its graph insert, dense-path refresh and push, log transform and lazy
+test, compiled from its sources into oracle/_ref/; its frpca.c and merge SVD
+over an MKL stand-in): each step is one dynamic snapshot for a sample of
+sources, timed whole (`ms_per_step`), and scaled to the full snapshot in the
+metric's unit (`value`, with the scaled seconds beside it). Its inputs come
+from the oracle's own generator (the same bytes), so that process never
+loads this library.
 
 Multi-GPU: the path is replicated, not sharded (one independent session per
 rank, no collective on the data path); value = all ranks' inserted edges per
@@ -18,6 +36,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import threading
 import time
 
@@ -30,6 +49,7 @@ for _p in (ROOT, PKG):
         sys.path.insert(0, _p)
 
 METRIC = "p50/p99 re-embed latency & edge updates/s, 1 GB300, vs plain GPU form"
+DEFAULT_WORKLOAD = "rmat-d-6.2m-1pct"
 
 
 def parse():
@@ -38,22 +58,24 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="rmat-d-2.7m")
+    ap.add_argument("--workload", default=DEFAULT_WORKLOAD)
     ap.add_argument("--n", type=int, default=None)
     ap.add_argument("--m", type=int, default=None)
     ap.add_argument("--sources", type=int, default=None)
     ap.add_argument("--parts", type=int, default=None)
+    ap.add_argument("--snapshots", type=int, default=None)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--hierarchy", type=int, default=None,
                     help="merge arity (the workload's default is 2; the reference's run.sh uses 8)")
-    ap.add_argument("--host-reserve", action="store_true",
-                    help="keep the PPR reserve in pinned host memory (ppr_host_reserve), for "
-                         "workloads whose state exceeds HBM (rmat-d-6.2m)")
+    ap.add_argument("--host-reserve", default="auto", choices=["auto", "on", "off"],
+                    help="PPR reserve in pinned host memory (auto: as the workload says)")
     ap.add_argument("--pipelined", action="store_true",
                     help="time tsvd_session_run (factor stage of snapshot k overlapped with the "
                          "push of k+1: more snapshots/s, longer per-snapshot latency) instead of "
                          "one tsvd_session_step per snapshot")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-sources", type=int, default=None,
+                    help="sources in the CPU sample (default: two per host thread)")
     ap.add_argument("--seed", type=int, default=20231)
     return ap.parse_args()
 
@@ -116,16 +138,22 @@ class ClockSampler:
                 "samples": len(self.samples)}
 
 
-def workload(args):
+def workload(args, generator=None):
     import workloads as W
-    cfg = W.scaled(args.workload, n=args.n, m=args.m, sources=args.sources, n_parts=args.parts)
+    cfg = W.scaled(args.workload, n=args.n, m=args.m, sources=args.sources,
+                   n_parts=args.parts, snapshots=args.snapshots)
     if args.hierarchy:
         cfg["hierarchy_n"] = args.hierarchy
     need = 1 + args.warmup + args.steps
     if cfg["snapshots"] < need:
-        cfg["snapshots"] = need  # the second half of the edges is cut into more, smaller deltas
-    edges, snaps, sources = W.build(cfg, seed=args.seed)
+        raise SystemExit("workload %s has %d deltas; --warmup + --steps (%d) must not exceed them "
+                         "(or pass --snapshots)" % (args.workload, cfg["snapshots"] - 1, need - 1))
+    edges, snaps, sources = W.build(cfg, seed=args.seed, generator=generator)
     return cfg, snaps, sources
+
+
+def host_reserve(args, cfg):
+    return {"on": True, "off": False}.get(args.host_reserve, bool(cfg.get("host_reserve")))
 
 
 def peaks():
@@ -138,12 +166,14 @@ def peaks():
 
 # ------------------------------------------------------------------ our arm
 def run_ours(args, cfg, snaps, sources, device):
-    """Our arm. Each timed snapshot is one tsvd_session_step(_device) call, or
-    with --pipelined all K go through one tsvd_session_run(_device) call (the
-    factor stage of snapshot k overlapped with the push of snapshot k+1).
+    """Our arm. Each timed snapshot is one tsvd_session_step_device call (or,
+    with --pipelined, all K go through one tsvd_session_run_device call).
     Every snapshot is complete (embedding written) inside the timed region.
     Per-snapshot latency (stats ms_total) runs from the start of a snapshot's
-    insert to the end of its factor stage."""
+    insert to the end of its factor stage. The e2e leg continues the same
+    session through tsvd_session_step with host deltas."""
+    import ctypes
+
     import torch
     import tsvd_gb300 as T
     import workloads as W
@@ -152,16 +182,17 @@ def run_ours(args, cfg, snaps, sources, device):
     kw = W.session_kwargs(cfg, dynamic_start=2, lazy_start=2)
     kw["device"] = device
     kw["seed"] = args.seed
-    kw["ppr_host_reserve"] = args.host_reserve
+    kw["ppr_host_reserve"] = host_reserve(args, cfg)
     t0i, t1i = 1 + args.warmup, 1 + args.warmup + args.steps
     timed = snaps[t0i:t1i]
     off = np.concatenate([[0], np.cumsum([len(e) for e in timed])]).astype(np.int64)
-    # --- device-resident inputs: every delta uploaded before the timed region
     dev = [torch.from_numpy(np.ascontiguousarray(e)).to(f"cuda:{device}") for e in snaps[:t0i]]
     dev_timed = torch.from_numpy(np.ascontiguousarray(np.concatenate(timed))).to(f"cuda:{device}")
     res = {}
     with T.Session(cfg["n"], sources, **kw) as s:
+        t = time.perf_counter()
         s.step_device(dev[0].data_ptr(), len(snaps[0]))  # set-up: first snapshot, from scratch
+        res["setup_s"] = time.perf_counter() - t
         for k in range(args.warmup):
             s.step_device(dev[1 + k].data_ptr(), len(snaps[1 + k]))
         stream = torch.cuda.ExternalStream(s.stream(), device=device)
@@ -185,164 +216,238 @@ def run_ours(args, cfg, snaps, sources, device):
         ms = ev0.elapsed_time(ev1)
         res.update(ms=ms, wall=wall, per_step=[st["ms_total"] for st in stage], stages=stage,
                    launches=launches, clocks=clk.summary(), edges=int(off[-1]))
-    del dev, dev_timed
-    torch.cuda.empty_cache()
-    if args.no_e2e:
-        return res
-    # --- end to end through the C-ABI: host edges (pinned) copied in and every
-    # snapshot's embedding read back inside the timed region
-    pinned_timed = torch.from_numpy(np.ascontiguousarray(np.concatenate(timed))).pin_memory()
-    import ctypes
-    with T.Session(cfg["n"], sources, **kw) as s:
+        del dev, dev_timed
+        rest = snaps[t1i:t1i + args.steps]
+        if args.no_e2e or not rest:
+            return res
+        # --- end to end through the C-ABI on the deltas that follow: host
+        # pairs (pinned) copied in and the embedding read back every step
+        pinned = [torch.from_numpy(np.ascontiguousarray(e)).pin_memory() for e in rest]
         L = T.lib()
-        for i in range(t0i):
-            e = torch.from_numpy(np.ascontiguousarray(snaps[i])).pin_memory()
-            T._check(L.tsvd_session_step(
-                s._h, ctypes.cast(e.data_ptr(), ctypes.POINTER(ctypes.c_int32)), len(snaps[i])))
-        emb = np.zeros((args.steps, len(sources), cfg["rank_d"]), np.float64)
-        stats = (T.StepStats * args.steps)()
-        stream = torch.cuda.ExternalStream(s.stream(), device=device)
+        emb = np.zeros((len(rest), len(sources), cfg["rank_d"]), np.float64)
+        stats = (T.StepStats * len(rest))()
         ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         torch.cuda.synchronize(device)
         i32p, f64p = ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_double)
         ev0.record(stream)
-        if args.pipelined:
-            T._check(L.tsvd_session_run(
-                s._h, ctypes.cast(pinned_timed.data_ptr(), i32p),
-                off.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), args.steps,
-                emb.ctypes.data_as(f64p), stats))
-        else:
-            for k in range(args.steps):
-                T._check(L.tsvd_session_step(
-                    s._h, ctypes.cast(pinned_timed.data_ptr() + int(off[k]) * 8, i32p),
-                    int(off[k + 1] - off[k])))
-                T._check(L.tsvd_session_embedding(s._h, emb[k].ctypes.data_as(f64p)))
-                T._check(L.tsvd_session_last_stats(s._h, ctypes.byref(stats[k])))
+        for k, e in enumerate(pinned):
+            T._check(L.tsvd_session_step(s._h, ctypes.cast(e.data_ptr(), i32p), len(rest[k])))
+            T._check(L.tsvd_session_embedding(s._h, emb[k].ctypes.data_as(f64p)))
+            T._check(L.tsvd_session_last_stats(s._h, ctypes.byref(stats[k])))
         ev1.record(stream)
         torch.cuda.synchronize(device)
         assert np.isfinite(emb).all()
         res["e2e_ms"] = ev0.elapsed_time(ev1)
-        res["e2e_lat"] = [stats[k].ms_total for k in range(args.steps)]
-        res["h2d"] = int(off[-1] * 8 / args.steps)
-        res["d2h"] = int(len(sources) * cfg["rank_d"] * 4)
+        res["e2e_edges"] = int(sum(len(e) for e in rest))
+        res["e2e_steps"] = len(rest)
+        res["e2e_lat"] = [stats[k].ms_total for k in range(len(rest))]
+        res["h2d"] = int(res["e2e_edges"] * 8 / len(rest))
+        res["d2h"] = int(len(sources) * cfg["rank_d"] * 8)
     return res
 
 
-def cpu_sample(cfg, snaps, sources, budget_sources=None, threads=None):
-    """Times the CPU oracle (the reference algorithm restated) on a bounded
-    sample of one dynamic snapshot and scales it to the full workload:
-    refresh + push on a subset of sources (cost is per source), one block's
-    log transform + frPCA at full |S| (on a synthetic block of the measured
-    density) and one merge, scaled by the blocks / merges of the snapshot."""
+# ------------------------------------------------------------- CPU samples
+class _QuietStdout:
+    """The reference's graph reader reports progress on stdout; keep it off
+    the bench's one-line output (fd 1 goes to /dev/null meanwhile)."""
+
+    def __enter__(self):
+        sys.stdout.flush()
+        self.saved = os.dup(1)
+        self.null = os.open(os.devnull, os.O_WRONLY)
+        os.dup2(self.null, 1)
+
+    def __exit__(self, *a):
+        os.dup2(self.saved, 1)
+        os.close(self.saved)
+        os.close(self.null)
+
+
+def cpu_sample(cfg, snaps, sources, steps, k=None, threads=None, budget_s=150.0):
+    """Times the reference's own CPU code on a bounded sample of the workload.
+
+    Set-up (untimed): the reference graph store is fed the first snapshot
+    through its own reader, and k sampled sources are pushed from scratch
+    (both directions for a directed graph). Each step then times one dynamic
+    snapshot: the reference's insert of the delta file, its refresh + push for
+    the k sources (std::threads over source ranges, as its drivers run them),
+    its log transform + lazy test of every block on those k rows, frPCA
+    (frpca.c) of two real blocks of the snapshot (the k sampled rows tiled to
+    |S| rows, so the block has the full shape, density and values), and one
+    merge SVD of their two factors. The full snapshot is the sum of the
+    insert, (push + log) x |S|/k, frPCA x blocks (every block dirty) and the
+    merge x (blocks - 1).
+
+    With oracle/_ref absent (no reference sources were ever staged), the
+    oracle's restatement (oracle/) stands in for each piece."""
     from oracle import native
-    from oracle.tree_oracle import frpca, log_transform
+    from oracle.tree_oracle import frpca as port_frpca
+    from oracle.tree_oracle import gaussian_matrix, log_transform
     import scipy.sparse as sp
 
     threads = threads or os.cpu_count() or 1
-    S = len(sources)
-    k = budget_sources or max(threads, min(S, 2 * threads))
+    S, n, nparts = len(sources), cfg["n"], cfg["n_parts"]
+    k = min(S, k or 2 * threads)
     sub = np.sort(np.random.default_rng(0).choice(sources, k, replace=False)).astype(np.int32)
-    n, alpha, rmax = cfg["n"], cfg["alpha"], cfg["rmax"]
+    alpha, rmax, d, q = cfg["alpha"], cfg["rmax"], cfg["rank_d"], cfg["passes_q"]
     dirs = 2 if cfg["directed"] else 1
-    g = native.OracleGraph(n, cfg["directed"])
-    st = [native.OraclePPR(n, sub) for _ in range(dirs)]
-    g.insert(snaps[0])
-    for d in range(dirs):
-        st[d].refresh(g, d, 1, 2, alpha, rmax, threads=threads)
-        st[d].push(g, d, alpha, rmax, threads=threads)
-    t = time.perf_counter()
-    g.insert(snaps[1])
-    for d in range(dirs):
-        st[d].refresh(g, d, 2, 2, alpha, rmax, threads=threads)
-        st[d].push(g, d, alpha, rmax, threads=threads)
-    t_push = time.perf_counter() - t
-    p = sum(x.reserve().astype(np.float64) for x in st)
-    nparts = cfg["n_parts"]
     cd = n // nparts
-    t = time.perf_counter()
-    A = log_transform(p[:, :cd], rmax, cfg["transform"], n)
-    t_log = (time.perf_counter() - t) * nparts
-    density = np.count_nonzero(A) / A.size
-    # one full-size block (|S| x n_b) of the measured density for frPCA
-    rng = np.random.default_rng(1)
-    nnz = int(density * S * cd)
-    rows = rng.integers(0, S, nnz)
-    cols = rng.integers(0, cd, nnz)
-    vals = rng.uniform(0, np.log10(1 / rmax), nnz)
-    B = sp.csr_matrix((vals, (rows, cols)), shape=(S, cd))
-    omega = rng.standard_normal((cd, cfg["rank_d"] + 5))
-    t = time.perf_counter()
-    U, Sg, V = frpca(B, cfg["rank_d"], cfg["passes_q"], omega=omega)
-    t_frpca = time.perf_counter() - t
-    M = rng.standard_normal((S, cfg["hierarchy_n"] * cfg["rank_d"]))
-    t = time.perf_counter()
-    np.linalg.svd(M, full_matrices=False)
-    t_merge = time.perf_counter() - t
-    merges = nparts - 1
-    est = t_push * S / k + t_log * S / k + t_frpca * nparts + t_merge * merges
-    return {"seconds_per_snapshot": est, "edges": len(snaps[1]), "threads": threads,
-            "sample": ("one dynamic snapshot (%d edges): refresh+push on %d of %d sources "
-                       "(%.2fs, scaled x%.1f), log transform of one block (x%d), frPCA of one "
-                       "%dx%d block at density %.3f (%.2fs, x%d blocks), one %dx%d merge SVD "
-                       "(x%d); all blocks assumed dirty" % (
-                           len(snaps[1]), k, S, t_push, S / k, nparts, S, cd, density, t_frpca,
-                           nparts, S, cfg["hierarchy_n"] * cfg["rank_d"], merges))}
+    kind = "reference" if native.ref_available() else "port"
+    kind_frpca = "reference" if native.ref_frpca_available() else "port"
+    tmp = tempfile.mkdtemp(prefix="tsvd_cpu_")
+    t_setup = time.perf_counter()
+    if kind == "reference":
+        path0 = os.path.join(tmp, "snap0.txt")
+        native.write_edges_text(path0, snaps[0])
+        g = native.RefGraph(n, cfg["directed"])
+        with _QuietStdout():
+            g.insert_file(path0)
+        os.unlink(path0)
+        st = [native.RefPPR(n, sub, nparts, alpha, rmax) for _ in range(dirs)]
+        for dd in range(dirs):
+            st[dd].step(g, dd, 1, 2, threads)
+    else:
+        g = native.OracleGraph(n, cfg["directed"])
+        g.insert(snaps[0])
+        st = [native.OraclePPR(n, sub) for _ in range(dirs)]
+        for dd in range(dirs):
+            st[dd].refresh(g, dd, 1, 2, alpha, rmax, threads=threads)
+            st[dd].push(g, dd, alpha, rmax, threads=threads)
+    t_setup = time.perf_counter() - t_setup
+    out = []
+    t_budget = time.perf_counter()
+    for step in range(steps):
+        delta = snaps[1 + step]
+        path = os.path.join(tmp, "delta.txt")
+        if kind == "reference":
+            native.write_edges_text(path, delta)
+        w0 = time.perf_counter()
+        if kind == "reference":
+            with _QuietStdout():
+                g.insert_file(path)
+        else:
+            g.insert(delta)
+        t_ins = time.perf_counter() - w0
+        t = time.perf_counter()
+        for dd in range(dirs):
+            if kind == "reference":
+                st[dd].step(g, dd, 2 + step, 2, threads)
+            else:
+                st[dd].refresh(g, dd, 2 + step, 2, alpha, rmax, threads=threads)
+                st[dd].push(g, dd, alpha, rmax, threads=threads)
+        t_push = time.perf_counter() - t
+        t = time.perf_counter()
+        blocks = []
+        if kind == "reference":
+            st[0].log_only(2 + step, cfg.get("delta", 0.3), np.zeros(nparts))
+            for b in (0, nparts // 2):
+                rp, ci, va = st[0].block_csr(b)
+                width = n - (nparts - 1) * cd if b == nparts - 1 else cd
+                blocks.append(sp.csr_matrix((va, ci, rp), shape=(k, width)))
+        else:
+            p = st[0].reserve().astype(np.float64)
+            for b in range(nparts):
+                c1 = n if b == nparts - 1 else (b + 1) * cd
+                A = log_transform(p[:, b * cd:c1], rmax, cfg["transform"], n)
+                if b in (0, nparts // 2):
+                    blocks.append(sp.csr_matrix(A))
+        t_log = time.perf_counter() - t
+        # frPCA of two real blocks at full |S|: the k rows tiled
+        t_fr, factors = [], []
+        for A in blocks:
+            full = sp.vstack([A] * (S // k + 1), format="csr")[:S]
+            t = time.perf_counter()
+            if kind_frpca == "reference":
+                U, Sg, V, _ = native.ref_frpca(full, d, q, seed=7)
+                Sg = Sg[::-1]
+                U = U[:, ::-1]
+            else:
+                omega = gaussian_matrix(7, 0, full.shape[1], d + 5)
+                U, Sg, V = port_frpca(full, d, q, omega=omega)
+                Sg, U = Sg[::-1], U[:, ::-1]
+            t_fr.append(time.perf_counter() - t)
+            factors.append(U * Sg[None, :])
+        M = np.hstack(factors)
+        t = time.perf_counter()
+        if kind_frpca == "reference":
+            native.ref_merge_svd(M, d)
+        else:
+            np.linalg.svd(M, full_matrices=False)
+        t_merge = time.perf_counter() - t
+        wall = time.perf_counter() - w0
+        scaled = t_ins + (t_push + t_log) * S / k + float(np.mean(t_fr)) * nparts + \
+            t_merge * (nparts - 1)
+        out.append(dict(wall_s=wall, scaled_s=scaled, edges=len(delta), insert_s=t_ins,
+                        push_s=t_push, log_s=t_log, frpca_block_s=float(np.mean(t_fr)),
+                        merge_s=t_merge))
+        if time.perf_counter() - t_budget > budget_s:
+            break
+    try:
+        os.rmdir(tmp)
+    except OSError:
+        pass
+    desc = ("%s code on %d host threads: one dynamic snapshot per step (%d-edge deltas): insert "
+            "of the delta file; refresh + push of %d of %d sources (%s), x %.1f; log transform + "
+            "lazy test of all %d blocks on those rows, x %.1f; frPCA (q = %d, d = %d) of two real "
+            "%d x %d blocks (the sampled rows tiled to |S| rows; %s), x %d blocks (all assumed "
+            "dirty); one %d x %d merge SVD, x %d. Set-up (first snapshot, from-scratch push of "
+            "the sampled sources) %.0f s, untimed" % (
+                "the reference's own" if kind == "reference" else "the oracle's restated",
+                threads, len(snaps[1]), k, S, "forward and reverse" if dirs == 2 else "undirected",
+                S / k, nparts, S / k, q, d, S, cd, kind_frpca + " frpca.c" if kind_frpca ==
+                "reference" else "oracle frPCA", nparts, S, 2 * d, nparts - 1, t_setup))
+    return {"steps": out, "threads": threads, "kind": kind, "sample": desc, "k": k,
+            "setup_s": t_setup}
 
 
 def run_reference(args):
     rank, world, local = dist_env()
     if rank != 0:
         return
-    cfg, snaps, sources = workload(args)
-    vals = []
-    info = None
-    t0 = time.perf_counter()
-    # each step is one bounded CPU sample of a dynamic snapshot, scaled to the
-    # full workload; the run stops after two minutes of samples
-    for k in range(max(1, args.steps)):
-        info = cpu_sample(cfg, snaps, sources)
-        vals.append(info["edges"] / info["seconds_per_snapshot"])
-        if time.perf_counter() - t0 > 120:
-            break
-    v = statistics.median(vals)
+    from oracle import native
+    cfg, snaps, sources = workload(args, generator=native)
+    info = cpu_sample(cfg, snaps, sources, steps=max(1, args.steps), k=args.cpu_sources)
+    st = info["steps"]
+    rate = [s["edges"] / s["scaled_s"] for s in st]
+    v = float(statistics.median(rate))
+    scaled_ms = [s["scaled_s"] * 1e3 for s in st]
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "edge updates/s",
-            "n_gpus": args.gpus, "steps": len(vals), "warmup": args.warmup,
-            "ms_per_step": info["edges"] / v * 1e3, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32 state / f64 arithmetic",
-            "data": "synthetic (seeded R-MAT)",
-            "config": {"workload": args.workload, "n": cfg["n"], "m": cfg["m"],
-                       "sources": cfg["sources"], "n_parts": cfg["n_parts"]},
+            "n_gpus": args.gpus, "steps": len(st), "warmup": 0,
+            "ms_per_step": float(np.mean([s["wall_s"] for s in st]) * 1e3),
+            "p50_ms": float(np.percentile(scaled_ms, 50)),
+            "p99_ms": float(np.percentile(scaled_ms, 99)),
+            "scaled_ms_per_snapshot": float(np.mean(scaled_ms)),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 PPR state, f64 arithmetic (reference dense path); f64 frPCA and merge",
+            "data": "synthetic (seeded R-MAT from the oracle's generator)",
+            "config": {"workload": cfg["name"], "n": cfg["n"], "m": cfg["m"],
+                       "sources": cfg["sources"], "n_parts": cfg["n_parts"],
+                       "rank_d": cfg["rank_d"], "snapshots": cfg["snapshots"]},
+            "stage_s_mean": {k: float(np.mean([s[k] for s in st]))
+                             for k in ("insert_s", "push_s", "log_s", "frpca_block_s", "merge_s")},
             "cpu_baseline": {"value": v, "unit": "edge updates/s", "cores": info["threads"],
-                             "kind": "port", "sample": info["sample"]},
+                             "kind": info["kind"], "sample": info["sample"]},
             "e2e": {"value": v, "unit": "edge updates/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
 
-# DRAM bytes (read + write) of push_kernel + push_heavy_kernel per pushed
-# item-neighbour (one 256-byte residue-run atomic), from one ncu capture of
-# every push launch of a timed rmat-d-2.7m snapshot (dram__bytes_read.sum +
-# dram__bytes_write.sum, one pass): 2443.6 GB over 7.615e9 item-neighbours,
-# one 256-byte run atomic each (profiles/push_kernel_rmat-d-2.7m.md).
-# `traffic` scales it to the launches of the run being reported.
-PUSH_TRAFFIC_BYTES_PER_ITEM_EDGE = 320.9
-
-
+# --------------------------------------------------------------- roofline
 def push_roofline(stages):
     """Roofline of the dominant kernels (push_kernel + push_heavy_kernel) over
     the timed steps, duration from CUDA events around every launch on the
     session stream.
 
-    Algorithmic bytes (`achieved`) follow the per-push work of the reference's
-    FIFO push: per executed push of (v, s) 8 (r_v read) + 8 (r_v write) + 16
-    (p_v read-modify-write) + 8 (row offsets), and per edge update 4
-    (neighbour id) + 16 (r_u atomic read-modify-write).
+    `achieved` counts the bytes of the reference's FIFO push at the width the
+    state is stored in (fp32 residue and reserve): per executed push of (v, s)
+    4 (r_v read) + 4 (r_v write) + 8 (p_v read-modify-write) + 8 (row offsets),
+    and per edge update 4 (neighbour id) + 8 (r_u read-modify-write).
 
     `achieved_min` counts the bytes this design has to move at least: per lane
     push 16 (fp32 residue exchange + reserve update), per lane edge update 8
     (fp32 atomic read-modify-write), per item-neighbour 4 (the neighbour id is
-    read once for the 64 sources of a chunk), per item 20 (frontier entry, row start,
-    degree)."""
+    read once for the 64 sources of a chunk), per item 20 (frontier entry, row
+    start, degree)."""
     pk, _ = peaks()
     peak = float(pk.get("hbm_gbs", 6800.0))
     pushes = sum(s["pushes"] for s in stages)
@@ -351,7 +456,7 @@ def push_roofline(stages):
     iedges = sum(s["push_item_edges"] for s in stages)
     ms = sum(s["ms_push_kernels"] for s in stages)
     launches = sum(2 * s["push_rounds"] for s in stages)
-    byts = 40.0 * pushes + 20.0 * upd
+    byts = 24.0 * pushes + 12.0 * upd
     byts_min = 16.0 * pushes + 8.0 * upd + 4.0 * iedges + 20.0 * items
     sec = ms / 1e3
     achieved = byts / sec / 1e9 if ms > 0 else 0.0
@@ -367,6 +472,14 @@ def push_roofline(stages):
             "launches": launches, "kernel_ms": ms,
             "lanes_per_item": pushes / max(1, items),
             "peak_source": "MEASURED_PEAKS.json hbm_gbs (copy bandwidth), of measured"}
+
+
+# DRAM bytes (read + write) of push_kernel + push_heavy_kernel per pushed
+# item-neighbour (one 256-byte residue-run atomic), measured by ncu
+# (dram__bytes_read.sum + dram__bytes_write.sum) over the push launches of
+# one dynamic snapshot of a small directed case whose state exceeds L2,
+# scaled per launch by the item-neighbours the run reports.
+PUSH_TRAFFIC_BYTES_PER_ITEM_EDGE = 320.9
 
 
 def aggregate(ms, edges, device=None):
@@ -410,20 +523,23 @@ def main():
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32 PPR state, f16 x (f16 hi+lo) tensor products, f32/f64 small solves",
             "data": "synthetic (seeded R-MAT, inputs resident in HBM; state >> L2)",
-            "config": {"workload": args.workload, "n": cfg["n"], "m": cfg["m"],
+            "config": {"workload": cfg["name"], "n": cfg["n"], "m": cfg["m"],
                        "directed": cfg["directed"], "sources": cfg["sources"],
                        "n_parts": cfg["n_parts"], "rank_d": cfg["rank_d"],
                        "hierarchy_n": cfg["hierarchy_n"],
                        "passes_q": cfg["passes_q"], "snapshots": cfg["snapshots"],
+                       "edges_per_step": res["edges"] / args.steps,
                        "l2": "working set (PPR state) larger than L2",
                        "parallelism": "replicas x%d" % world,
-                       "ppr_reserve": "pinned host memory" if args.host_reserve else "HBM",
+                       "ppr_reserve": "pinned host memory" if host_reserve(args, cfg) else "HBM",
                        "driver": ("tsvd_session_run: factor stage of snapshot k overlapped "
                                   "with the push of k+1") if args.pipelined
                        else "tsvd_session_step per snapshot"},
+            "setup_s": res["setup_s"],
             "clocks": res["clocks"], "gpu_launches": res["launches"],
             "stage_ms_mean": {k: float(np.mean([s[k] for s in res["stages"]]))
-                              for k in ("ms_insert", "ms_push", "ms_log", "ms_frpca", "ms_merge")},
+                              for k in ("ms_insert", "ms_refresh", "ms_push", "ms_log",
+                                        "ms_frpca", "ms_merge")},
             "push_rounds_mean": float(np.mean([s["push_rounds"] for s in res["stages"]])),
             "pushes_mean": float(np.mean([s["pushes"] for s in res["stages"]])),
             "push_edge_updates_mean": float(np.mean([s["push_edge_updates"] for s in res["stages"]])),
@@ -436,15 +552,19 @@ def main():
             "eig_refine_sweeps_max": int(max(s["eig_refine_sweeps"] for s in res["stages"]))}
     line["roofline"] = push_roofline(res["stages"])
     if "e2e_ms" in res:
-        line["e2e"] = {"value": edges_all / (res["e2e_ms"] / 1e3), "unit": "edge updates/s",
+        line["e2e"] = {"value": res["e2e_edges"] * world / (res["e2e_ms"] / 1e3),
+                       "unit": "edge updates/s", "steps": res["e2e_steps"],
                        "h2d_bytes_per_step": res["h2d"], "d2h_bytes_per_step": res["d2h"],
                        "p50_ms": float(np.percentile(res["e2e_lat"], 50)),
-                       "p99_ms": float(np.percentile(res["e2e_lat"], 99))}
+                       "p99_ms": float(np.percentile(res["e2e_lat"], 99)),
+                       "deltas": "the %d deltas after the timed ones, same session"
+                                 % res["e2e_steps"]}
     if rank == 0 and not args.no_cpu:
-        info = cpu_sample(cfg, snaps, sources)
-        cv = info["edges"] / info["seconds_per_snapshot"]
-        line["cpu_baseline"] = {"value": cv, "unit": "edge updates/s", "cores": info["threads"],
-                                "kind": "port", "sample": info["sample"]}
+        info = cpu_sample(cfg, snaps, sources, steps=1, k=args.cpu_sources)
+        s0 = info["steps"][0]
+        line["cpu_baseline"] = {"value": s0["edges"] / s0["scaled_s"], "unit": "edge updates/s",
+                                "cores": info["threads"], "kind": info["kind"],
+                                "sample": info["sample"], "sample_wall_s": s0["wall_s"]}
     if rank == 0:
         print(json.dumps(line))
     if dist:

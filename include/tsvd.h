@@ -98,16 +98,20 @@ tsvd_status tsvd_frpca(int32_t nrows, int32_t ncols, int64_t nnz,
                        int32_t q, uint64_t seed, double *U, double *S,
                        double *V);
 
-/* Same computation and arguments as tsvd_frpca, but it allocates nothing:
- * for callers that may not call cudaMalloc (code inside a stream capture,
- * plug-ins whose host application owns the device memory pool, loops that
- * must stay off the allocator). No counterpart in the reference. All device
+/* Same computation and arguments as tsvd_frpca, but it allocates nothing.
+ * No counterpart in the reference. For callers that cannot call cudaMalloc:
+ * plug-ins inside a host application that reserves the device memory pool
+ * for its own allocator, and latency-bound host loops that must stay off the
+ * allocator (cudaMalloc/cudaFree can synchronize the device). All device
  * scratch is one static array of about 11 MB that every GPU loading this
  * library keeps until process exit; host staging is static too. Limits:
  * nrows <= 512, ncols <= 16384, <= 2048 non-empty columns, nnz <= 262144,
- * k <= 64; larger inputs return TSVD_ERR_INVALID. The first call on a device
- * resolves the array's address (make it before any stream capture). Calls
- * share the array, so calls that overlap on the GPU race. */
+ * k <= 64, |values| <= FLT_MAX; larger inputs return TSVD_ERR_INVALID. The
+ * call is synchronous: it runs on the legacy default stream (ordered with
+ * the caller's blocking streams), reads a count back to the host midway and
+ * returns with the results in U, S, V. The first call on a device resolves
+ * the array's address (make it before any stream capture). Calls share the
+ * array, so calls that overlap on the GPU race. */
 tsvd_status tsvd_frpca_noalloc(int32_t nrows, int32_t ncols, int64_t nnz,
                                const int64_t *row_ptr, const int32_t *col_idx,
                                const double *values, int32_t index_base,

@@ -3,5 +3,5 @@
 set -e
 HERE=$(cd "$(dirname "$0")" && pwd)
 ${CC:-gcc} -O2 -ffp-contract=off -fPIC -shared -pthread -std=gnu99 \
-  "$HERE/oracle_ppr.c" -o "$HERE/liboracle_ppr.so" -lm
+  "$HERE/oracle_ppr.c" "$HERE/oracle_synth.c" -o "$HERE/liboracle_ppr.so" -lm
 echo "built $HERE/liboracle_ppr.so"

@@ -11,7 +11,9 @@
  * the Gaussian test matrices) is ignored, so runs repeat, and the last
  * Gaussian draw is kept for tsvd_ref_last_gaussian(). */
 #include <math.h>
+#include <pthread.h>
 #include <stdint.h>
+#include <unistd.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -24,25 +26,79 @@ static void scale_c(const MKL_INT rows, const MKL_INT n, const double beta, doub
     for (MKL_INT i = 0; i < rows; ++i) c[i + (size_t)j * ldc] = beta == 0.0 ? 0.0 : beta * c[i + (size_t)j * ldc];
 }
 
+/* MKL runs this product on every core; so does the stand-in (threads =
+ * TSVD_REF_THREADS, default: all online cores). B is first copied row-major
+ * so that each stored entry of A reads one contiguous row of B. Without
+ * transpose, threads take contiguous row ranges of C; with it (C = A^T B),
+ * each thread accumulates its rows of A into a private k x n buffer and the
+ * buffers are summed. */
+typedef struct {
+  int trans;
+  MKL_INT m, n, k, r0, r1;
+  double alpha;
+  const double *val, *bt;
+  const MKL_INT *indx, *pntrb, *pntre;
+  double *acc;   /* row-major: m x n (no transpose: rows r0..r1) or k x n (private) */
+} csrmm_job;
+
+static void *csrmm_run(void *arg) {
+  csrmm_job *J = (csrmm_job *)arg;
+  const MKL_INT n = J->n;
+  for (MKL_INT i = J->r0; i < J->r1; ++i)
+    for (MKL_INT p = J->pntrb[i] - 1; p < J->pntre[i] - 1; ++p) {
+      const MKL_INT col = J->indx[p] - 1;
+      const double a = J->alpha * J->val[p];
+      double *dst = J->trans ? J->acc + (size_t)col * n : J->acc + (size_t)i * n;
+      const double *src = J->trans ? J->bt + (size_t)i * n : J->bt + (size_t)col * n;
+      for (MKL_INT j = 0; j < n; ++j) dst[j] += a * src[j];
+    }
+  return NULL;
+}
+
+static int shim_threads(void) {
+  const char *e = getenv("TSVD_REF_THREADS");
+  long t = e ? atol(e) : sysconf(_SC_NPROCESSORS_ONLN);
+  return t < 1 ? 1 : (t > 256 ? 256 : (int)t);
+}
+
 void mkl_dcsrmm(const char *transa, const MKL_INT *m, const MKL_INT *n, const MKL_INT *k,
                 const double *alpha, const char *matdescra, const double *val,
                 const MKL_INT *indx, const MKL_INT *pntrb, const MKL_INT *pntre, const double *b,
                 const MKL_INT *ldb, const double *beta, double *c, const MKL_INT *ldc) {
   (void)matdescra;
   const int trans = transa[0] == 'T' || transa[0] == 't';
-  const MKL_INT out_rows = trans ? *k : *m;
-  scale_c(out_rows, *n, *beta, c, *ldc);
-  for (MKL_INT i = 0; i < *m; ++i)
-    for (MKL_INT p = pntrb[i] - 1; p < pntre[i] - 1; ++p) {
-      const MKL_INT col = indx[p] - 1;
-      const double a = *alpha * val[p];
-      for (MKL_INT j = 0; j < *n; ++j) {
-        if (trans)
-          c[col + (size_t)j * *ldc] += a * b[i + (size_t)j * *ldb];
-        else
-          c[i + (size_t)j * *ldc] += a * b[col + (size_t)j * *ldb];
-      }
+  const MKL_INT out_rows = trans ? *k : *m, in_rows = trans ? *m : *k, nc = *n;
+  scale_c(out_rows, nc, *beta, c, *ldc);
+  double *bt = (double *)malloc(sizeof(double) * (size_t)in_rows * nc + 8);
+  for (MKL_INT j = 0; j < nc; ++j)
+    for (MKL_INT i = 0; i < in_rows; ++i) bt[(size_t)i * nc + j] = b[i + (size_t)j * *ldb];
+  int T = shim_threads();
+  if (T > *m) T = *m > 0 ? *m : 1;
+  csrmm_job jobs[256];
+  pthread_t th[256];
+  double *acc = NULL;
+  if (!trans) acc = (double *)calloc((size_t)*m * nc + 1, sizeof(double));
+  for (int t = 0; t < T; ++t) {
+    csrmm_job J = {trans, *m, nc, *k, (MKL_INT)((long long)*m * t / T),
+                   (MKL_INT)((long long)*m * (t + 1) / T), *alpha, val, bt, indx, pntrb, pntre,
+                   trans ? (double *)calloc((size_t)*k * nc + 1, sizeof(double)) : acc};
+    jobs[t] = J;
+    pthread_create(&th[t], NULL, csrmm_run, &jobs[t]);
+  }
+  for (int t = 0; t < T; ++t) pthread_join(th[t], NULL);
+  for (MKL_INT i = 0; i < out_rows; ++i)
+    for (MKL_INT j = 0; j < nc; ++j) {
+      double x = 0.0;
+      if (trans)
+        for (int t = 0; t < T; ++t) x += jobs[t].acc[(size_t)i * nc + j];
+      else
+        x = acc[(size_t)i * nc + j];
+      c[i + (size_t)j * *ldc] += x;
     }
+  if (trans)
+    for (int t = 0; t < T; ++t) free(jobs[t].acc);
+  free(acc);
+  free(bt);
 }
 
 void mkl_dcoomm(const char *transa, const MKL_INT *m, const MKL_INT *n, const MKL_INT *k,

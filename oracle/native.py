@@ -67,8 +67,52 @@ def lib():
                                      ctypes.c_double, ctypes.c_int32, ctypes.c_int32]
         L.or_ppr_push.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32,
                                   ctypes.c_double, ctypes.c_double, ctypes.c_int32]
+        L.or_rmat_edges.restype = ctypes.c_int
+        L.or_rmat_edges.argtypes = [ctypes.c_int32, ctypes.c_int64, ctypes.c_double,
+                                    ctypes.c_double, ctypes.c_double, ctypes.c_int32,
+                                    ctypes.c_uint64, ctypes.c_int32, _i32p]
+        L.or_sample_sources.restype = ctypes.c_int
+        L.or_sample_sources.argtypes = [ctypes.c_int32, _i32p, ctypes.c_int64, ctypes.c_int32,
+                                        ctypes.c_uint64, _i32p]
+        L.or_write_edges_text.restype = ctypes.c_int
+        L.or_write_edges_text.argtypes = [ctypes.c_char_p, _i32p, ctypes.c_int64]
         _lib = L
     return _lib
+
+
+def rmat_edges(n, m, a=0.57, b=0.19, c=0.19, directed=True, seed=20231, threads=None):
+    """The seeded R-MAT edge list (m x 2 int32, timestamp order) drawn by the
+    oracle's own generator (oracle_synth.c); identical to the product's."""
+    out = np.zeros((int(m), 2), np.int32)
+    rc = lib().or_rmat_edges(int(n), int(m), a, b, c, int(bool(directed)), int(seed),
+                             int(threads or os.cpu_count() or 1), _ptr(out, _i32p))
+    if rc != 0:
+        raise RuntimeError("or_rmat_edges failed (%d)" % rc)
+    return out
+
+
+def snapshot_sizes(m, count, first_frac):
+    """First snapshot round(first_frac * m) edges, the rest split evenly (the
+    earlier deltas take the remainder)."""
+    first = m if count == 1 else int(np.floor(first_frac * m + 0.5))
+    rest = m - first
+    k = count - 1
+    return [first] + [rest // k + (1 if i < rest % k else 0) for i in range(k)]
+
+
+def sample_sources(n, edges, k, seed=20231):
+    e = np.ascontiguousarray(edges, np.int32)
+    out = np.zeros(int(k), np.int32)
+    if lib().or_sample_sources(int(n), _ptr(e, _i32p), len(e), int(k), int(seed),
+                               _ptr(out, _i32p)) != 0:
+        raise RuntimeError("or_sample_sources failed")
+    return out
+
+
+def write_edges_text(path, edges):
+    e = np.ascontiguousarray(edges, np.int32)
+    if lib().or_write_edges_text(path.encode(), _ptr(e, _i32p), len(e)) != 0:
+        raise OSError("cannot write %s" % path)
 
 
 class OracleGraph:
@@ -162,6 +206,10 @@ def ref_lib():
         L.ref_ppr_dense.argtypes = [ctypes.c_void_p, _f64p]
         L.ref_log_blocks.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                      ctypes.c_double, _f64p, _f64p, _i32p, _i64p]
+        L.ref_ppr_step_mt.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                      ctypes.c_int, ctypes.c_int, ctypes.c_int]
+        L.ref_block_csr.restype = ctypes.c_longlong
+        L.ref_block_csr.argtypes = [ctypes.c_void_p, ctypes.c_int, _i32p, _i32p, _f64p]
         _ref = L
     return _ref
 
@@ -219,8 +267,30 @@ class RefPPR:
             ref_lib().ref_ppr_free(self.h)
             self.h = None
 
-    def step(self, g, transpose, iter, dyn_start):
-        ref_lib().ref_ppr_step(self.h, g.h, int(transpose), iter, dyn_start)
+    def step(self, g, transpose, iter, dyn_start, threads=1):
+        """Refresh + push of every source; threads > 1 splits the sources into
+        contiguous ranges, one std::thread each, as the reference's drivers do."""
+        if threads > 1:
+            ref_lib().ref_ppr_step_mt(self.h, g.h, int(transpose), iter, dyn_start, int(threads))
+        else:
+            ref_lib().ref_ppr_step(self.h, g.h, int(transpose), iter, dyn_start)
+
+    def log_only(self, iter, delta, resid, lp=False):
+        """The reference's log transform + lazy test of every block, without
+        copying anything out (for timing)."""
+        r = np.ascontiguousarray(resid, np.float64)
+        ref_lib().ref_log_blocks(self.h, int(lp), 1, int(iter), float(delta), _ptr(r, _f64p),
+                                 None, None, None)
+
+    def block_csr(self, b):
+        """Block b's accepted log matrix (|S| x cols) as (indptr, indices, data)."""
+        L = ref_lib()
+        nnz = L.ref_block_csr(self.h, int(b), None, None, None)
+        rp = np.zeros(self.s + 1, np.int32)
+        ci = np.zeros(max(nnz, 1), np.int32)
+        va = np.zeros(max(nnz, 1), np.float64)
+        L.ref_block_csr(self.h, int(b), _ptr(rp, _i32p), _ptr(ci, _i32p), _ptr(va, _f64p))
+        return rp, ci[:nnz], va[:nnz]
 
     def state(self, which):
         out = np.zeros((self.s, self.n), np.float32)

@@ -25,6 +25,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <thread>
 #include <unordered_map>
 #include <vector>
 
@@ -321,6 +322,51 @@ void ref_ppr_step(void *sp, void *gp, int transpose, int iter, int dyn_start) {
   }
 }
 
+// The same refresh + push, the way the reference's drivers run it
+// (Code/Tree_u_NC.cpp:566-640): `threads` std::threads, each calling the
+// entry points on its own contiguous range of sources.
+void ref_ppr_step_mt(void *sp, void *gp, int transpose, int iter, int dyn_start, int threads) {
+  RefPPR *st = (RefPPR *)sp;
+  RefGraph *g = (RefGraph *)gp;
+  const int S = st->S;
+  if (threads < 1) threads = 1;
+  if (threads > S) threads = S;
+  float **r = st->r.data(), **p = st->p.data();
+  bool **fl = st->flags.data();
+  Queue *q = st->queues.data();
+  vector<std::thread> pool;
+  for (int t = 0; t < threads; ++t) {
+    const int a = (int)((long long)S * t / threads), b = (int)((long long)S * (t + 1) / threads);
+    pool.emplace_back([=]() {
+      if (!g->directed) {
+        nodegree_DenseUndirected_Refresh_PPR_initialization(
+            a, b, g->ug, st->rmax, st->alpha, st->sources, r, p, fl, q, iter, st->n,
+            st->col_dim, st->nparts, st->inner, &st->tree, st->row_index, st->indicator,
+            dyn_start);
+        nodegree_DenseDynamicForwardPush(a, b, g->ug, st->rmax, st->alpha, st->sources, r, p,
+                                         fl, q, st->row_index, st->col_dim, st->nparts,
+                                         &st->tree, st->inner, st->indicator);
+      } else if (!transpose) {
+        nodegree_DenseDirected_Refresh_PPR_initialization(
+            a, b, g->dg, st->rmax, st->rmax, st->alpha, st->sources, r, p, fl, q, st->col_dim,
+            st->nparts, st->inner, iter, st->n, &st->tree, dyn_start);
+        nodegree_DenseDirectedDynamicForwardPush(a, b, g->dg, st->rmax, st->rmax, st->alpha,
+                                                 st->sources, r, p, fl, q, st->col_dim,
+                                                 st->nparts, st->inner, &st->tree);
+      } else {
+        nodegree_DenseDirected_Refresh_PPR_initialization_Transpose(
+            a, b, g->dg, st->rmax, st->rmax, st->alpha, st->sources, r, p, fl, q, st->col_dim,
+            st->nparts, st->inner, iter, st->n, &st->tree, dyn_start);
+        nodegree_DenseDirectedDynamicForwardPushTranspose(a, b, g->dg, st->rmax, st->rmax,
+                                                          st->alpha, st->sources, r, p, fl, q,
+                                                          st->col_dim, st->nparts, st->inner,
+                                                          &st->tree);
+      }
+    });
+  }
+  for (auto &th : pool) th.join();
+}
+
 // which: 0 residue, 1 reserve (|S| x N floats).
 void ref_ppr_state(void *sp, int which, float *out) {
   RefPPR *st = (RefPPR *)sp;
@@ -372,15 +418,36 @@ void ref_log_blocks(void *sp, int lp, int with_norm, int iter, double delta,
                                                       delta, st->S, 0, st->nnz_record);
     }
   }
-  memset(accepted, 0, sizeof(double) * (size_t)st->S * st->n);
+  if (accepted) memset(accepted, 0, sizeof(double) * (size_t)st->S * st->n);
   for (int b = 0; b < P; ++b) {
     SparseMatrix<double, 0, int> &m = t.mat_mapping[b];
-    for (int j = 0; j < m.ncols; ++j)
-      for (int q = m.outer[j]; q < m.outer[j + 1]; ++q)
-        accepted[(size_t)m.inner[q] * st->n + (size_t)b * st->col_dim + j] = m.val[q];
-    record[b] = upd[b];
-    nnz[b] = st->nnz_record[b];
+    if (accepted)
+      for (int j = 0; j < m.ncols; ++j)
+        for (int q = m.outer[j]; q < m.outer[j + 1]; ++q)
+          accepted[(size_t)m.inner[q] * st->n + (size_t)b * st->col_dim + j] = m.val[q];
+    if (record) record[b] = upd[b];
+    if (nnz) nnz[b] = st->nnz_record[b];
   }
+}
+
+// Block b's accepted log matrix (mat_mapping[b], |S| x cols) as 0-based CSR:
+// with null outputs, returns the entry count only.
+long long ref_block_csr(void *sp, int b, int *rowptr, int *cols, double *vals) {
+  RefPPR *st = (RefPPR *)sp;
+  SparseMatrix<double, 0, int> &m = st->tree.mat_mapping[b];
+  const long long nnz = (long long)m.val.size();
+  if (!rowptr) return nnz;
+  vector<int> cnt((size_t)st->S + 1, 0);
+  for (int q = 0; q < (int)nnz; ++q) cnt[(size_t)m.inner[q] + 1]++;
+  for (int i = 0; i < st->S; ++i) cnt[i + 1] += cnt[i];
+  memcpy(rowptr, cnt.data(), sizeof(int) * ((size_t)st->S + 1));
+  for (int j = 0; j < m.ncols; ++j)
+    for (int q = m.outer[j]; q < m.outer[j + 1]; ++q) {
+      const int pos = cnt[m.inner[q]]++;
+      cols[pos] = j;
+      vals[pos] = m.val[q];
+    }
+  return nnz;
 }
 
 }  // extern "C"

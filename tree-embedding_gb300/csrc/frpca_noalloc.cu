@@ -1,23 +1,32 @@
 // tsvd_frpca_noalloc: tsvd_frpca without any allocation.
 //
-// For callers that cannot allocate device memory: code running while a CUDA
-// stream is being captured into a graph (cudaMalloc is not capturable and
-// would invalidate the capture), plug-ins living inside a host application
-// that owns the whole device memory pool, or real-time loops that must not hit
-// the allocator. Every buffer the randomized SVD needs lives in one
+// For callers that cannot allocate device memory: plug-ins living inside a
+// host application that reserves the whole device memory pool for itself
+// (its own allocator hands out every byte, so a cudaMalloc of ours fails or
+// steals from it), and latency-bound host loops that must not go through the
+// allocator (cudaMalloc and cudaFree can synchronize the device and stall the
+// caller's other streams). Every buffer the randomized SVD needs lives in one
 // file-scope __device__ array (g_noalloc_scratch, kNoallocScratchBytes bytes,
 // held by every GPU that loads this library until the process exits), and
 // every host-side staging buffer is a file-scope array as well. Inputs and
 // outputs are the caller's, exactly as for tsvd_frpca.
 //
+// The call is synchronous: it runs on the legacy default stream (stream 0,
+// so it is ordered with the caller's blocking streams), reads the count of
+// non-empty columns back to the host midway, and returns once the results
+// are in the caller's buffers.
+//
 // Limits (larger inputs are rejected with TSVD_ERR_INVALID before any GPU
 // work): nrows <= 512, ncols <= 16384, at most 2048 non-empty columns,
-// nnz <= 262144, k <= 64 (q is free).
+// nnz <= 262144, k <= 64 (q is free), |values| <= FLT_MAX.
 //
 // Set-up: the first call on a device, with that device current, resolves the
-// array's device address once (cudaGetSymbolAddress); make that first call
-// before any stream capture. Calls share the array: two calls that overlap on
-// the GPU (from several host threads, or on several streams) race.
+// array's device address once (cudaGetSymbolAddress) and checks that the
+// regions reserved for the Gram and Jacobi work areas hold what the kernels
+// ask for at the limits; make that first call before any stream capture.
+// Calls share the array: two calls that overlap on the GPU (from several host
+// threads, or on several streams) race.
+#include <cfloat>
 #include <cmath>
 #include <cstring>
 
@@ -112,15 +121,18 @@ int32_t g_hcmap[kNaMaxUsedCols];
 constexpr int kMaxDevices = 64;
 unsigned char *g_dev_scratch[kMaxDevices] = {nullptr};
 
-// misc: [0] max |value| as float bits, [1] non-empty column count
+// misc: [0..1] max |value| as the bits of a double (non-negative doubles
+// order like their bit patterns, so an integer maximum finds the largest
+// magnitude exactly as tsvd_frpca's host loop does), [2] non-empty columns
 __global__ void na_mark_kernel(const int64_t *row_ptr, const int32_t *col, const double *val,
                                int nrows, int32_t *cinv, uint32_t *misc) {
+  unsigned long long *vmax_bits = reinterpret_cast<unsigned long long *>(misc);
   for (int i = blockIdx.x; i < nrows; i += gridDim.x)
     for (int64_t t = row_ptr[i] + threadIdx.x; t < row_ptr[i + 1]; t += blockDim.x) {
       double v = val[t];
       if (v == 0.0) continue;
       cinv[col[t]] = 1;
-      atomicMax(&misc[0], __float_as_uint(fabsf((float)v)));
+      atomicMax(vmax_bits, (unsigned long long)__double_as_longlong(fabs(v)));
     }
 }
 
@@ -163,7 +175,7 @@ __global__ void na_compact_kernel(int32_t *cinv, int ncols, int32_t *cmap, uint3
     if (threadIdx.x == 0) base += total;
     __syncthreads();
   }
-  if (threadIdx.x == 0) misc[1] = (uint32_t)base;
+  if (threadIdx.x == 0) misc[2] = (uint32_t)base;
 }
 
 __global__ void na_densify_kernel(const int64_t *row_ptr, const int32_t *col, const double *val,
@@ -183,14 +195,18 @@ tsvd_status scratch_for_current_device(unsigned char **out) {
   TSVD_CUDA(cudaGetDevice(&dev));
   if (dev < 0 || dev >= kMaxDevices) return fail(TSVD_ERR_INVALID, "device %d", dev);
   if (!g_dev_scratch[dev]) {
+    // the fixed regions must hold what the shared kernels ask for at the limits
+    const size_t gram_need = gram_work_bytes(std::max(kNaMaxUsedCols, kNaMaxRows), kNaMaxL, 1);
+    const size_t jac_need = jacobi_work_bytes(kNaMaxL, 1);
+    if (gram_need > kGramB || jac_need > kJacB)
+      return fail(TSVD_ERR_STATE,
+                  "frpca_noalloc: static scratch too small for the kernels (Gram %zu > %zu or "
+                  "Jacobi %zu > %zu bytes)", gram_need, kGramB, jac_need, kJacB);
     void *p = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess || !p)
       return fail(TSVD_ERR_DEVICE, "cudaGetSymbolAddress(g_noalloc_scratch): %s",
                   cudaGetErrorString(e));
-    // the refinement's pointer array (one problem) never changes: set it now
-    double *dh = (double *)((unsigned char *)p + kOffDh);
-    TSVD_CUDA(cudaMemcpy((unsigned char *)p + kOffHp, &dh, sizeof(dh), cudaMemcpyHostToDevice));
     g_dev_scratch[dev] = (unsigned char *)p;
   }
   *out = g_dev_scratch[dev];
@@ -223,6 +239,8 @@ extern "C" tsvd_status tsvd_frpca_noalloc(int32_t nrows, int32_t ncols, int64_t 
     int32_t c = col_idx[t] - index_base;
     if (c < 0 || c >= ncols) return fail(TSVD_ERR_INVALID, "frpca_noalloc: column out of range");
     if (!std::isfinite(values[t])) return fail(TSVD_ERR_NUMERIC, "frpca_noalloc: non-finite value");
+    if (std::fabs(values[t]) > (double)FLT_MAX)
+      return fail(TSVD_ERR_INVALID, "frpca_noalloc: |value| above the float range");
   }
   unsigned char *base = nullptr;
   TSVD_TRY(scratch_for_current_device(&base));
@@ -244,6 +262,17 @@ extern "C" tsvd_status tsvd_frpca_noalloc(int32_t nrows, int32_t ncols, int64_t 
   // the array keeps the previous call's contents: clear what must start at 0
   TSVD_CUDA(cudaMemsetAsync(d_cinv, 0, sizeof(int32_t) * ncols, st));
   TSVD_CUDA(cudaMemsetAsync(d_misc, 0, kMiscB, st));
+  {
+    // the fp64 refinement reads its matrix through a one-entry pointer array
+    // in the scratch: written on every call, so the array never relies on
+    // what an earlier call (or an earlier context) left there
+    static double *dh_host[kMaxDevices];
+    int dev = 0;
+    TSVD_CUDA(cudaGetDevice(&dev));
+    dh_host[dev] = (double *)(base + kOffDh);
+    TSVD_CUDA(cudaMemcpyAsync(base + kOffHp, &dh_host[dev], sizeof(double *),
+                              cudaMemcpyHostToDevice, st));
+  }
   TSVD_CUDA(cudaMemsetAsync(base + kOffAt, 0, kAtB, st));
   const int grid = std::min(nrows, 4 * sm_count());
   if (index_base == 1) {  // rebase the copied indices to 0
@@ -254,16 +283,16 @@ extern "C" tsvd_status tsvd_frpca_noalloc(int32_t nrows, int32_t ncols, int64_t 
   TSVD_LAUNCH_CHECK();
   na_compact_kernel<<<1, 1024, 0, st>>>(d_cinv, ncols, d_cmap, d_misc);
   TSVD_LAUNCH_CHECK();
-  uint32_t hmisc[2];
+  uint32_t hmisc[4];
   TSVD_CUDA(cudaMemcpyAsync(hmisc, d_misc, sizeof hmisc, cudaMemcpyDeviceToHost, st));
   TSVD_CUDA(cudaStreamSynchronize(st));
-  const int32_t nc = (int32_t)hmisc[1];
+  const int32_t nc = (int32_t)hmisc[2];
   if (nc > kNaMaxUsedCols)
     return fail(TSVD_ERR_INVALID, "frpca_noalloc: %d non-empty columns > %d", nc, kNaMaxUsedCols);
-  float vmax;
-  std::memcpy(&vmax, &hmisc[0], 4);
+  double vmax;
+  std::memcpy(&vmax, &hmisc[0], sizeof vmax);
   int e2 = 0;
-  if (vmax > 0) std::frexp((double)vmax, &e2);
+  if (vmax > 0) std::frexp(vmax, &e2);
   const double scale = std::ldexp(1.0, 14 - e2);
   if (nc > 0) {
     na_densify_kernel<<<grid, 128, 0, st>>>(d_rp, d_col, d_val, nrows, d_cinv, sp, (float)scale,

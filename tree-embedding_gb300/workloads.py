@@ -5,32 +5,50 @@ Each config follows one of the five workload descriptions of the build
 random timestamps split into a first snapshot plus equal deltas). The graphs
 take their vertex and edge counts from the reference README's dataset table
 (Patent, Wikipedia, YouTube/Flickr, Twitter); no dataset content is used.
+
+This module does not load the library by itself: `build` draws the inputs
+with the generator module it is given (the library's binding by default; the
+CPU reference arm passes the oracle's own generator, which gives the same
+bytes without the library).
 """
 import numpy as np
 
-import tsvd_gb300 as T
+# values of the TSVD_TRANSFORM_* and TSVD_DIRTY_* constants of include/tsvd.h
+TRANSFORM_LOG10_NC, TRANSFORM_LOG10_LP, TRANSFORM_LN_N = 0, 1, 2
+DIRTY_REFERENCE, DIRTY_FROBENIUS, DIRTY_ALL = 0, 1, 2
 
 CONFIGS = {
     # Plain method, CPU-runnable (undirected, N=1e5, M=1e6, 10 snapshots).
     "rmat-u-100k": dict(n=100_000, m=1_000_000, directed=False, snapshots=10, first=0.5,
-                        sources=500, alpha=0.2, rmax=1e-6, transform=T.TRANSFORM_LN_N,
+                        sources=500, alpha=0.2, rmax=1e-6, transform=TRANSFORM_LN_N,
                         n_parts=16, hierarchy_n=2, rank_d=128, passes_q=6,
-                        dirty_rule=T.DIRTY_REFERENCE, delta=0.3),
+                        dirty_rule=DIRTY_REFERENCE, delta=0.3),
     # Plain GPU form (directed, Patent-sized, 20 snapshots).
     "rmat-d-2.7m": dict(n=2_738_013, m=13_960_811, directed=True, snapshots=20, first=0.5,
-                        sources=3000, alpha=0.2, rmax=1e-7, transform=T.TRANSFORM_LOG10_NC,
+                        sources=3000, alpha=0.2, rmax=1e-7, transform=TRANSFORM_LOG10_NC,
                         n_parts=64, hierarchy_n=2, rank_d=128, passes_q=6,
-                        dirty_rule=T.DIRTY_FROBENIUS, dirty_frac=0.01, delta=0.3),
+                        dirty_rule=DIRTY_FROBENIUS, dirty_frac=0.01, delta=0.3),
     # Precision form (directed, Wikipedia-sized, 10 snapshots, first 70%).
+    # Its PPR state (16 N Sp bytes = 305 GB) exceeds HBM: the reserve half
+    # lives in pinned host memory.
     "rmat-d-6.2m": dict(n=6_216_199, m=177_862_656, directed=True, snapshots=10, first=0.7,
-                        sources=3000, alpha=0.2, rmax=1e-7, transform=T.TRANSFORM_LOG10_NC,
+                        sources=3000, alpha=0.2, rmax=1e-7, transform=TRANSFORM_LOG10_NC,
                         n_parts=128, hierarchy_n=2, rank_d=128, passes_q=6,
-                        dirty_rule=T.DIRTY_FROBENIUS, dirty_frac=0.01, delta=0.3),
+                        dirty_rule=DIRTY_FROBENIUS, dirty_frac=0.01, delta=0.3,
+                        host_reserve=True),
+    # The same graph refreshed by 1%-insertion snapshots (1.78M edges each)
+    # after a 70 % first snapshot: 30 deltas.
+    "rmat-d-6.2m-1pct": dict(n=6_216_199, m=177_862_656, directed=True, snapshots=31,
+                             first=0.7, sources=3000, alpha=0.2, rmax=1e-7,
+                             transform=TRANSFORM_LOG10_NC, n_parts=128, hierarchy_n=2,
+                             rank_d=128, passes_q=6, dirty_rule=DIRTY_FROBENIUS,
+                             dirty_frac=0.01, delta=0.3, host_reserve=True),
 }
 
 
 def scaled(name, n=None, m=None, sources=None, n_parts=None, rank_d=None, snapshots=None):
     c = dict(CONFIGS[name])
+    c["name"] = name
     for k, v in dict(n=n, m=m, sources=sources, n_parts=n_parts, rank_d=rank_d,
                      snapshots=snapshots).items():
         if v is not None:
@@ -38,13 +56,17 @@ def scaled(name, n=None, m=None, sources=None, n_parts=None, rank_d=None, snapsh
     return c
 
 
-def build(cfg, seed=20231):
-    """Edges (in timestamp order), the snapshot deltas and the source subset."""
-    edges = T.rmat_edges(cfg["n"], cfg["m"], directed=cfg["directed"], seed=seed)
-    sizes = T.snapshot_sizes(len(edges), cfg["snapshots"], cfg["first"])
+def build(cfg, seed=20231, generator=None):
+    """Edges (in timestamp order), the snapshot deltas and the source subset.
+    `generator` provides rmat_edges / snapshot_sizes / sample_sources (the
+    library binding when None)."""
+    if generator is None:
+        import tsvd_gb300 as generator
+    edges = generator.rmat_edges(cfg["n"], cfg["m"], directed=cfg["directed"], seed=seed)
+    sizes = generator.snapshot_sizes(len(edges), cfg["snapshots"], cfg["first"])
     bounds = np.concatenate([[0], np.cumsum(sizes)])
     snaps = [edges[bounds[i]:bounds[i + 1]] for i in range(len(sizes))]
-    sources = T.sample_sources(cfg["n"], snaps[0], cfg["sources"], seed=seed)
+    sources = generator.sample_sources(cfg["n"], snaps[0], cfg["sources"], seed=seed)
     return edges, snaps, sources
 
 
