@@ -74,6 +74,9 @@ def parse():
                          "push of k+1: more snapshots/s, longer per-snapshot latency) instead of "
                          "one tsvd_session_step per snapshot")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-plain", action="store_true",
+                    help="skip the plain-GPU-form leg (same session, the deltas after the e2e leg)")
+    ap.add_argument("--plain-steps", type=int, default=3)
     ap.add_argument("--cpu-sources", type=int, default=None,
                     help="sources in the CPU sample (default: two per host thread)")
     ap.add_argument("--seed", type=int, default=20231)
@@ -171,9 +174,8 @@ def run_ours(args, cfg, snaps, sources, device):
     Every snapshot is complete (embedding written) inside the timed region.
     Per-snapshot latency (stats ms_total) runs from the start of a snapshot's
     insert to the end of its factor stage. The e2e leg continues the same
-    session through tsvd_session_step with host deltas."""
-    import ctypes
-
+    session through tsvd_session_step with host deltas, then the plain-form
+    leg on the deltas after those."""
     import torch
     import tsvd_gb300 as T
     import workloads as W
@@ -217,33 +219,68 @@ def run_ours(args, cfg, snaps, sources, device):
         res.update(ms=ms, wall=wall, per_step=[st["ms_total"] for st in stage], stages=stage,
                    launches=launches, clocks=clk.summary(), edges=int(off[-1]))
         del dev, dev_timed
-        rest = snaps[t1i:t1i + args.steps]
-        if args.no_e2e or not rest:
-            return res
-        # --- end to end through the C-ABI on the deltas that follow: host
-        # pairs (pinned) copied in and the embedding read back every step
-        pinned = [torch.from_numpy(np.ascontiguousarray(e)).pin_memory() for e in rest]
-        L = T.lib()
-        emb = np.zeros((len(rest), len(sources), cfg["rank_d"]), np.float64)
-        stats = (T.StepStats * len(rest))()
-        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        torch.cuda.synchronize(device)
-        i32p, f64p = ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_double)
-        ev0.record(stream)
-        for k, e in enumerate(pinned):
-            T._check(L.tsvd_session_step(s._h, ctypes.cast(e.data_ptr(), i32p), len(rest[k])))
-            T._check(L.tsvd_session_embedding(s._h, emb[k].ctypes.data_as(f64p)))
-            T._check(L.tsvd_session_last_stats(s._h, ctypes.byref(stats[k])))
-        ev1.record(stream)
-        torch.cuda.synchronize(device)
-        assert np.isfinite(emb).all()
-        res["e2e_ms"] = ev0.elapsed_time(ev1)
-        res["e2e_edges"] = int(sum(len(e) for e in rest))
-        res["e2e_steps"] = len(rest)
-        res["e2e_lat"] = [stats[k].ms_total for k in range(len(rest))]
-        res["h2d"] = int(res["e2e_edges"] * 8 / len(rest))
-        res["d2h"] = int(len(sources) * cfg["rank_d"] * 8)
+        left = snaps[t1i:]
+        n_plain = 0 if args.no_plain else min(args.plain_steps, len(left) // 2)
+        rest = left[:min(args.steps, len(left) - n_plain)]
+        plain_snaps = left[len(rest):len(rest) + n_plain]
+        if not args.no_e2e and rest:
+            res.update(e2e_leg(s, rest, sources, cfg, device, stream))
+        if plain_snaps:
+            res["plain"] = plain_leg(s, plain_snaps, device, stream)
     return res
+
+
+def e2e_leg(s, rest, sources, cfg, device, stream):
+    """End to end through the C-ABI on the deltas that follow the timed ones:
+    host pairs (pinned) copied in and the embedding read back every step."""
+    import ctypes
+
+    import torch
+    import tsvd_gb300 as T
+    pinned = [torch.from_numpy(np.ascontiguousarray(e)).pin_memory() for e in rest]
+    L = T.lib()
+    emb = np.zeros((len(rest), len(sources), cfg["rank_d"]), np.float64)
+    stats = (T.StepStats * len(rest))()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize(device)
+    i32p, f64p = ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_double)
+    ev0.record(stream)
+    for k, e in enumerate(pinned):
+        T._check(L.tsvd_session_step(s._h, ctypes.cast(e.data_ptr(), i32p), len(rest[k])))
+        T._check(L.tsvd_session_embedding(s._h, emb[k].ctypes.data_as(f64p)))
+        T._check(L.tsvd_session_last_stats(s._h, ctypes.byref(stats[k])))
+    ev1.record(stream)
+    torch.cuda.synchronize(device)
+    assert np.isfinite(emb).all()
+    edges = int(sum(len(e) for e in rest))
+    return {"e2e_ms": ev0.elapsed_time(ev1), "e2e_edges": edges, "e2e_steps": len(rest),
+            "e2e_lat": [stats[k].ms_total for k in range(len(rest))],
+            "h2d": int(edges * 8 / len(rest)), "d2h": int(len(sources) * cfg["rank_d"] * 8)}
+
+
+def plain_leg(s, plain_snaps, device, stream):
+    """The same session switched to the plain GPU form for the next deltas
+    (device-resident, one tsvd_session_step_device each): per-snapshot
+    latency of the form the mixed-precision batched form is measured
+    against."""
+    import torch
+    import tsvd_gb300 as T
+    dev = [torch.from_numpy(np.ascontiguousarray(e)).to(f"cuda:{device}") for e in plain_snaps]
+    s.set_form(T.FORM_PLAIN)
+    stages = []
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize(device)
+    ev0.record(stream)
+    for e, d in zip(plain_snaps, dev):
+        s.step_device(d.data_ptr(), len(e))
+        stages.append(s.stats())
+    ev1.record(stream)
+    torch.cuda.synchronize(device)
+    s.set_form(T.FORM_MIXED)
+    lat = [st["ms_total"] for st in stages]
+    edges = int(sum(len(e) for e in plain_snaps))
+    return {"steps": len(stages), "ms": ev0.elapsed_time(ev1), "edges": edges, "lat": lat,
+            "stages": stages}
 
 
 # ------------------------------------------------------------- CPU samples
@@ -559,6 +596,21 @@ def main():
                        "p99_ms": float(np.percentile(res["e2e_lat"], 99)),
                        "deltas": "the %d deltas after the timed ones, same session"
                                  % res["e2e_steps"]}
+    if "plain" in res:
+        pl = res["plain"]
+        plat = pl["lat"]
+        line["plain_form"] = {
+            "form": "TSVD_FORM_PLAIN: one frontier entry and one scalar atomic per (vertex, "
+                    "source) cell, fp64 push arithmetic on the fp32 state, FP32 CSR SpMM "
+                    "frPCA one dirty block at a time, one merge per tree node",
+            "steps": pl["steps"], "p50_ms": float(np.percentile(plat, 50)),
+            "p99_ms": float(np.percentile(plat, 99)),
+            "value": pl["edges"] / (pl["ms"] / 1e3), "unit": "edge updates/s",
+            "stage_ms_mean": {k: float(np.mean([st[k] for st in pl["stages"]]))
+                              for k in ("ms_insert", "ms_push", "ms_log", "ms_frpca",
+                                        "ms_merge")},
+            "deltas": "the %d deltas after the e2e leg, same session" % pl["steps"]}
+        line["p50_plain_over_mixed"] = line["plain_form"]["p50_ms"] / line["p50_ms"]
     if rank == 0 and not args.no_cpu:
         info = cpu_sample(cfg, snaps, sources, steps=1, k=args.cpu_sources)
         s0 = info["steps"][0]

@@ -80,7 +80,12 @@ typedef struct {
  * Code/Tree_u_NC.cpp:139-142 and are overwritten. Singular values come
  * back in ascending order, like the reference (dsyevd order, frpca.c:298-310).
  * The Gaussian test matrix comes from the counter-based generator seeded by
- * tsvd_set_frpca_seed() (the reference seeds MKL VSL with time(NULL)).
+ * tsvd_set_frpca_seed() (the reference seeds MKL VSL with time(NULL)). The
+ * caller's double values are rounded to float and both products run as FP32
+ * SpMM on the GPU (tsvd_frpca_fp32); the small solves are fp32 with fp64
+ * Grams and an fp64-refined eigen-solve, so results match the reference's
+ * FP64 frPCA to about 1e-6 relative in the leading singular values, not to
+ * double precision.
  * Errors are reported through tsvd_last_error(); the legacy signature has no
  * return value, and on error the outputs are left zero-filled. */
 void frPCA(mat_csr *A, mat **U, mat **S, mat **V, int k, int q);
@@ -97,6 +102,19 @@ tsvd_status tsvd_frpca(int32_t nrows, int32_t ncols, int64_t nnz,
                        const double *values, int32_t index_base, int32_t k,
                        int32_t q, uint64_t seed, double *U, double *S,
                        double *V);
+
+/* Same arguments and outputs as tsvd_frpca, with the matrix kept in FP32 (a
+ * CSR / CSC pair of the non-empty columns, values rounded from double to
+ * float) and both products of every pass run as FP32 SpMM, as in the plain
+ * GPU form. tsvd_frpca rounds the values to half precision (relative 2^-11)
+ * for the tensor-core products. The legacy frPCA symbol uses this path.
+ * Replaces Code/frpca.c:239 (products: csr_matrix_{,transpose_}matrix_mult,
+ * Code/matrix_vector_functions_intel_mkl_ext.c:364-398). */
+tsvd_status tsvd_frpca_fp32(int32_t nrows, int32_t ncols, int64_t nnz,
+                            const int64_t *row_ptr, const int32_t *col_idx,
+                            const double *values, int32_t index_base, int32_t k,
+                            int32_t q, uint64_t seed, double *U, double *S,
+                            double *V);
 
 /* Same computation and arguments as tsvd_frpca, but it allocates nothing.
  * No counterpart in the reference. For callers that cannot call cudaMalloc:
@@ -157,6 +175,20 @@ enum {
   TSVD_REFRESH_INTDIV = 1 /* p *= (j+1)/j in int   (ppr:2102, 3875, 4203, the dense path)  */
 };
 
+enum {
+  /* How tsvd_session_step computes a snapshot. Both give the same results
+   * within the parity tolerances and leave the same state behind, so a
+   * session may switch between them (tsvd_session_set_form). */
+  TSVD_FORM_MIXED = 0, /* 64-source residue runs (one 256-byte vector atomic per       */
+                       /* neighbour), dirty blocks batched per stage, products on the  */
+                       /* tensor cores with half-precision A^T and hi+lo skinny        */
+                       /* operands                                                     */
+  TSVD_FORM_PLAIN = 1  /* the plain GPU form: one frontier entry and one scalar atomic */
+                       /* per (vertex, source) cell with fp64 push arithmetic; every   */
+                       /* dirty block factorized on its own with FP32 CSR SpMM; one    */
+                       /* merge launch sequence per tree node                          */
+};
+
 typedef struct tsvd_config {
   int32_t n_vertices;       /* N (argv[9] of the reference drivers)                  */
   int32_t directed;         /* 0: UGraph (Tree_u_*), 1: Graph + transpose (Tree_d_*)  */
@@ -191,6 +223,7 @@ typedef struct tsvd_config {
                             /* over NVLink-C2C; the residues stay in HBM. For graphs  */
                             /* whose 16 N Sp bytes of state exceed HBM (N 6.2M,       */
                             /* |S| 3000: 305 GB)                                      */
+  int32_t form;             /* TSVD_FORM_*: how a snapshot is computed (see below)   */
 } tsvd_config;
 
 /* Fills the reference's defaults (Tree_u_NC, run.sh: alpha .5, q 12, ...). */
@@ -212,6 +245,10 @@ tsvd_status tsvd_session_embedding(tsvd_session *s, double *out);
 /* Device pointer to the current embedding (|S| x d row-major float), valid
  * until the next step. */
 tsvd_status tsvd_session_embedding_device(tsvd_session *s, const float **out);
+
+/* Switches the form of the following snapshots (TSVD_FORM_*). The plain form
+ * runs one snapshot per call: tsvd_session_run refuses it. */
+tsvd_status tsvd_session_set_form(tsvd_session *s, int32_t form);
 
 /* The session's CUDA stream (cudaStream_t), for callers that order their own
  * work or timing events against the session's kernels. */

@@ -19,11 +19,6 @@ INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 NVCC = os.environ.get("NVCC", "nvcc")
 
 
-def _cuda_lib_dir():
-    """lib64 of the toolkit nvcc belongs to (runtime path of libcublas)."""
-    import shutil
-    exe = shutil.which(NVCC) or NVCC
-    return os.path.join(os.path.dirname(os.path.dirname(os.path.realpath(exe))), "lib64")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-I" + INCLUDE, "-I" + CSRC,
           "-Xcompiler", "-fPIC,-pthread,-ffp-contract=off", "-diag-suppress", "177"]
@@ -52,8 +47,7 @@ def build(verbose=False):
     with cf.ThreadPoolExecutor(max_workers=max(2, os.cpu_count() or 2)) as ex:
         objs = list(ex.map(lambda s: _compile(s, hm), srcs))
     if not os.path.exists(LIB) or os.path.getmtime(LIB) < _newest(objs):
-        cmd = [NVCC] + ARCH + ["-shared", "-o", LIB] + objs + ["-Xcompiler", "-pthread", "-lcublas",
-                                                            "-Xlinker", "-rpath," + _cuda_lib_dir()]
+        cmd = [NVCC] + ARCH + ["-shared", "-o", LIB] + objs + ["-Xcompiler", "-pthread"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed:\n%s%s" % (r.stdout, r.stderr))

@@ -17,10 +17,9 @@
 #include <algorithm>
 #include <cmath>
 
-#include <cublas_v2.h>
-
 #include "factor.h"
 #include "philox_gauss.h"
+#include "plain.h"
 
 namespace tsvd {
 
@@ -233,18 +232,9 @@ void frpca_work_free(FrpcaWork &W) {
   cudaFree(W.wm); cudaFree(W.wv); cudaFree(W.ww); cudaFree(W.wy); cudaFree(W.wy2);
   cudaFree(W.wchol); cudaFree(W.wnorm); cudaFree(W.wk);
   cudaFree(W.dv); cudaFree(W.dt); cudaFree(W.dh); cudaFree(W.dh_ptrs);
-  if (W.blas) cublasDestroy((cublasHandle_t)W.blas);
   cudaGetLastError();  // the launch checks read this slot: leave nothing from teardown in it
   W = FrpcaWork();
 }
-
-#define TSVD_BLAS(call)                                                        \
-  do {                                                                         \
-    cublasStatus_t s_ = (call);                                                \
-    if (s_ != CUBLAS_STATUS_SUCCESS)                                           \
-      return fail(TSVD_ERR_DEVICE, "cuBLAS status %d at %s:%d", (int)s_,       \
-                  __FILE__, __LINE__);                                         \
-  } while (0)
 
 namespace {
 
@@ -355,9 +345,27 @@ tsvd_status frpca_batch(FrpcaWork &W, const FrpcaProblem *probs, int nprob, int 
     cbase[i] = P.col_base;
     blk[i] = P.block;
   }
+  const bool sparse = probs[0].sparse != nullptr;
+  std::vector<const int64_t *> rptr(nprob), cptr(nprob);
+  std::vector<const int32_t *> ridx(nprob), cidx(nprob);
+  std::vector<const float *> rval(nprob), cval(nprob);
+  for (int i = 0; i < nprob; ++i) {
+    const SparseBlock *sb = probs[i].sparse;
+    if ((sb != nullptr) != sparse)
+      return fail(TSVD_ERR_INVALID, "frpca: a batch mixes sparse and dense blocks");
+    if (!sb) continue;
+    if (sb->cols != ncols[i] || sb->rows != sp)
+      return fail(TSVD_ERR_INVALID, "frpca: sparse block %d x %d, expected %d x %d", sb->rows,
+                  sb->cols, sp, ncols[i]);
+    rptr[i] = sb->rowptr; ridx[i] = sb->colidx; rval[i] = sb->rval;
+    cptr[i] = sb->colptr; cidx[i] = sb->rowidx; cval[i] = sb->cval;
+  }
   PtrPack pk(W);
   auto d_at = pk.add(at);
   auto d_xhi = pk.add(xhi), d_xlo = pk.add(xlo), d_qhi = pk.add(qhi), d_qlo = pk.add(qlo);
+  auto d_rptr = pk.add(rptr), d_cptr = pk.add(cptr);
+  auto d_ridx = pk.add(ridx), d_cidx = pk.add(cidx);
+  auto d_rval = pk.add(rval), d_cval = pk.add(cval);
   auto d_z = pk.add(z), d_y = pk.add(y), d_t = pk.add(t), d_lam = pk.add(lam), d_v = pk.add(v);
   auto d_cs = pk.add(cs), d_csi = pk.add(csi), d_bout = pk.add(bout), d_sout = pk.add(sout);
   auto d_uout = pk.add(uout), d_vout = pk.add(vout);
@@ -370,14 +378,27 @@ tsvd_status frpca_batch(FrpcaWork &W, const FrpcaProblem *probs, int nprob, int 
 
   GemmBatch gb{d_at, d_nc, sp, nprob};
   const size_t ybytes = (size_t)nprob * SK * sizeof(float);
+  // Y = A X (sp x kLp) and Z = A^T Q (n_c x kLp): tensor-core GEMMs on the
+  // half-precision A^T, or FP32 SpMM over the block's CSR / CSC
+  auto prod_fwd = [&](const __half *const *hi, const __half *const *lo,
+                      float scale) -> tsvd_status {
+    if (sparse)
+      return spmm_batched(d_rptr, d_ridx, d_rval, d_sprows, sp, hi, lo, d_y, scale, nprob, st);
+    return gemm_fwd(gb, hi, lo, d_y, W.y, ybytes, sp, max_nc, scale, st);
+  };
+  auto prod_bwd = [&](const __half *const *hi, const __half *const *lo,
+                      float scale) -> tsvd_status {
+    if (sparse)
+      return spmm_batched(d_cptr, d_cidx, d_cval, d_nc, max_nc, hi, lo, d_z, scale, nprob, st);
+    return gemm_bwd(gb, hi, lo, d_z, sp, max_nc, scale, st);
+  };
   const int niter = (q - 1) / 2;
   float in_scale = 1.f / kSplitScale;
   if (q % 2 == 0) {
     omega_kernel<<<dim3(grid_for((int64_t)max_nc * kLp, 256, 4), nprob), 256, 0, st>>>(
         d_xhi, d_nc, d_cmap, d_cbase, d_blk, W.rows_max, l, seed);
     TSVD_LAUNCH_CHECK();
-    TSVD_TRY(gemm_fwd(gb, (const __half *const *)d_xhi, nullptr, d_y, W.y, ybytes, sp, max_nc,
-                      1.f, st));
+    TSVD_TRY(prod_fwd((const __half *const *)d_xhi, nullptr, 1.f));
     TSVD_TRY(cholqr(W, d_y, d_sprows, sp, d_g, d_t, d_qhi, d_qlo, nprob, st, niter ? 1 : 2));
   } else {
     const float split = 2048.f;
@@ -392,16 +413,14 @@ tsvd_status frpca_batch(FrpcaWork &W, const FrpcaProblem *probs, int nprob, int 
   // LU factor there, frpca.c:261-291). The last basis Q, which B = Q V S is
   // built from, gets both passes.
   for (int it = 1; it <= niter; ++it) {
-    TSVD_TRY(gemm_bwd(gb, (const __half *const *)d_qhi, (const __half *const *)d_qlo, d_z, sp,
-                      max_nc, in_scale, st));
+    TSVD_TRY(prod_bwd((const __half *const *)d_qhi, (const __half *const *)d_qlo, in_scale));
     TSVD_TRY(cholqr(W, d_z, d_nc, max_nc, d_g, d_t, d_xhi, d_xlo, nprob, st, 1));
-    TSVD_TRY(gemm_fwd(gb, (const __half *const *)d_xhi, (const __half *const *)d_xlo, d_y, W.y,
-                      ybytes, sp, max_nc, 1.f / kSplitScale, st));
+    TSVD_TRY(prod_fwd((const __half *const *)d_xhi, (const __half *const *)d_xlo,
+                      1.f / kSplitScale));
     TSVD_TRY(cholqr(W, d_y, d_sprows, sp, d_g, d_t, d_qhi, d_qlo, nprob, st, it == niter ? 2 : 1));
     in_scale = 1.f / kSplitScale;
   }
-  TSVD_TRY(gemm_bwd(gb, (const __half *const *)d_qhi, (const __half *const *)d_qlo, d_z, sp,
-                    max_nc, in_scale, st));
+  TSVD_TRY(prod_bwd((const __half *const *)d_qhi, (const __half *const *)d_qlo, in_scale));
   // eigSVD of Z = A^T Q (frpca.c:99-136): Gram, eigenpairs, top-d.
   TSVD_TRY(gram_batched((const float *const *)d_z, d_nc, max_nc, l, kLp, d_g, W.gram_work,
                         W.gram_bytes, nprob, st));
@@ -516,12 +535,6 @@ constexpr int64_t kWideK = 256 * 256 + 256 * 257 / 2;  // fp32 Gram + packed fac
 tsvd_status wide_reserve(FrpcaWork &W, int nprob, int n) {
   const int nsrc = W.sp;
   const size_t need = (size_t)nprob * nsrc * n;
-  if (!W.blas) {
-    cublasHandle_t h = nullptr;
-    TSVD_BLAS(cublasCreate(&h));
-    W.blas = h;
-    TSVD_BLAS(cublasSetMathMode(h, CUBLAS_PEDANTIC_MATH));  // fp32 products, no tf32
-  }
   if (need <= W.wide_cap && nprob <= W.wide_nprob && n <= W.wide_n && W.wm) return TSVD_OK;
   cudaFree(W.wm); cudaFree(W.wv); cudaFree(W.ww); cudaFree(W.wy); cudaFree(W.wy2);
   cudaFree(W.wchol); cudaFree(W.wnorm); cudaFree(W.wk);
@@ -579,7 +592,7 @@ tsvd_status orthonormalize(FrpcaWork &W, float *x, int64_t xstride, float *y, in
 // and stopped when ||M V||_F^2 gains less than 1e-7 of itself. The result is
 // then the merge of the p columns of M V (compensated Gram + Jacobi), the
 // same arithmetic as a narrow merge. The products are plain fp32 GEMMs
-// (cuBLAS, pedantic math).
+// (sgemm_batched: fixed-order sums, 64 x 64 tiles).
 tsvd_status merge_wide_core(FrpcaWork &W, const MergeProblem *probs, int nprob, int n, int nsrc,
                             int root_mode, cudaStream_t st);
 
@@ -617,8 +630,6 @@ tsvd_status merge_wide_core(FrpcaWork &W, const MergeProblem *probs, int nprob, 
   const int p = std::min(256, std::min(n, nsrc));
   if (p < d) return fail(TSVD_ERR_INVALID, "merge: %d rows or columns, below rank d = %d",
                          std::min(n, nsrc), d);
-  cublasHandle_t blas = (cublasHandle_t)W.blas;
-  TSVD_BLAS(cublasSetStream(blas, st));
   const int64_t sm = (int64_t)nsrc * n, sv = (int64_t)n * p, sy = (int64_t)nsrc * p;
   // start: the p columns of M with the largest norms (the children's largest sigmas)
   colnorm_kernel<<<dim3(ceil_div(n, 256), nprob), 256, 0, st>>>(W.wm, nsrc, n, W.wnorm);
@@ -643,25 +654,22 @@ tsvd_status merge_wide_core(FrpcaWork &W, const MergeProblem *probs, int nprob, 
     TSVD_LAUNCH_CHECK();
     TSVD_CUDA(cudaStreamSynchronize(st));
   }
-  const float one = 1.f, zero = 0.f;
   std::vector<double> energy(nprob), prev(nprob, 0.0);
-  // x (rows x p, row-major, problem stride xs) -> y: fp32 Gram (cuBLAS; problem
-  // i at W.wk + i p p), shifted fp32 Cholesky (packed factors after all the
+  // x (rows x p, row-major, problem stride xs) -> y: fp32 Gram (problem i at
+  // W.wk + i p p), shifted fp32 Cholesky (packed factors after all the
   // Grams), triangular solve.
   const int64_t kp = (int64_t)p * p;
   auto cheap_basis = [&](const float *x, int64_t xs, float *y, int rows) -> tsvd_status {
-    // K = x^T x: column-major K (p x p) = (x^T) (x^T)^T with x^T (p x rows, ld p)
-    TSVD_BLAS(cublasSgemmStridedBatched(blas, CUBLAS_OP_N, CUBLAS_OP_T, p, p, rows, &one, x, p,
-                                        xs, x, p, xs, &zero, W.wk, p, kp, nprob));
+    // K = x^T x (p x p)
+    TSVD_TRY(sgemm_batched(true, p, p, rows, x, p, xs, x, p, xs, W.wk, p, kp, nprob, st));
     TSVD_TRY(chol_shift_solve_batched(W.wk, W.wk + nprob * kp, x, y, rows, p, xs, 1e-6f, nprob,
                                       st));
     return TSVD_OK;
   };
   int it = 0;
   for (; it < 40; ++it) {
-    // Y = M V: column-major, Y^T (p x |S|) = V^T (p x n) M^T (n x |S|)
-    TSVD_BLAS(cublasSgemmStridedBatched(blas, CUBLAS_OP_N, CUBLAS_OP_N, p, nsrc, n, &one, W.wv,
-                                        p, sv, W.wm, n, sm, &zero, W.wy, p, sy, nprob));
+    // Y = M V (|S| x p)
+    TSVD_TRY(sgemm_batched(false, nsrc, p, n, W.wm, n, sm, W.wv, p, sv, W.wy, p, sy, nprob, st));
     TSVD_TRY(cheap_basis(W.wy, sy, W.wy2, nsrc));
     // ||M V||_F^2 = trace(Y^T Y), from the diagonal of the Gram just formed
     std::vector<float> diag((size_t)nprob * p);
@@ -679,9 +687,8 @@ tsvd_status merge_wide_core(FrpcaWork &W, const MergeProblem *probs, int nprob, 
     }
     prev = energy;
     if (done) break;
-    // W = M^T Yq: column-major, W^T (p x n) = Yq^T (p x |S|) M (|S| x n)
-    TSVD_BLAS(cublasSgemmStridedBatched(blas, CUBLAS_OP_N, CUBLAS_OP_T, p, n, nsrc, &one, W.wy2,
-                                        p, sy, W.wm, n, sm, &zero, W.ww, p, sv, nprob));
+    // W = M^T Yq (n x p)
+    TSVD_TRY(sgemm_batched(true, n, p, nsrc, W.wm, n, sm, W.wy2, p, sy, W.ww, p, sv, nprob, st));
     TSVD_TRY(cheap_basis(W.ww, sv, W.wv, n));
   }
   // one accurate CholeskyQR pass: an orthonormal V to working precision
@@ -692,9 +699,8 @@ tsvd_status merge_wide_core(FrpcaWork &W, const MergeProblem *probs, int nprob, 
   const int64_t RK = std::max<int64_t>(W.rows_max * kLp, (int64_t)W.sp * 256);
   std::vector<float *> z(nprob);
   for (int i = 0; i < nprob; ++i) z[i] = W.z + i * RK;
-  for (int i = 0; i < nprob; ++i)
-    TSVD_BLAS(cublasSgemm(blas, CUBLAS_OP_N, CUBLAS_OP_N, p, nsrc, n, &one, W.wv + i * sv, p,
-                          W.wm + i * sm, n, &zero, z[i], p));
+  // Z = M V (|S| x p), problem i at W.z + i RK
+  TSVD_TRY(sgemm_batched(false, nsrc, p, n, W.wm, n, sm, W.wv, p, sv, W.z, p, RK, nprob, st));
   return merge_finish(W, probs, nprob, p, nsrc, root_mode, z, st);
 }
 

@@ -28,7 +28,6 @@ struct FrpcaWork {
   int32_t *dint = nullptr; // device int area (row counts, block ids)
   int32_t *hint = nullptr;
   int last_sweeps = 0;
-  void *blas = nullptr;     // cublasHandle_t
   double *dv = nullptr, *dt = nullptr, *dh = nullptr;  // [nmax][256*256] eigen refinement
   double **dh_ptrs = nullptr;  // device: dh + i 256^2 for each problem i
   int last_refine_sweeps = 0;
@@ -49,6 +48,8 @@ struct FrpcaWork {
 tsvd_status frpca_work_alloc(FrpcaWork &W, int nmax, int64_t rows_max, int sp, int l, int d);
 void frpca_work_free(FrpcaWork &W);
 
+struct SparseBlock;
+
 struct FrpcaProblem {
   int32_t block;            // Gaussian stream id
   const __half *at;         // A^T [ncols][sp]
@@ -59,10 +60,14 @@ struct FrpcaProblem {
   float *sigma_out;         // d, or null
   float *u_out;             // sp x d (ld d): U, or null
   float *v_out;             // ncols x d (ld d): V, or null
+  const SparseBlock *sparse = nullptr;  // FP32 CSR/CSC of the block (plain form): both
+                                        // products as SpMM instead of tensor-core GEMMs
 };
 
 // Runs frPCA (k = d, oversampling l - d, q passes) on every problem. sum_sigma2
-// (host, nprob) receives the sum of the kept squared singular values.
+// (host, nprob) receives the sum of the kept squared singular values. Either
+// every problem carries a SparseBlock (FP32 SpMM products) or none does
+// (half-precision A^T on the tensor cores).
 tsvd_status frpca_batch(FrpcaWork &W, const FrpcaProblem *probs, int nprob, int q,
                         uint64_t seed, int nsrc, cudaStream_t st, double *sum_sigma2);
 

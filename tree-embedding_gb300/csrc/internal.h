@@ -102,6 +102,12 @@ tsvd_status gemm_bwd(const GemmBatch &gb, const __half *const *yhi,
 // check (a bounded wait ran out); synchronizes the stream.
 tsvd_status gemm_check(cudaStream_t st);
 
+// C[z] = op(A[z]) B[z] in fp32, row-major (op(A) = A^T when trans_a: A is
+// K x M), problem z at z * stride of each operand; fixed-order sums.
+tsvd_status sgemm_batched(bool trans_a, int M, int N, int K, const float *A, int lda, int64_t sa,
+                          const float *B, int ldb, int64_t sb, float *C, int ldc, int64_t sc,
+                          int nprob, cudaStream_t st);
+
 // G[b] (l x l fp64) = X[b]^T X[b], X row-major [rows_b][ld] fp32.
 tsvd_status gram_batched(const float *const *x, const int32_t *rows, int max_rows,
                          int l, int ld, double *const *g, double *work,

@@ -15,6 +15,7 @@
 #include "blocks.h"
 #include "factor.h"
 #include "internal.h"
+#include "plain.h"
 #include "ppr.h"
 
 // ------------------------------------------------------------------ errors
@@ -101,6 +102,10 @@ struct tsvd_session {
   int32_t *pairs_dev = nullptr;
   double *scores_dev = nullptr;
   int64_t pairs_cap = 0;
+  // plain form (allocated on its first snapshot)
+  int form = TSVD_FORM_MIXED;
+  PlainPpr plain[2];
+  PlainBlockWork pbw;
 
   size_t node_elems() const { return (size_t)S * d; }
   float *node_b(int i) { return tree_b + (size_t)i * node_elems(); }
@@ -322,6 +327,9 @@ static void session_release(tsvd_session *s) {
   cudaFree(s->lp_v); cudaFree(s->lp_u); cudaFree(s->lp_valid_dev); cudaFree(s->colpos);
   cudaFree(s->src_row); cudaFree(s->pairs_dev); cudaFree(s->scores_dev);
   frpca_work_free(s->fw);
+  for (int dd = 0; dd < 2; ++dd)
+    if (s->plain[dd].cbits) plain_free(s->plain[dd]);
+  plain_block_free(s->pbw);
   cudaFreeHost(s->emb_stage);
   for (auto &e : s->ev)
     if (e) cudaEventDestroy(e);
@@ -354,6 +362,8 @@ extern "C" tsvd_status tsvd_session_create(const tsvd_config *cfg, tsvd_session 
   if (c.passes_q < 1) return fail(TSVD_ERR_INVALID, "passes_q must be >= 1");
   if (c.transform < 0 || c.transform > 2 || c.dirty_rule < 0 || c.dirty_rule > 2)
     return fail(TSVD_ERR_INVALID, "bad transform or dirty rule");
+  if (c.form != TSVD_FORM_MIXED && c.form != TSVD_FORM_PLAIN)
+    return fail(TSVD_ERR_INVALID, "form must be TSVD_FORM_MIXED or TSVD_FORM_PLAIN");
   if (c.lp_right_factor && c.root_scaling != TSVD_ROOT_U)
     return fail(TSVD_ERR_INVALID, "lp_right_factor needs root_scaling TSVD_ROOT_U (LP drivers)");
   std::vector<int32_t> src(c.sources, c.sources + c.n_sources);
@@ -380,6 +390,7 @@ extern "C" tsvd_status tsvd_session_create(const tsvd_config *cfg, tsvd_session 
   s->l = c.rank_d + c.oversample;
   s->q = c.passes_q;
   s->directed = c.directed ? 1 : 0;
+  s->form = c.form;
   tsvd_status st = session_alloc(s);
   if (st != TSVD_OK) {
     std::string msg = tsvd_last_error();
@@ -585,7 +596,31 @@ static tsvd_status stage_factorize(tsvd_session *s, FactorJob &job, cudaStream_t
     P.v_out = nullptr;
   }
   std::vector<double> ssum(nf);
-  TSVD_TRY(frpca_batch(s->fw, probs.data(), nf, s->q, s->cfg.seed, s->S, st, ssum.data()));
+  if (s->form == TSVD_FORM_PLAIN) {
+    // every dirty block on its own: FP32 CSR / CSC from the reserve, then
+    // frPCA with SpMM products
+    for (int i = 0; i < nf; ++i) {
+      const int b = job.factor_now[i];
+      BlockSource src;
+      src.p1 = s->ppr[0].p;
+      src.p2 = s->directed ? s->ppr[1].p : nullptr;
+      src.colmap = s->colmap + (size_t)b * s->col_dim;
+      src.ncols = job.ncols[b];
+      src.n = s->n;
+      src.sp = s->sp;
+      src.nsrc = s->S;
+      src.transform = s->cfg.transform;
+      src.rmin_f = (float)s->cfg.rmax;
+      src.inv_rmin_f = (float)(1.0 / s->cfg.rmax);
+      src.n_f = (float)s->n;
+      TSVD_TRY(plain_block_build(s->pbw, src, s->nnz_h[b], st));
+      probs[i].sparse = &s->pbw.blk;
+      TSVD_TRY(frpca_batch(s->fw, &probs[i], 1, s->q, s->cfg.seed, s->S, st, &ssum[i]));
+      job.stats.eig_refine_sweeps = std::max(job.stats.eig_refine_sweeps, s->fw.last_refine_sweeps);
+    }
+  } else {
+    TSVD_TRY(frpca_batch(s->fw, probs.data(), nf, s->q, s->cfg.seed, s->S, st, ssum.data()));
+  }
   job.stats.eig_sweeps_frpca = s->fw.last_sweeps;
   job.stats.eig_refine_sweeps = std::max(job.stats.eig_refine_sweeps, s->fw.last_refine_sweeps);
   // Residual ||A - U S V^T||_F = sqrt(||A||^2 - sum sigma^2) for an orthonormal
@@ -619,7 +654,11 @@ static tsvd_status stage_merge(tsvd_session *s, FactorJob &job, cudaStream_t st)
     }
     int mode = 0;
     if (root) mode = s->cfg.root_scaling == TSVD_ROOT_U ? 2 : 1;
-    TSVD_TRY(merge_batch(s->fw, probs.data(), (int)probs.size(), h, s->S, mode, st));
+    if (s->form == TSVD_FORM_PLAIN) {
+      for (auto &pr : probs) TSVD_TRY(merge_batch(s->fw, &pr, 1, h, s->S, mode, st));
+    } else {
+      TSVD_TRY(merge_batch(s->fw, probs.data(), (int)probs.size(), h, s->S, mode, st));
+    }
     job.stats.eig_sweeps_merge = std::max(job.stats.eig_sweeps_merge, s->fw.last_sweeps);
     job.stats.merge_subspace_iters = std::max(job.stats.merge_subspace_iters, s->fw.wide_iters);
     job.stats.eig_refine_sweeps = std::max(job.stats.eig_refine_sweeps, s->fw.last_refine_sweeps);
@@ -679,9 +718,16 @@ static tsvd_status stage_lp(tsvd_session *s, const FactorJob &job, cudaStream_t 
 static tsvd_status stage_ppr(tsvd_session *s, int iter, int dir) {
   const bool scratch = iter < s->cfg.dynamic_ppr_start_iter;
   PprParams prm = ppr_params(s);
-  TSVD_TRY(ppr_refresh(s->ppr[dir], s->adj[dir], s->sources_dev, scratch, prm, s->vmark, s->st));
   PushStats ps;
-  TSVD_TRY(ppr_push(s->ppr[dir], s->adj[dir], prm, s->vmark, s->st, &ps));
+  if (s->form == TSVD_FORM_PLAIN) {
+    if (!s->plain[dir].cbits) TSVD_TRY(plain_alloc(s->plain[dir], s->n, s->sp));
+    TSVD_TRY(plain_refresh(s->plain[dir], s->ppr[dir], s->adj[dir], s->sources_dev, scratch, prm,
+                           s->st));
+    TSVD_TRY(plain_push(s->plain[dir], s->ppr[dir], s->adj[dir], prm, s->vmark, s->st, &ps));
+  } else {
+    TSVD_TRY(ppr_refresh(s->ppr[dir], s->adj[dir], s->sources_dev, scratch, prm, s->vmark, s->st));
+    TSVD_TRY(ppr_push(s->ppr[dir], s->adj[dir], prm, s->vmark, s->st, &ps));
+  }
   s->last.push_rounds += ps.rounds;
   s->last.pushes += ps.pushes;
   s->last.push_edge_updates += ps.edge_updates;
@@ -843,6 +889,9 @@ static tsvd_status run_snapshots(tsvd_session *s, const int32_t *edges, bool on_
                                  tsvd_step_stats *stats_out) {
   TSVD_CUDA(cudaSetDevice(s->cfg.device));
   cudaGetLastError();  // not ours: see session_alloc
+  if (s->form == TSVD_FORM_PLAIN)
+    return fail(TSVD_ERR_INVALID,
+                "the plain form reads the reserve in its factor stage: one snapshot per call");
   int64_t max_m = 0;
   for (int k = 0; k < count; ++k) {
     const int64_t m = offsets[k + 1] - offsets[k];
@@ -953,6 +1002,15 @@ extern "C" tsvd_status tsvd_session_embedding_device(tsvd_session *s, const floa
   return TSVD_OK;
 }
 
+extern "C" tsvd_status tsvd_session_set_form(tsvd_session *s, int32_t form) {
+  if (!s) return fail(TSVD_ERR_INVALID, "null session");
+  if (form != TSVD_FORM_MIXED && form != TSVD_FORM_PLAIN)
+    return fail(TSVD_ERR_INVALID, "form must be TSVD_FORM_MIXED or TSVD_FORM_PLAIN");
+  s->form = form;
+  s->cfg.form = form;
+  return TSVD_OK;
+}
+
 extern "C" tsvd_status tsvd_session_stream(tsvd_session *s, void **stream) {
   if (!s || !stream) return fail(TSVD_ERR_INVALID, "null argument");
   *stream = (void *)s->st;
@@ -979,8 +1037,13 @@ extern "C" tsvd_status tsvd_ppr_refresh(tsvd_session *s, int32_t iter, int32_t t
   TSVD_CUDA(cudaSetDevice(s->cfg.device));
   PprParams prm = ppr_params(s);
   const int dir = transpose ? 1 : 0;
-  return ppr_refresh(s->ppr[dir], s->adj[dir], s->sources_dev,
-                     iter < s->cfg.dynamic_ppr_start_iter, prm, s->vmark, s->st);
+  const bool scratch = iter < s->cfg.dynamic_ppr_start_iter;
+  if (s->form == TSVD_FORM_PLAIN) {
+    if (!s->plain[dir].cbits) TSVD_TRY(plain_alloc(s->plain[dir], s->n, s->sp));
+    return plain_refresh(s->plain[dir], s->ppr[dir], s->adj[dir], s->sources_dev, scratch, prm,
+                         s->st);
+  }
+  return ppr_refresh(s->ppr[dir], s->adj[dir], s->sources_dev, scratch, prm, s->vmark, s->st);
 }
 
 extern "C" tsvd_status tsvd_ppr_push(tsvd_session *s, int32_t transpose) {
@@ -990,7 +1053,12 @@ extern "C" tsvd_status tsvd_ppr_push(tsvd_session *s, int32_t transpose) {
   PprParams prm = ppr_params(s);
   const int dir = transpose ? 1 : 0;
   PushStats ps;
-  TSVD_TRY(ppr_push(s->ppr[dir], s->adj[dir], prm, s->vmark, s->st, &ps));
+  if (s->form == TSVD_FORM_PLAIN) {
+    if (!s->plain[dir].cbits) return fail(TSVD_ERR_STATE, "push before refresh");
+    TSVD_TRY(plain_push(s->plain[dir], s->ppr[dir], s->adj[dir], prm, s->vmark, s->st, &ps));
+  } else {
+    TSVD_TRY(ppr_push(s->ppr[dir], s->adj[dir], prm, s->vmark, s->st, &ps));
+  }
   s->last.push_rounds += ps.rounds;
   s->last.pushes += ps.pushes;
   s->last.push_edge_updates += ps.edge_updates;

@@ -16,6 +16,7 @@ TRANSFORM_LOG10_NC, TRANSFORM_LOG10_LP, TRANSFORM_LN_N = 0, 1, 2
 DIRTY_REFERENCE, DIRTY_FROBENIUS, DIRTY_ALL = 0, 1, 2
 ROOT_SQRT_SIGMA, ROOT_U = 0, 1
 REFRESH_EXACT, REFRESH_INTDIV = 0, 1
+FORM_MIXED, FORM_PLAIN = 0, 1
 
 STATUS = {0: "ok", 1: "invalid argument", 2: "out of memory", 3: "device error",
           4: "timeout", 5: "bad state", 6: "i/o error", 7: "numeric error"}
@@ -42,7 +43,7 @@ class Config(ctypes.Structure):
         ("device", ctypes.c_int32), ("max_push_rounds", ctypes.c_int32),
         ("push_levels", ctypes.c_int32), ("push_ratio", ctypes.c_double),
         ("push_cofrac", ctypes.c_double), ("lp_right_factor", ctypes.c_int32),
-        ("ppr_host_reserve", ctypes.c_int32),
+        ("ppr_host_reserve", ctypes.c_int32), ("form", ctypes.c_int32),
     ]
 
 
@@ -80,10 +81,14 @@ _SIGS = {
     "tsvd_version": (ctypes.c_char_p, []),
     "tsvd_launch_count": (ctypes.c_int64, []),
     "tsvd_session_stream": (ctypes.c_int, [_vp, ctypes.POINTER(_vp)]),
+    "tsvd_session_set_form": (ctypes.c_int, [_vp, ctypes.c_int32]),
     "tsvd_set_frpca_seed": (None, [ctypes.c_uint64]),
     "tsvd_frpca": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.c_int64, _i64p, _i32p,
                                   _f64p, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
                                   ctypes.c_uint64, _f64p, _f64p, _f64p]),
+    "tsvd_frpca_fp32": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.c_int64, _i64p,
+                                       _i32p, _f64p, ctypes.c_int32, ctypes.c_int32,
+                                       ctypes.c_int32, ctypes.c_uint64, _f64p, _f64p, _f64p]),
     "tsvd_frpca_noalloc": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.c_int64, _i64p,
                                           _i32p, _f64p, ctypes.c_int32, ctypes.c_int32,
                                           ctypes.c_int32, ctypes.c_uint64, _f64p, _f64p, _f64p]),
@@ -216,9 +221,10 @@ def launch_count():
 
 
 def frpca(csr_indptr, csr_indices, csr_data, shape, k, q, seed=20231, index_base=0,
-          noalloc=False):
+          noalloc=False, fp32=False):
     """Randomized SVD of a CSR matrix; returns U (m x k), S (k, descending), V (n x k).
-    noalloc=True calls tsvd_frpca_noalloc (no allocation, bounded sizes)."""
+    noalloc=True calls tsvd_frpca_noalloc (no allocation, bounded sizes);
+    fp32=True calls tsvd_frpca_fp32 (FP32 SpMM products)."""
     m, n = shape
     rp = np.ascontiguousarray(csr_indptr, dtype=np.int64)
     ci = np.ascontiguousarray(csr_indices, dtype=np.int32)
@@ -226,7 +232,8 @@ def frpca(csr_indptr, csr_indices, csr_data, shape, k, q, seed=20231, index_base
     U = np.zeros((k, m), np.float64)
     S = np.zeros(k, np.float64)
     V = np.zeros((k, n), np.float64)
-    fn = lib().tsvd_frpca_noalloc if noalloc else lib().tsvd_frpca
+    fn = (lib().tsvd_frpca_noalloc if noalloc else
+          lib().tsvd_frpca_fp32 if fp32 else lib().tsvd_frpca)
     _check(fn(m, n, len(va), _p(rp, _i64p), _p(ci, _i32p), _p(va, _f64p), index_base, k, q,
               seed, _p(U, _f64p), _p(S, _f64p), _p(V, _f64p)))
     return U.T.copy(), S, V.T.copy()
@@ -253,7 +260,7 @@ class Session:
                  transform=TRANSFORM_LOG10_NC, dirty_rule=DIRTY_REFERENCE, dirty_frac=0.01,
                  root_scaling=ROOT_SQRT_SIGMA, refresh_mode=REFRESH_EXACT, seed=20231, device=0,
                  max_push_rounds=0, push_levels=1, push_ratio=8.0, push_cofrac=0.85,
-                 lp_right_factor=False, ppr_host_reserve=False):
+                 lp_right_factor=False, ppr_host_reserve=False, form=FORM_MIXED):
         self.sources = np.ascontiguousarray(sources, dtype=np.int32)
         c = Config()
         lib().tsvd_config_default(ctypes.byref(c))
@@ -273,6 +280,7 @@ class Session:
         c.push_cofrac = float(push_cofrac)
         c.lp_right_factor = int(bool(lp_right_factor))
         c.ppr_host_reserve = int(bool(ppr_host_reserve))
+        c.form = int(form)
         self.cfg = c
         self.n, self.S, self.d = c.n_vertices, c.n_sources, c.rank_d
         self.n_parts, self.h, self.directed = c.n_parts, c.hierarchy_n, bool(directed)
@@ -340,6 +348,10 @@ class Session:
         p = _vp()
         _check(lib().tsvd_session_embedding_device(self._h, ctypes.byref(p)))
         return p.value
+
+    def set_form(self, form):
+        """FORM_MIXED or FORM_PLAIN for the following snapshots."""
+        _check(lib().tsvd_session_set_form(self._h, int(form)))
 
     def stream(self):
         p = _vp()
