@@ -80,6 +80,12 @@ def parse():
     ap.add_argument("--cpu-sources", type=int, default=None,
                     help="sources in the CPU sample (default: two per host thread)")
     ap.add_argument("--seed", type=int, default=20231)
+    ap.add_argument("--serve", action="store_true",
+                    help="serving measurement instead of the headline: tenants of different sizes "
+                         "on one GPU, Poisson-arriving edge batches, p50/p99 request latency")
+    ap.add_argument("--serve-tenants", type=int, default=8)
+    ap.add_argument("--serve-requests", type=int, default=160)
+    ap.add_argument("--serve-slots", type=int, default=4)
     return ap.parse_args()
 
 
@@ -536,8 +542,90 @@ def aggregate(ms, edges, device=None):
     return ms, edges, edges / (ms / 1e3)
 
 
+def run_serve(args):
+    """Serving form on one GPU: `--serve-tenants` directed R-MAT tenants with
+    N log-spaced in [1e5, 3e6] (M = 10 N), |S| in [500, 2000], d in {64, 128},
+    each admitted by its HBM footprint and set up with half of its edges;
+    then `--serve-requests` edge batches with sizes log-uniform in
+    [1e3, min(1e5, M / 40)] drawn from the tenants' remaining edges arrive as
+    a Poisson stream (mean gap 30 ms) at random tenants, each followed by an
+    embedding query. Reports p50 / p99 latency (arrival to completion) of the
+    updates, edge updates per second over the stream, and the mean service
+    time per tenant size."""
+    import torch
+    import tsvd_gb300 as T
+    import workloads as W
+    rng = np.random.default_rng(args.seed)
+    device = 0
+    torch.cuda.set_device(device)
+    k = args.serve_tenants
+    ns = np.unique(np.round(np.logspace(5, np.log10(3e6), k)).astype(int))
+    tenants = []
+    with T.Server(device=device, slots=args.serve_slots) as srv:
+        t_setup = time.perf_counter()
+        for i, n in enumerate(ns):
+            cfg = W.scaled("rmat-d-2.7m", n=int(n), m=int(10 * n),
+                           sources=int(rng.integers(500, 2001)), n_parts=16,
+                           rank_d=int(rng.choice([64, 128])), snapshots=2)
+            _, snaps, src = W.build(cfg, seed=args.seed + i)
+            kw = W.session_kwargs(cfg, dynamic_start=2, lazy_start=2)
+            try:
+                tid = srv.add_tenant(cfg["n"], src, cfg["m"], **kw)
+            except T.TsvdError:
+                continue  # not admitted: the HBM budget is spent
+            srv.wait(srv.submit_update(tid, snaps[0]))
+            tenants.append(dict(id=tid, n=int(n), rest=snaps[1], pos=0, cfg=cfg))
+        t_setup = time.perf_counter() - t_setup
+        stats0 = srv.stats()
+        reqs = []
+        t0 = time.perf_counter()
+        next_t = t0
+        with ClockSampler(device) as clk:
+            for r in range(args.serve_requests):
+                ten = tenants[int(rng.integers(len(tenants)))]
+                hi = max(1e3, min(1e5, ten["cfg"]["m"] / 40))
+                size = int(np.exp(rng.uniform(np.log(1e3), np.log(hi))))
+                if ten["pos"] + size > len(ten["rest"]):
+                    ten["pos"] = 0  # wrap: the batch re-inserts earlier pairs as duplicates
+                e = ten["rest"][ten["pos"]:ten["pos"] + size]
+                ten["pos"] += size
+                next_t += rng.exponential(0.03)
+                now = time.perf_counter()
+                if next_t > now:
+                    time.sleep(next_t - now)
+                u = srv.submit_update(ten["id"], e)
+                q = srv.submit_query(ten["id"])
+                reqs.append((ten["n"], len(e), u, q))
+            lat, svc = [], {}
+            for n, m, u, q in reqs:
+                l, sv, _ = srv.wait(u)
+                srv.wait(q)
+                lat.append(l)
+                svc.setdefault(n, []).append(sv)
+            wall = time.perf_counter() - t0
+        edges = sum(m for _, m, _, _ in reqs)
+        st = srv.stats()
+    line = {"metric": "serving: p50/p99 refresh latency & edge updates/s, 1 GB300",
+            "value": edges / wall, "unit": "edge updates/s", "n_gpus": 1,
+            "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+            "requests": len(reqs), "tenants_admitted": len(tenants),
+            "tenants_offered": len(ns), "slots": args.serve_slots,
+            "setup_s": t_setup, "stream_s": wall,
+            "hbm_budget_gb": st["hbm_budget"] / 1e9, "hbm_charged_gb": st["hbm_charged"] / 1e9,
+            "service_ms_mean_by_tenant_n": {str(n): float(np.mean(v)) for n, v in sorted(svc.items())},
+            "clocks": clk.summary(), "higher_is_better": True,
+            "data": "synthetic (seeded R-MAT tenants, Poisson arrivals)",
+            "config": {"workload": "serve-%d-tenants" % len(ns), "tenant_n": [int(x) for x in ns],
+                       "batch_edges": "log-uniform [1e3, min(1e5, M/40)]",
+                       "arrivals": "Poisson, mean gap 30 ms", "alpha": 0.2, "rmax": 1e-7}}
+    print(json.dumps(line))
+
+
 def main():
     args = parse()
+    if args.serve:
+        run_serve(args)
+        return
     if args.impl == "reference":
         run_reference(args)
         return

@@ -189,6 +189,21 @@ enum {
                        /* merge launch sequence per tree node                          */
 };
 
+enum {
+  /* Product path of the mixed form's block frPCA (the plain form always uses
+   * FP32 CSR SpMM, one block at a time). */
+  TSVD_BLOCKS_DENSE = 0,  /* half-precision A^T of the block's non-empty columns,     */
+                          /* tensor-core products, all dirty blocks in one batch      */
+  TSVD_BLOCKS_SPARSE = 1, /* FP32 CSR / CSC of every dirty block, SpMM products in    */
+                          /* one batch                                                */
+  TSVD_BLOCKS_AUTO = 2    /* per block, by density: at the first factorization both   */
+                          /* paths are timed on sample blocks of different density    */
+                          /* and a cost model (dense: per stored cell; sparse: per    */
+                          /* non-zero and per stored cell of the build) gives the     */
+                          /* density below which a block takes the SpMM path; each    */
+                          /* snapshot then runs one dense and one sparse batch        */
+};
+
 typedef struct tsvd_config {
   int32_t n_vertices;       /* N (argv[9] of the reference drivers)                  */
   int32_t directed;         /* 0: UGraph (Tree_u_*), 1: Graph + transpose (Tree_d_*)  */
@@ -224,12 +239,18 @@ typedef struct tsvd_config {
                             /* whose 16 N Sp bytes of state exceed HBM (N 6.2M,       */
                             /* |S| 3000: 305 GB)                                      */
   int32_t form;             /* TSVD_FORM_*: how a snapshot is computed (see below)   */
+  int32_t block_path;       /* TSVD_BLOCKS_*: product path of the mixed form's frPCA */
 } tsvd_config;
 
 /* Fills the reference's defaults (Tree_u_NC, run.sh: alpha .5, q 12, ...). */
 void tsvd_config_default(tsvd_config *cfg);
 
 tsvd_status tsvd_session_create(const tsvd_config *cfg, tsvd_session **out);
+/* Estimated device bytes of a session with this configuration once
+ * expected_edges pairs are inserted (no counterpart in the reference; the
+ * serving layer admits tenants by it). */
+tsvd_status tsvd_session_footprint(const tsvd_config *cfg, int64_t expected_edges,
+                                   int64_t *bytes);
 tsvd_status tsvd_session_destroy(tsvd_session *s);
 
 /* One snapshot (one iteration of the driver loop, Tree_u_NC.cpp:507-866):
@@ -276,6 +297,9 @@ typedef struct tsvd_step_stats {
                             /* columns (max over levels; 0 for narrow merges)    */
   int32_t eig_refine_sweeps;/* sweeps of the fp64 refinement Jacobi (max, all     */
                             /* eigen-solves of the snapshot)                     */
+  int32_t sparse_blocks;    /* blocks factorized through FP32 CSR SpMM            */
+  double tune_density;      /* TSVD_BLOCKS_AUTO: density below which a block takes */
+                            /* the SpMM path (0 before the first factorization)  */
 } tsvd_step_stats;
 tsvd_status tsvd_session_last_stats(tsvd_session *s, tsvd_step_stats *out);
 
@@ -348,6 +372,10 @@ tsvd_status tsvd_graph_adjacency(tsvd_session *s, int32_t dir, int64_t *offsets,
 /* PPR state as |S| x N row-major float: which = 0 residue, 1 reserve. */
 tsvd_status tsvd_ppr_state(tsvd_session *s, int32_t transpose, int32_t which,
                            float *out);
+/* The same for the listed source rows only (count x N row-major float; row i
+ * = source index rows[i]), for sampled checks of large sessions. */
+tsvd_status tsvd_ppr_state_rows(tsvd_session *s, int32_t transpose, int32_t which,
+                                const int32_t *rows, int32_t count, float *out);
 /* Per-block numbers: ||A||_F, ||A-A_old||_F, residual, nnz(A), dirty flag. */
 tsvd_status tsvd_block_info(tsvd_session *s, double *norm_a, double *norm_diff,
                             double *resid, int64_t *nnz, uint8_t *dirty);
@@ -356,6 +384,53 @@ tsvd_status tsvd_tree_factor(tsvd_session *s, int32_t node, double *out,
                              double *sigma);
 /* Dense log-transformed block b as |S| x n_b row-major float (tests). */
 tsvd_status tsvd_block_dense(tsvd_session *s, int32_t b, float *out);
+
+/* ------------------------------------------------------------------------- */
+/* Serving: many tenants on one GPU, requests taken as they arrive.            */
+/* No counterpart in the reference (its drivers refresh one graph from a list  */
+/* of delta files). A tenant is one session; it is admitted when its          */
+/* estimated footprint fits in the HBM budget left, and charged the larger of */
+/* that estimate and the device memory its creation took. `slots` worker      */
+/* threads each take the oldest waiting request whose tenant is idle, so      */
+/* requests start as soon as a slot and their tenant are free and different   */
+/* tenants' snapshots overlap on the device (one stream per session).         */
+/* Thread-safe: any thread may submit or wait.                                */
+/* ------------------------------------------------------------------------- */
+typedef struct tsvd_server tsvd_server;
+typedef struct tsvd_server_stats_t {
+  int64_t updates;       /* completed edge-update requests                 */
+  int64_t edges;         /* edges they applied                             */
+  double p50_ms, p99_ms; /* update latency, submission to completion       */
+  double edges_per_s;    /* edges over first submission .. last completion */
+  int64_t hbm_budget, hbm_charged;
+  int32_t tenants;
+} tsvd_server_stats_t;
+
+/* hbm_budget_bytes <= 0: the free device memory now, less 4 GB. */
+tsvd_status tsvd_server_create(int32_t device, int64_t hbm_budget_bytes, int32_t slots,
+                               tsvd_server **out);
+/* TSVD_ERR_OOM when the tenant does not fit in the budget left (nothing is
+ * allocated then). expected_edges sizes the footprint estimate. */
+tsvd_status tsvd_server_add_tenant(tsvd_server *sv, const tsvd_config *cfg,
+                                   int64_t expected_edges, int32_t *tenant);
+/* Waits for the tenant's queued requests, then frees its session and budget. */
+tsvd_status tsvd_server_remove_tenant(tsvd_server *sv, int32_t tenant);
+/* One snapshot of m (from, to) pairs (copied at submission). */
+tsvd_status tsvd_server_submit_update(tsvd_server *sv, int32_t tenant, const int32_t *edges,
+                                      int64_t m, int64_t *request);
+/* The tenant's embedding (|S| x d doubles into out, which must stay valid
+ * until the request completes) after every update submitted before it. */
+tsvd_status tsvd_server_submit_query(tsvd_server *sv, int32_t tenant, double *out,
+                                     int64_t *request);
+/* Blocks until the request completes; its status, latency (submission to
+ * completion) and service time (start to completion). */
+tsvd_status tsvd_server_wait(tsvd_server *sv, int64_t request, double *latency_ms,
+                             double *service_ms);
+tsvd_status tsvd_server_drain(tsvd_server *sv);
+tsvd_status tsvd_server_stats(tsvd_server *sv, tsvd_server_stats_t *out);
+/* The tenant's session (inspection; do not step it while requests run). */
+tsvd_status tsvd_server_session(tsvd_server *sv, int32_t tenant, tsvd_session **out);
+tsvd_status tsvd_server_destroy(tsvd_server *sv);
 
 /* ------------------------------------------------------------------------- */
 /* Synthetic inputs (seeded; stand in for the reference's datasets).           */

@@ -1,0 +1,68 @@
+"""Block product paths of the mixed form: every dirty block on the tensor
+cores (TSVD_BLOCKS_DENSE), every dirty block through FP32 SpMM over its
+half-precision values (TSVD_BLOCKS_SPARSE), or per block by the density the
+autotuner measured (TSVD_BLOCKS_AUTO), on a degree-sorted graph whose
+blocks range from dense (the hubs) to nearly empty. The two paths multiply
+the same values, so the three sessions agree with each other to rounding,
+and each agrees with the oracle run on its own reserve."""
+import numpy as np
+import pytest
+
+import tsvd_gb300 as T
+import workloads as W
+from helpers import gap_index, gram_rel_err
+from oracle.tree_oracle import OracleTreeSVD
+
+pytestmark = pytest.mark.gpu
+
+
+def test_block_paths_agree_on_a_degree_sorted_graph():
+    cfg = W.scaled("rmat-u-3.2m-deg", n=40000, m=200000, sources=128, n_parts=32, rank_d=32,
+                   snapshots=4)
+    cfg["rmax"] = 1e-6
+    _, snaps, src = W.build(cfg, seed=51)
+    kw = W.session_kwargs(cfg, dynamic_start=2, lazy_start=2)
+    okw = dict(kw)
+    okw.pop("seed")
+    okw.pop("block_path")
+    out = {}
+    for path in (T.BLOCKS_DENSE, T.BLOCKS_SPARSE, T.BLOCKS_AUTO):
+        kw["block_path"] = path
+        iso = OracleTreeSVD(cfg["n"], src, seed=kw["seed"], **okw)
+        embs, sigs, stats, dirties = [], [], [], []
+        with T.Session(cfg["n"], src, **kw) as s:
+            for e in snaps:
+                st = s.step(e)
+                p = s.ppr_state(False, 1).astype(np.float64)
+                emb_o = iso.step(e, reserve=p)
+                emb = s.embedding()
+                _, sig = s.tree_factor(0)
+                if np.array_equal(s.block_info()["dirty"], iso.dirty):
+                    assert np.allclose(sig[:16], iso.sigma[0][:16], rtol=1e-3)
+                    assert gram_rel_err(emb, emb_o) < 5e-3
+                embs.append(emb)
+                sigs.append(sig)
+                stats.append(st)
+                dirties.append(s.block_info()["dirty"].copy())
+            nnz = s.block_info()["nnz"]
+        out[path] = (embs, sigs, stats, dirties)
+        if path == T.BLOCKS_SPARSE:
+            assert all(st["sparse_blocks"] == st["factorized_blocks"] for st in stats)
+        if path == T.BLOCKS_DENSE:
+            assert all(st["sparse_blocks"] == 0 for st in stats)
+    nz = nnz[nnz > 0]
+    print("block nnz: max %d, min %d (x%.0f); autotuner density threshold %.3g, sparse blocks %s"
+          % (nz.max(), nz.min(), nz.max() / nz.min(), out[T.BLOCKS_AUTO][2][-1]["tune_density"],
+             [st["sparse_blocks"] for st in out[T.BLOCKS_AUTO][2]]))
+    assert nz.max() >= 100 * nz.min()  # the blocks are skewed as intended
+    assert out[T.BLOCKS_AUTO][2][0]["tune_density"] > 0
+    # same values, same Gaussian: the sessions agree to rounding (while their
+    # lazy decisions agree: a near-tie may fall either way on rounding)
+    for path in (T.BLOCKS_SPARSE, T.BLOCKS_AUTO):
+        for k in range(len(snaps)):
+            if not np.array_equal(out[path][3][k], out[T.BLOCKS_DENSE][3][k]):
+                break
+            sd, sp_ = out[T.BLOCKS_DENSE][1][k], out[path][1][k]
+            j = gap_index(sd, cfg["rank_d"])
+            assert np.allclose(sp_[:j], sd[:j], rtol=1e-4), (path, k)
+            assert gram_rel_err(out[path][0][k], out[T.BLOCKS_DENSE][0][k]) < 1e-3

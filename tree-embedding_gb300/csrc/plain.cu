@@ -202,9 +202,21 @@ __device__ __forceinline__ float block_transform(float x, const BlockSource &a) 
   }
 }
 
-// The four transformed values of sources s0..s0+3 of column v (the same
-// fp32 expression the block materialization rounds to half precision).
-__device__ __forceinline__ void cell4(const BlockSource &a, int32_t v, int32_t s0, float *out) {
+// The four values of sources s0..s0+3 of compacted column c (vertex v): the
+// stored half-precision A^T, or the transform of the reserve (the same fp32
+// expression the block materialization rounds to half precision).
+__device__ __forceinline__ void cell4(const BlockSource &a, int64_t c, int32_t v, int32_t s0,
+                                      float *out) {
+  if (a.at) {
+    const uint2 raw = *reinterpret_cast<const uint2 *>(a.at + c * a.sp + s0);
+    const __half2 h01 = *reinterpret_cast<const __half2 *>(&raw.x);
+    const __half2 h23 = *reinterpret_cast<const __half2 *>(&raw.y);
+    out[0] = __low2float(h01);
+    out[1] = __high2float(h01);
+    out[2] = __low2float(h23);
+    out[3] = __high2float(h23);
+    return;
+  }
   const int64_t cell = ppr_cell(v, s0, a.n);
   float4 x = __ldcs(reinterpret_cast<const float4 *>(a.p1 + cell));
   if (a.p2) {
@@ -227,12 +239,12 @@ __global__ void __launch_bounds__(256) csc_kernel(BlockSource a, int32_t *cnt,
   const int64_t gw = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
   for (int64_t c = gw; c < a.ncols; c += nw) {
-    const int32_t v = a.colmap[c];
+    const int32_t v = a.at ? 0 : a.colmap[c];
     int64_t pos = PASS ? colptr[c] : 0;
     int32_t total = 0;
     for (int32_t s0 = lane * 4; s0 < a.sp; s0 += 128) {
       float x[4];
-      cell4(a, v, s0, x);
+      cell4(a, c, v, s0, x);
       const int mine = (x[0] != 0.f) + (x[1] != 0.f) + (x[2] != 0.f) + (x[3] != 0.f);
       int incl = mine;
 #pragma unroll

@@ -68,11 +68,15 @@ struct PlainBlockWork {
   size_t tmp_bytes = 0;
 };
 
+// Where a block's values come from: the log transform of the reserve in fp32
+// (plain form), or the accepted half-precision A^T of the mixed form (then
+// the sparse and the tensor-core paths multiply exactly the same values).
 struct BlockSource {
-  const float *p1, *p2;      // reserve (forward, reverse or null), chunk-major
-  const int32_t *colmap;     // compacted column -> vertex, for this block
-  int32_t ncols, n, sp, nsrc, transform;
-  float rmin_f, inv_rmin_f, n_f;
+  const float *p1 = nullptr, *p2 = nullptr;  // reserve (forward, reverse or null), chunk-major
+  const int32_t *colmap = nullptr;           // compacted column -> vertex, for this block
+  const __half *at = nullptr;                // or: A^T [ncols][sp] (then p1, p2 unused)
+  int32_t ncols = 0, n = 0, sp = 0, nsrc = 0, transform = 0;
+  float rmin_f = 0.f, inv_rmin_f = 0.f, n_f = 0.f;
 };
 
 tsvd_status plain_block_build(PlainBlockWork &W, const BlockSource &src, int64_t nnz_hint,

@@ -106,6 +106,11 @@ struct tsvd_session {
   int form = TSVD_FORM_MIXED;
   PlainPpr plain[2];
   PlainBlockWork pbw;
+  // block-path autotuner and the sparse batch's CSR / CSC (mixed form)
+  std::vector<PlainBlockWork> sbw;
+  bool tuned = false;
+  double tune_density = 0.0;
+  cudaEvent_t tev[2]{};           // the autotuner's trial timings
 
   size_t node_elems() const { return (size_t)S * d; }
   float *node_b(int i) { return tree_b + (size_t)i * node_elems(); }
@@ -229,6 +234,7 @@ static tsvd_status session_alloc(tsvd_session *s) {
   TSVD_CUDA(cudaStreamCreateWithPriority(&s->st, cudaStreamNonBlocking, prio_high));
   TSVD_CUDA(cudaStreamCreateWithPriority(&s->st2, cudaStreamNonBlocking, prio_low));
   for (auto &e : s->ev) TSVD_CUDA(cudaEventCreate(&e));
+  for (auto &e : s->tev) TSVD_CUDA(cudaEventCreate(&e));
   for (auto &set : s->pev)
     for (auto &e : set) TSVD_CUDA(cudaEventCreate(&e));
   const int ndir = s->directed ? 2 : 1;
@@ -330,8 +336,11 @@ static void session_release(tsvd_session *s) {
   for (int dd = 0; dd < 2; ++dd)
     if (s->plain[dd].cbits) plain_free(s->plain[dd]);
   plain_block_free(s->pbw);
+  for (auto &w : s->sbw) plain_block_free(w);
   cudaFreeHost(s->emb_stage);
   for (auto &e : s->ev)
+    if (e) cudaEventDestroy(e);
+  for (auto &e : s->tev)
     if (e) cudaEventDestroy(e);
   for (auto &set : s->pev)
     for (auto &e : set)
@@ -364,6 +373,8 @@ extern "C" tsvd_status tsvd_session_create(const tsvd_config *cfg, tsvd_session 
     return fail(TSVD_ERR_INVALID, "bad transform or dirty rule");
   if (c.form != TSVD_FORM_MIXED && c.form != TSVD_FORM_PLAIN)
     return fail(TSVD_ERR_INVALID, "form must be TSVD_FORM_MIXED or TSVD_FORM_PLAIN");
+  if (c.block_path < TSVD_BLOCKS_DENSE || c.block_path > TSVD_BLOCKS_AUTO)
+    return fail(TSVD_ERR_INVALID, "block_path must be one of TSVD_BLOCKS_*");
   if (c.lp_right_factor && c.root_scaling != TSVD_ROOT_U)
     return fail(TSVD_ERR_INVALID, "lp_right_factor needs root_scaling TSVD_ROOT_U (LP drivers)");
   std::vector<int32_t> src(c.sources, c.sources + c.n_sources);
@@ -399,6 +410,42 @@ extern "C" tsvd_status tsvd_session_create(const tsvd_config *cfg, tsvd_session 
     return fail(st, "%s", msg.c_str());
   }
   *out = s;
+  return TSVD_OK;
+}
+
+// Device bytes a session with this configuration holds once expected_edges
+// pairs are inserted (the allocations of session_alloc, ppr_alloc and
+// frpca_work_alloc; the adjacency with its 50 % slack; one insert's sort
+// buffers). Used by the serving layer to admit tenants by HBM footprint.
+extern "C" tsvd_status tsvd_session_footprint(const tsvd_config *c, int64_t expected_edges,
+                                              int64_t *bytes) {
+  if (!c || !bytes || c->n_vertices < 1 || c->n_sources < 1 || c->n_parts < 1 ||
+      expected_edges < 0)
+    return fail(TSVD_ERR_INVALID, "footprint: bad arguments");
+  const double n = c->n_vertices, sp = (double)round_up(c->n_sources, kRowPad);
+  const double S = c->n_sources, d = c->rank_d, P = c->n_parts;
+  const double chunks = sp / 64.0, dirs = c->directed ? 2 : 1;
+  const double entries = (c->directed ? 1.0 : 2.0) * expected_edges;  // per direction list
+  double b = 0;
+  b += dirs * (8 * (n + 1) + 8 * n + 1.5 * 4 * entries);            // adjacency
+  b += 16.0 * expected_edges / 8 + 16.0 * entries;                     // insert staging, sort
+  const double state = 4 * n * sp;
+  b += dirs * (state * (c->ppr_host_reserve ? 1 : 2));                 // r (+ p)
+  b += dirs * (2 * n * chunks / 8 + 2 * 8 * n * chunks + 4 * n);       // bitsets, frontiers
+  b += dirs * ((1 << 20) * 64 * 4.0 + (1 << 20) * 8.0 + (1 << 22) * 8.0);  // hub units
+  b += 2 * 2 * n * sp + 13 * n;                                         // A^T blocks, maps
+  int levels = 1;
+  for (int t = c->n_parts; t > 1 && c->hierarchy_n > 1; t /= c->hierarchy_n) ++levels;
+  double nodes = 0, pw = 1;
+  for (int i = 0; i < levels; ++i, pw *= c->hierarchy_n) nodes += pw;
+  b += nodes * S * d * 4 + nodes * d * 4 + S * d * 4;                   // tree factors
+  const double rows_max = n - (P - 1) * std::floor(n / P) + 1;
+  b += P * rows_max * kLp * 8 + P * sp * 256 * 4;                      // X hi/lo, Z
+  b += P * sp * kLp * 8 + P * 65536 * (8 + 4 + 24) + P * 2048 * 4;     // Y, Q, G, V, refine
+  b += (std::min(P * std::ceil(std::max(rows_max, sp) / 128), 2048.0) + P) * 65536 * 8;  // Grams
+  b += P * 30.0 * 255 * 128 * 8;                                        // Jacobi rotation logs
+  if (c->lp_right_factor) b += n * kLp * 4 + P * S * d * 4 + 8 * n;
+  *bytes = (int64_t)(b * 1.05) + (64ll << 20);
   return TSVD_OK;
 }
 
@@ -577,6 +624,126 @@ static void make_job(const tsvd_session *s, int iter, FactorJob &job) {
   job.stats = s->last;
 }
 
+// The sparse path of the mixed form: block b's accepted half-precision A^T
+// compressed into CSR / CSC (the tensor-core path's values, exactly).
+static BlockSource at_source(const tsvd_session *s, const FactorJob &job, int b) {
+  BlockSource src;
+  src.at = const_cast<tsvd_session *>(s)->at_block(job.atcur[b], b);
+  src.colmap = s->colmap + (size_t)b * s->col_dim;
+  src.ncols = job.ncols[b];
+  src.n = s->n;
+  src.sp = s->sp;
+  src.nsrc = s->S;
+  return src;
+}
+
+// Block-path autotuner (TSVD_BLOCKS_AUTO), run at the first factorization:
+// up to three dirty blocks spanning the density range are factorized alone
+// through both paths, timed with events. Dense cost is modelled per stored
+// cell (Sp x n_c: every pass streams the half-precision A^T), sparse cost per
+// non-zero (the SpMM gathers) plus per stored cell (the CSR / CSC build reads
+// the block once per pass of the build); the crossover density follows.
+static tsvd_status tune_block_paths(tsvd_session *s, const FactorJob &job,
+                                    const std::vector<FrpcaProblem> &probs, cudaStream_t st) {
+  const int nf = (int)job.factor_now.size();
+  std::vector<int> order(nf);
+  std::vector<double> dens(nf);
+  for (int i = 0; i < nf; ++i) {
+    const int b = job.factor_now[i];
+    order[i] = i;
+    dens[i] = (double)s->nnz_h[b] / std::max(1.0, (double)s->S * job.ncols[b]);
+  }
+  std::sort(order.begin(), order.end(), [&](int a, int b) { return dens[a] > dens[b]; });
+  std::vector<int> pick;
+  for (int q : {0, nf / 2, nf - 1})
+    if (std::find(pick.begin(), pick.end(), order[q]) == pick.end()) pick.push_back(order[q]);
+  cudaEvent_t e0 = s->tev[0], e1 = s->tev[1];
+  double sd = 0, sc = 0;                      // dense: time over cells
+  double a11 = 0, a12 = 0, a22 = 0, r1 = 0, r2 = 0;  // sparse: least squares in (nnz, cells)
+  if (s->sbw.empty()) s->sbw.resize(1);
+  for (int i : pick) {
+    const int b = job.factor_now[i];
+    FrpcaProblem P = probs[i];
+    P.b_out = nullptr;  // a trial: results dropped
+    P.sigma_out = nullptr;
+    const double cells = (double)s->sp * job.ncols[b], nnz = (double)s->nnz_h[b];
+    double ss = 0;
+    TSVD_CUDA(cudaEventRecord(e0, st));
+    TSVD_TRY(frpca_batch(s->fw, &P, 1, s->q, s->cfg.seed, s->S, st, &ss));
+    TSVD_CUDA(cudaEventRecord(e1, st));
+    TSVD_CUDA(cudaEventSynchronize(e1));
+    const double td = ms_between(e0, e1);
+    TSVD_CUDA(cudaEventRecord(e0, st));
+    TSVD_TRY(plain_block_build(s->sbw[0], at_source(s, job, b), s->nnz_h[b], st));
+    P.sparse = &s->sbw[0].blk;
+    TSVD_TRY(frpca_batch(s->fw, &P, 1, s->q, s->cfg.seed, s->S, st, &ss));
+    TSVD_CUDA(cudaEventRecord(e1, st));
+    TSVD_CUDA(cudaEventSynchronize(e1));
+    const double ts = ms_between(e0, e1);
+    sd += td;
+    sc += cells;
+    a11 += nnz * nnz; a12 += nnz * cells; a22 += cells * cells;
+    r1 += nnz * ts; r2 += cells * ts;
+  }
+  const double cd = sd / std::max(sc, 1.0);
+  double c1, c2;
+  const double det = a11 * a22 - a12 * a12;
+  if (pick.size() >= 2 && std::fabs(det) > 1e-12 * a11 * a22) {
+    c1 = (r1 * a22 - r2 * a12) / det;
+    c2 = (a11 * r2 - a12 * r1) / det;
+  } else {
+    c1 = r1 / std::max(a11, 1.0);  // one point: all of it per non-zero
+    c2 = 0;
+  }
+  c1 = std::max(c1, 1e-30);
+  c2 = std::max(c2, 0.0);
+  // sparse is cheaper while c1 rho S + c2 < cd (per stored cell, rho S / Sp ~ rho)
+  s->tune_density = std::max(0.0, (cd - c2) / c1) * ((double)s->sp / s->S);
+  s->tuned = true;
+  return TSVD_OK;
+}
+
+// Mixed form with TSVD_BLOCKS_SPARSE / TSVD_BLOCKS_AUTO: one batch of dense
+// blocks on the tensor cores and one batch of sparse blocks through SpMM.
+static tsvd_status factorize_two_paths(tsvd_session *s, FactorJob &job,
+                                       std::vector<FrpcaProblem> &probs,
+                                       std::vector<double> &ssum, cudaStream_t st) {
+  const int nf = (int)job.factor_now.size();
+  if (s->cfg.block_path == TSVD_BLOCKS_AUTO && !s->tuned)
+    TSVD_TRY(tune_block_paths(s, job, probs, st));
+  std::vector<int> di, si;
+  for (int i = 0; i < nf; ++i) {
+    const int b = job.factor_now[i];
+    const double rho = (double)s->nnz_h[b] / std::max(1.0, (double)s->S * job.ncols[b]);
+    const bool sparse = s->cfg.block_path == TSVD_BLOCKS_SPARSE || rho < s->tune_density;
+    (sparse ? si : di).push_back(i);
+  }
+  if (!di.empty()) {
+    std::vector<FrpcaProblem> pd;
+    for (int i : di) pd.push_back(probs[i]);
+    std::vector<double> sd(di.size());
+    TSVD_TRY(frpca_batch(s->fw, pd.data(), (int)pd.size(), s->q, s->cfg.seed, s->S, st, sd.data()));
+    for (size_t k = 0; k < di.size(); ++k) ssum[di[k]] = sd[k];
+  }
+  if (!si.empty()) {
+    if (s->sbw.size() < si.size()) s->sbw.resize(si.size());
+    std::vector<FrpcaProblem> ps;
+    for (size_t k = 0; k < si.size(); ++k) {
+      const int b = job.factor_now[si[k]];
+      TSVD_TRY(plain_block_build(s->sbw[k], at_source(s, job, b), s->nnz_h[b], st));
+      FrpcaProblem P = probs[si[k]];
+      P.sparse = &s->sbw[k].blk;
+      ps.push_back(P);
+    }
+    std::vector<double> sv(si.size());
+    TSVD_TRY(frpca_batch(s->fw, ps.data(), (int)ps.size(), s->q, s->cfg.seed, s->S, st, sv.data()));
+    for (size_t k = 0; k < si.size(); ++k) ssum[si[k]] = sv[k];
+  }
+  job.stats.sparse_blocks = (int)si.size();
+  job.stats.tune_density = s->tune_density;
+  return TSVD_OK;
+}
+
 static tsvd_status stage_factorize(tsvd_session *s, FactorJob &job, cudaStream_t st) {
   const int nf = (int)job.factor_now.size();
   job.stats.factorized_blocks = nf;
@@ -618,8 +785,10 @@ static tsvd_status stage_factorize(tsvd_session *s, FactorJob &job, cudaStream_t
       TSVD_TRY(frpca_batch(s->fw, &probs[i], 1, s->q, s->cfg.seed, s->S, st, &ssum[i]));
       job.stats.eig_refine_sweeps = std::max(job.stats.eig_refine_sweeps, s->fw.last_refine_sweeps);
     }
-  } else {
+  } else if (s->cfg.block_path == TSVD_BLOCKS_DENSE) {
     TSVD_TRY(frpca_batch(s->fw, probs.data(), nf, s->q, s->cfg.seed, s->S, st, ssum.data()));
+  } else {
+    TSVD_TRY(factorize_two_paths(s, job, probs, ssum, st));
   }
   job.stats.eig_sweeps_frpca = s->fw.last_sweeps;
   job.stats.eig_refine_sweeps = std::max(job.stats.eig_refine_sweeps, s->fw.last_refine_sweeps);
@@ -1145,6 +1314,55 @@ extern "C" tsvd_status tsvd_ppr_state(tsvd_session *s, int32_t transpose, int32_
   for (int v = 0; v < s->n; ++v)
     for (int k = 0; k < s->S; ++k) out[(size_t)k * s->n + v] = tmp[ppr_cell(v, k, s->n)];
   return TSVD_OK;
+}
+
+namespace {
+// out[i][v] = state cell (v, rows[i]) for the listed source rows
+__global__ void gather_rows_kernel(const float *__restrict__ x, const int32_t *__restrict__ rows,
+                                   int32_t count, int32_t n, float *__restrict__ out) {
+  const int64_t total = (int64_t)count * n;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t k = (int32_t)(i / n), v = (int32_t)(i % n);
+    out[i] = x[ppr_cell(v, rows[k], n)];
+  }
+}
+}  // namespace
+
+extern "C" tsvd_status tsvd_ppr_state_rows(tsvd_session *s, int32_t transpose, int32_t which,
+                                           const int32_t *rows, int32_t count, float *out) {
+  if (!s || !out || !rows || count < 1 || (transpose && !s->directed))
+    return fail(TSVD_ERR_INVALID, "bad arguments");
+  for (int32_t i = 0; i < count; ++i)
+    if (rows[i] < 0 || rows[i] >= s->S) return fail(TSVD_ERR_INVALID, "row %d out of range", rows[i]);
+  TSVD_CUDA(cudaSetDevice(s->cfg.device));
+  TSVD_CUDA(cudaStreamSynchronize(s->st));
+  const PprState &P = s->ppr[transpose ? 1 : 0];
+  int32_t *drows = nullptr;
+  float *dout = nullptr;
+  TSVD_CUDA(cudaMalloc(&drows, sizeof(int32_t) * count));
+  if (cudaMalloc(&dout, sizeof(float) * (size_t)count * s->n) != cudaSuccess) {
+    cudaGetLastError();
+    cudaFree(drows);
+    return fail(TSVD_ERR_OOM, "ppr_state_rows: %d rows", count);
+  }
+  tsvd_status st = TSVD_OK;
+  if (cudaMemcpyAsync(drows, rows, sizeof(int32_t) * count, cudaMemcpyHostToDevice, s->st) !=
+      cudaSuccess)
+    st = fail(TSVD_ERR_DEVICE, "ppr_state_rows: copy");
+  if (st == TSVD_OK) {
+    gather_rows_kernel<<<grid_for((int64_t)count * s->n, 256), 256, 0, s->st>>>(
+        which ? P.p : P.r, drows, count, s->n, dout);
+    count_launch();
+    if (cudaGetLastError() != cudaSuccess ||
+        cudaMemcpyAsync(out, dout, sizeof(float) * (size_t)count * s->n, cudaMemcpyDeviceToHost,
+                        s->st) != cudaSuccess ||
+        cudaStreamSynchronize(s->st) != cudaSuccess)
+      st = fail(TSVD_ERR_DEVICE, "ppr_state_rows: gather");
+  }
+  cudaFree(drows);
+  cudaFree(dout);
+  return st;
 }
 
 extern "C" tsvd_status tsvd_block_info(tsvd_session *s, double *norm_a, double *norm_diff,

@@ -17,6 +17,7 @@ DIRTY_REFERENCE, DIRTY_FROBENIUS, DIRTY_ALL = 0, 1, 2
 ROOT_SQRT_SIGMA, ROOT_U = 0, 1
 REFRESH_EXACT, REFRESH_INTDIV = 0, 1
 FORM_MIXED, FORM_PLAIN = 0, 1
+BLOCKS_DENSE, BLOCKS_SPARSE, BLOCKS_AUTO = 0, 1, 2
 
 STATUS = {0: "ok", 1: "invalid argument", 2: "out of memory", 3: "device error",
           4: "timeout", 5: "bad state", 6: "i/o error", 7: "numeric error"}
@@ -44,6 +45,7 @@ class Config(ctypes.Structure):
         ("push_levels", ctypes.c_int32), ("push_ratio", ctypes.c_double),
         ("push_cofrac", ctypes.c_double), ("lp_right_factor", ctypes.c_int32),
         ("ppr_host_reserve", ctypes.c_int32), ("form", ctypes.c_int32),
+        ("block_path", ctypes.c_int32),
     ]
 
 
@@ -62,6 +64,7 @@ class StepStats(ctypes.Structure):
         ("push_item_edges", ctypes.c_int64), ("ms_lp", ctypes.c_double),
         ("eig_sweeps_frpca", ctypes.c_int32), ("eig_sweeps_merge", ctypes.c_int32),
         ("merge_subspace_iters", ctypes.c_int32), ("eig_refine_sweeps", ctypes.c_int32),
+        ("sparse_blocks", ctypes.c_int32), ("tune_density", ctypes.c_double),
     ]
 
     def as_dict(self):
@@ -82,6 +85,22 @@ _SIGS = {
     "tsvd_launch_count": (ctypes.c_int64, []),
     "tsvd_session_stream": (ctypes.c_int, [_vp, ctypes.POINTER(_vp)]),
     "tsvd_session_set_form": (ctypes.c_int, [_vp, ctypes.c_int32]),
+    "tsvd_session_footprint": (ctypes.c_int, [ctypes.POINTER(Config), ctypes.c_int64,
+                                              ctypes.POINTER(ctypes.c_int64)]),
+    "tsvd_server_create": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int64, ctypes.c_int32,
+                                          ctypes.POINTER(_vp)]),
+    "tsvd_server_add_tenant": (ctypes.c_int, [_vp, ctypes.POINTER(Config), ctypes.c_int64,
+                                              ctypes.POINTER(ctypes.c_int32)]),
+    "tsvd_server_remove_tenant": (ctypes.c_int, [_vp, ctypes.c_int32]),
+    "tsvd_server_submit_update": (ctypes.c_int, [_vp, ctypes.c_int32, _i32p, ctypes.c_int64,
+                                                 ctypes.POINTER(ctypes.c_int64)]),
+    "tsvd_server_submit_query": (ctypes.c_int, [_vp, ctypes.c_int32, _f64p,
+                                                ctypes.POINTER(ctypes.c_int64)]),
+    "tsvd_server_wait": (ctypes.c_int, [_vp, ctypes.c_int64, _f64p, _f64p]),
+    "tsvd_server_drain": (ctypes.c_int, [_vp]),
+    "tsvd_server_stats": (ctypes.c_int, [_vp, ctypes.c_void_p]),
+    "tsvd_server_session": (ctypes.c_int, [_vp, ctypes.c_int32, ctypes.POINTER(_vp)]),
+    "tsvd_server_destroy": (ctypes.c_int, [_vp]),
     "tsvd_set_frpca_seed": (None, [ctypes.c_uint64]),
     "tsvd_frpca": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.c_int64, _i64p, _i32p,
                                   _f64p, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
@@ -115,6 +134,8 @@ _SIGS = {
     "tsvd_graph_degrees": (ctypes.c_int, [_vp, ctypes.c_int32, _i32p, _i32p]),
     "tsvd_graph_adjacency": (ctypes.c_int, [_vp, ctypes.c_int32, _i64p, _i32p, ctypes.c_int64]),
     "tsvd_ppr_state": (ctypes.c_int, [_vp, ctypes.c_int32, ctypes.c_int32, _f32p]),
+    "tsvd_ppr_state_rows": (ctypes.c_int, [_vp, ctypes.c_int32, ctypes.c_int32, _i32p,
+                                           ctypes.c_int32, _f32p]),
     "tsvd_block_info": (ctypes.c_int, [_vp, _f64p, _f64p, _f64p, _i64p, _u8p]),
     "tsvd_tree_factor": (ctypes.c_int, [_vp, ctypes.c_int32, _f64p, _f64p]),
     "tsvd_block_dense": (ctypes.c_int, [_vp, ctypes.c_int32, _f32p]),
@@ -251,6 +272,46 @@ def merge_svd(M, d):
 
 
 # ----------------------------------------------------------------- session
+def make_config(n_vertices, sources, directed=False, alpha=0.5, rmax=1e-7, n_parts=64,
+                hierarchy_n=2, rank_d=128, oversample=5, passes_q=12, dynamic_ppr_start_iter=100,
+                lazy_update_start_iter=100, delta=0.3, transform=TRANSFORM_LOG10_NC,
+                dirty_rule=DIRTY_REFERENCE, dirty_frac=0.01, root_scaling=ROOT_SQRT_SIGMA,
+                refresh_mode=REFRESH_EXACT, seed=20231, device=0, max_push_rounds=0,
+                push_levels=1, push_ratio=8.0, push_cofrac=0.85, lp_right_factor=False,
+                ppr_host_reserve=False, form=FORM_MIXED, block_path=BLOCKS_DENSE):
+    """A tsvd_config; `sources` (int32, contiguous) must outlive it."""
+    c = Config()
+    lib().tsvd_config_default(ctypes.byref(c))
+    c.n_vertices, c.directed = int(n_vertices), int(directed)
+    c.n_sources = len(sources)
+    c.sources = _p(sources, _i32p)
+    c.alpha, c.rmax = float(alpha), float(rmax)
+    c.n_parts, c.hierarchy_n = int(n_parts), int(hierarchy_n)
+    c.rank_d, c.oversample, c.passes_q = int(rank_d), int(oversample), int(passes_q)
+    c.dynamic_ppr_start_iter = int(dynamic_ppr_start_iter)
+    c.lazy_update_start_iter = int(lazy_update_start_iter)
+    c.delta = float(delta)
+    c.transform, c.dirty_rule, c.dirty_frac = int(transform), int(dirty_rule), float(dirty_frac)
+    c.root_scaling, c.refresh_mode = int(root_scaling), int(refresh_mode)
+    c.seed, c.device, c.max_push_rounds = int(seed), int(device), int(max_push_rounds)
+    c.push_levels, c.push_ratio = int(push_levels), float(push_ratio)
+    c.push_cofrac = float(push_cofrac)
+    c.lp_right_factor = int(bool(lp_right_factor))
+    c.ppr_host_reserve = int(bool(ppr_host_reserve))
+    c.form = int(form)
+    c.block_path = int(block_path)
+    return c
+
+
+def footprint(n_vertices, sources, expected_edges, **kw):
+    """tsvd_session_footprint: estimated device bytes of such a session."""
+    src = np.ascontiguousarray(sources, dtype=np.int32)
+    c = make_config(n_vertices, src, **kw)
+    out = ctypes.c_int64()
+    _check(lib().tsvd_session_footprint(ctypes.byref(c), int(expected_edges), ctypes.byref(out)))
+    return out.value
+
+
 class Session:
     """A device-resident Tree-SVD state: graph store, PPR store, block factors, tree."""
 
@@ -260,37 +321,40 @@ class Session:
                  transform=TRANSFORM_LOG10_NC, dirty_rule=DIRTY_REFERENCE, dirty_frac=0.01,
                  root_scaling=ROOT_SQRT_SIGMA, refresh_mode=REFRESH_EXACT, seed=20231, device=0,
                  max_push_rounds=0, push_levels=1, push_ratio=8.0, push_cofrac=0.85,
-                 lp_right_factor=False, ppr_host_reserve=False, form=FORM_MIXED):
+                 lp_right_factor=False, ppr_host_reserve=False, form=FORM_MIXED,
+                 block_path=BLOCKS_DENSE):
         self.sources = np.ascontiguousarray(sources, dtype=np.int32)
-        c = Config()
-        lib().tsvd_config_default(ctypes.byref(c))
-        c.n_vertices, c.directed = int(n_vertices), int(directed)
-        c.n_sources = len(self.sources)
-        c.sources = _p(self.sources, _i32p)
-        c.alpha, c.rmax = float(alpha), float(rmax)
-        c.n_parts, c.hierarchy_n = int(n_parts), int(hierarchy_n)
-        c.rank_d, c.oversample, c.passes_q = int(rank_d), int(oversample), int(passes_q)
-        c.dynamic_ppr_start_iter = int(dynamic_ppr_start_iter)
-        c.lazy_update_start_iter = int(lazy_update_start_iter)
-        c.delta = float(delta)
-        c.transform, c.dirty_rule, c.dirty_frac = int(transform), int(dirty_rule), float(dirty_frac)
-        c.root_scaling, c.refresh_mode = int(root_scaling), int(refresh_mode)
-        c.seed, c.device, c.max_push_rounds = int(seed), int(device), int(max_push_rounds)
-        c.push_levels, c.push_ratio = int(push_levels), float(push_ratio)
-        c.push_cofrac = float(push_cofrac)
-        c.lp_right_factor = int(bool(lp_right_factor))
-        c.ppr_host_reserve = int(bool(ppr_host_reserve))
-        c.form = int(form)
+        c = make_config(n_vertices, self.sources, directed, alpha, rmax, n_parts, hierarchy_n,
+                        rank_d, oversample, passes_q, dynamic_ppr_start_iter,
+                        lazy_update_start_iter, delta, transform, dirty_rule, dirty_frac,
+                        root_scaling, refresh_mode, seed, device, max_push_rounds, push_levels,
+                        push_ratio, push_cofrac, lp_right_factor, ppr_host_reserve, form,
+                        block_path)
         self.cfg = c
         self.n, self.S, self.d = c.n_vertices, c.n_sources, c.rank_d
         self.n_parts, self.h, self.directed = c.n_parts, c.hierarchy_n, bool(directed)
         self._h = _vp()
         _check(lib().tsvd_session_create(ctypes.byref(c), ctypes.byref(self._h)))
 
+    @classmethod
+    def _view(cls, handle, cfg, sources):
+        """A non-owning Session around a handle (a server tenant's session)."""
+        self = cls.__new__(cls)
+        self.sources = sources
+        self.cfg = cfg
+        self.n, self.S, self.d = cfg.n_vertices, cfg.n_sources, cfg.rank_d
+        self.n_parts, self.h, self.directed = cfg.n_parts, cfg.hierarchy_n, bool(cfg.directed)
+        self._h = handle
+        self._owned = False
+        return self
+
+
+    _owned = True
+
     def close(self):
-        if getattr(self, "_h", None):
+        if getattr(self, "_h", None) and self._owned:
             lib().tsvd_session_destroy(self._h)
-            self._h = None
+        self._h = None
 
     def __del__(self):
         try:
@@ -405,6 +469,14 @@ class Session:
         _check(lib().tsvd_ppr_state(self._h, int(transpose), int(which), _p(out, _f32p)))
         return out
 
+    def ppr_state_rows(self, rows, transpose=False, which=1):
+        """State of the listed source rows only (len(rows) x N float32)."""
+        rows = np.ascontiguousarray(rows, dtype=np.int32)
+        out = np.zeros((len(rows), self.n), np.float32)
+        _check(lib().tsvd_ppr_state_rows(self._h, int(transpose), int(which), _p(rows, _i32p),
+                                         len(rows), _p(out, _f32p)))
+        return out
+
     def block_info(self):
         P = self.n_parts
         a, dd, r = (np.zeros(P) for _ in range(3))
@@ -452,3 +524,91 @@ class Session:
             tot += pw
             pw *= self.h
         return tot - self.n_parts
+
+
+# ----------------------------------------------------------------- serving
+class ServerStats(ctypes.Structure):
+    _fields_ = [("updates", ctypes.c_int64), ("edges", ctypes.c_int64),
+                ("p50_ms", ctypes.c_double), ("p99_ms", ctypes.c_double),
+                ("edges_per_s", ctypes.c_double), ("hbm_budget", ctypes.c_int64),
+                ("hbm_charged", ctypes.c_int64), ("tenants", ctypes.c_int32)]
+
+
+class Server:
+    """tsvd_server: tenants resident on one GPU, requests taken as they arrive."""
+
+    def __init__(self, device=0, hbm_budget_bytes=0, slots=4):
+        self._h = _vp()
+        _check(lib().tsvd_server_create(int(device), int(hbm_budget_bytes), int(slots),
+                                        ctypes.byref(self._h)))
+        self._tenants = {}
+        self._pending = {}  # request id -> (kind, buffer kept alive)
+
+    def add_tenant(self, n_vertices, sources, expected_edges, **kw):
+        src = np.ascontiguousarray(sources, dtype=np.int32)
+        c = make_config(n_vertices, src, **kw)
+        t = ctypes.c_int32()
+        _check(lib().tsvd_server_add_tenant(self._h, ctypes.byref(c), int(expected_edges),
+                                            ctypes.byref(t)))
+        self._tenants[t.value] = (c, src)
+        return t.value
+
+    def remove_tenant(self, tenant):
+        _check(lib().tsvd_server_remove_tenant(self._h, int(tenant)))
+        self._tenants.pop(tenant, None)
+
+    def submit_update(self, tenant, edges):
+        e = np.ascontiguousarray(edges, dtype=np.int32).reshape(-1, 2)
+        r = ctypes.c_int64()
+        _check(lib().tsvd_server_submit_update(self._h, int(tenant), _p(e, _i32p), e.shape[0],
+                                               ctypes.byref(r)))
+        self._pending[r.value] = ("update", None)
+        return r.value
+
+    def submit_query(self, tenant):
+        c, src = self._tenants[tenant]
+        out = np.zeros((c.n_sources, c.rank_d), np.float64)
+        r = ctypes.c_int64()
+        _check(lib().tsvd_server_submit_query(self._h, int(tenant), _p(out, _f64p),
+                                              ctypes.byref(r)))
+        self._pending[r.value] = ("query", out)
+        return r.value
+
+    def wait(self, request):
+        """(latency ms, service ms, embedding for queries or None)."""
+        lat, svc = ctypes.c_double(), ctypes.c_double()
+        kind, buf = self._pending.pop(request, (None, None))
+        _check(lib().tsvd_server_wait(self._h, int(request), ctypes.byref(lat), ctypes.byref(svc)))
+        return lat.value, svc.value, buf
+
+    def drain(self):
+        _check(lib().tsvd_server_drain(self._h))
+
+    def stats(self):
+        st = ServerStats()
+        _check(lib().tsvd_server_stats(self._h, ctypes.byref(st)))
+        return {k: getattr(st, k) for k, _ in st._fields_}
+
+    def session(self, tenant):
+        """A non-owning Session view of the tenant (inspection between requests)."""
+        h = _vp()
+        _check(lib().tsvd_server_session(self._h, int(tenant), ctypes.byref(h)))
+        c, src = self._tenants[tenant]
+        return Session._view(h, c, src)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().tsvd_server_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -16,6 +16,7 @@ import numpy as np
 # values of the TSVD_TRANSFORM_* and TSVD_DIRTY_* constants of include/tsvd.h
 TRANSFORM_LOG10_NC, TRANSFORM_LOG10_LP, TRANSFORM_LN_N = 0, 1, 2
 DIRTY_REFERENCE, DIRTY_FROBENIUS, DIRTY_ALL = 0, 1, 2
+BLOCKS_DENSE, BLOCKS_SPARSE, BLOCKS_AUTO = 0, 1, 2
 
 CONFIGS = {
     # Plain method, CPU-runnable (undirected, N=1e5, M=1e6, 10 snapshots).
@@ -43,7 +44,32 @@ CONFIGS = {
                              transform=TRANSFORM_LOG10_NC, n_parts=128, hierarchy_n=2,
                              rank_d=128, passes_q=6, dirty_rule=DIRTY_FROBENIUS,
                              dirty_frac=0.01, delta=0.3, host_reserve=True),
+    # Batched form: two undirected graphs (YouTube- and Flickr-sized), monthly
+    # splits (24 snapshots, the first with 40 % of the edges), 256 column
+    # blocks made deliberately uneven by numbering the vertices in descending
+    # order of their final degree (block 0 holds the hubs); the block-path
+    # autotuner picks tensor-core or SpMM products per block.
+    "rmat-u-3.2m-deg": dict(n=3_223_589, m=9_375_374, directed=False, snapshots=24, first=0.4,
+                            sources=3000, alpha=0.2, rmax=1e-7, transform=TRANSFORM_LOG10_NC,
+                            n_parts=256, hierarchy_n=2, rank_d=128, passes_q=6,
+                            dirty_rule=DIRTY_FROBENIUS, dirty_frac=0.01, delta=0.3,
+                            degree_sort=True, block_path=BLOCKS_AUTO),
+    "rmat-u-2.3m-deg": dict(n=2_302_925, m=33_140_017, directed=False, snapshots=24, first=0.4,
+                            sources=3000, alpha=0.2, rmax=1e-7, transform=TRANSFORM_LOG10_NC,
+                            n_parts=256, hierarchy_n=2, rank_d=128, passes_q=6,
+                            dirty_rule=DIRTY_FROBENIUS, dirty_frac=0.01, delta=0.3,
+                            degree_sort=True, block_path=BLOCKS_AUTO),
 }
+
+
+def degree_order(edges, n):
+    """Vertex ids renumbered in descending order of final degree (both
+    endpoints counted; ties keep the lower id first)."""
+    deg = np.bincount(edges.ravel(), minlength=n)
+    order = np.argsort(-deg, kind="stable")
+    new_id = np.empty(n, np.int32)
+    new_id[order] = np.arange(n, dtype=np.int32)
+    return new_id[edges].astype(np.int32)
 
 
 def scaled(name, n=None, m=None, sources=None, n_parts=None, rank_d=None, snapshots=None):
@@ -63,6 +89,8 @@ def build(cfg, seed=20231, generator=None):
     if generator is None:
         import tsvd_gb300 as generator
     edges = generator.rmat_edges(cfg["n"], cfg["m"], directed=cfg["directed"], seed=seed)
+    if cfg.get("degree_sort"):
+        edges = degree_order(edges, cfg["n"])
     sizes = generator.snapshot_sizes(len(edges), cfg["snapshots"], cfg["first"])
     bounds = np.concatenate([[0], np.cumsum(sizes)])
     snaps = [edges[bounds[i]:bounds[i + 1]] for i in range(len(sizes))]
@@ -76,4 +104,5 @@ def session_kwargs(cfg, dynamic_start=2, lazy_start=2, seed=20231):
                 passes_q=cfg["passes_q"], dynamic_ppr_start_iter=dynamic_start,
                 lazy_update_start_iter=lazy_start, delta=cfg.get("delta", 0.3),
                 transform=cfg["transform"], dirty_rule=cfg["dirty_rule"],
-                dirty_frac=cfg.get("dirty_frac", 0.01), seed=seed)
+                dirty_frac=cfg.get("dirty_frac", 0.01), block_path=cfg.get("block_path", 0),
+                seed=seed)
