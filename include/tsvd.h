@@ -240,6 +240,9 @@ typedef struct tsvd_config {
                             /* |S| 3000: 305 GB)                                      */
   int32_t form;             /* TSVD_FORM_*: how a snapshot is computed (see below)   */
   int32_t block_path;       /* TSVD_BLOCKS_*: product path of the mixed form's frPCA */
+  int32_t plain_frontier_cap; /* plain form: entries of its frontier list (0: 2^26);  */
+                            /* cells beyond it wait in the touched bitset for the    */
+                            /* next round                                            */
 } tsvd_config;
 
 /* Fills the reference's defaults (Tree_u_NC, run.sh: alpha .5, q 12, ...). */

@@ -21,9 +21,13 @@ the push-order difference. Checked on every snapshot:
 * dirty blocks: identical to the oracle run on the GPU's reserve; identical to
   the independent oracle outside near-ties (decision margin below 2 %, where
   the two pushes' matrices may legitimately fall on either side).
-* root singular values within 1e-3 relative and the largest principal-angle
-  sine of the gap-separated leading subspace within 1e-2, against both
-  oracles (against the independent one while its dirty decisions have agreed).
+* root singular values within 1e-3 relative against the oracle run on the
+  GPU's reserve (the factorization arithmetic alone), within 1e-2 against the
+  independent oracle (the two pushes stop at different valid states; with
+  the ln(x N) transform at rmax = 1e-6 that moves the root singular values
+  by up to 5.3e-3, measured on a GB300); the largest principal-angle sine of
+  the gap-separated leading subspace within 1e-2 against both (against the
+  independent one while its dirty decisions have agreed).
 
 The tree's embedding is not the exact SVD of the current matrix: blocks the
 lazy rule keeps are a snapshot old, and every block is truncated to rank d
@@ -168,12 +172,12 @@ def test_c1_end_to_end_against_the_fp64_oracle():
             emb = s.embedding()
             _, sig = s.tree_factor(0)
             assert np.isfinite(emb).all()
-            for name, ref_emb, ref_sig in (("iso", emb_i, iso.sigma[0]),
-                                           ("indep", emb_o, indep.sigma[0])):
+            for name, ref_emb, ref_sig, tol in (("iso", emb_i, iso.sigma[0], 1e-3),
+                                                ("indep", emb_o, indep.sigma[0], 1e-2)):
                 if not agreed[name]:
                     continue
                 rel = np.abs(sig - ref_sig) / ref_sig
-                assert rel.max() <= 1e-3, (it, name, rel.max(), int(rel.argmax()))
+                assert rel.max() <= tol, (it, name, rel.max(), int(rel.argmax()))
                 j = gap_index(ref_sig, d)
                 assert j > 0
                 sine = max_principal_sine(emb[:, :j], ref_emb[:, :j])

@@ -47,8 +47,11 @@ def _ppr_against_oracle(s, g, src, cfg, oracle_states):
         assert (np.abs(p.astype(np.float64) - po) <= bound * (1 + 1e-3) + 1e-6).all()
 
 
-@pytest.mark.parametrize("directed", [False, True])
-def test_plain_form_snapshots_match_the_oracle(directed):
+@pytest.mark.parametrize("directed,cap", [(False, 0), (True, 0), (True, 700)])
+def test_plain_form_snapshots_match_the_oracle(directed, cap):
+    """cap = 700: the frontier list holds far fewer cells than a round
+    touches, so most cells wait in the bitset for later rounds (the path a
+    large graph takes with the default 2^26 entries)."""
     cfg = small_cfg(directed, n=7003, m=50000, sources=96)
     _, snaps, src = W.build(cfg, seed=41)
     kw = W.session_kwargs(cfg, dynamic_start=2, lazy_start=2)
@@ -57,7 +60,7 @@ def test_plain_form_snapshots_match_the_oracle(directed):
     iso = OracleTreeSVD(cfg["n"], src, seed=kw["seed"], **okw)
     g = native.OracleGraph(cfg["n"], directed)
     ors = [native.OraclePPR(cfg["n"], src) for _ in range(2 if directed else 1)]
-    with T.Session(cfg["n"], src, form=T.FORM_PLAIN, **kw) as s:
+    with T.Session(cfg["n"], src, form=T.FORM_PLAIN, plain_frontier_cap=cap, **kw) as s:
         for it, e in enumerate(snaps, start=1):
             st = s.step(e)
             g.insert(e)

@@ -25,7 +25,7 @@ __device__ __forceinline__ void mark_cell(uint32_t *bits, int64_t cell) {
 
 struct PlainArgs {
   const int2 *front;
-  const int32_t *front_count;
+  const unsigned long long *front_count;  // may exceed cap: entries beyond it were not stored
   float *r, *p;
   const int64_t *off;
   const int32_t *deg, *nbr, *former;
@@ -37,7 +37,7 @@ struct PlainArgs {
   uint8_t *vmark;
   unsigned long long *stats;
   int2 *next;
-  int32_t *next_count;
+  unsigned long long *next_count;
   int64_t cap;
   int64_t nwords;
   const int32_t *upd;
@@ -52,7 +52,7 @@ __global__ void __launch_bounds__(256) plain_push_kernel(PlainArgs a) {
   const int lane = threadIdx.x & 31;
   const int64_t gw = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  const int32_t nitems = *a.front_count;
+  const int64_t nitems = (int64_t)min(*a.front_count, (unsigned long long)a.cap);
   unsigned long long pushes = 0, upd = 0;
   for (int64_t i = gw; i < nitems; i += nw) {
     const int2 it = a.front[i];
@@ -116,8 +116,8 @@ __global__ void __launch_bounds__(256) plain_collect_kernel(PlainArgs a) {
       const int32_t v = (int32_t)(run - (int64_t)c * a.n);
       const int32_t s = c * 64 + (int32_t)(cell & 63);
       if (s >= a.nsrc || a.deg[v] == 0 || !(a.r[cell] > a.rmax_f)) continue;
-      const int32_t slot = atomicAdd(a.next_count, 1);
-      if (slot < a.cap)
+      const unsigned long long slot = atomicAdd(a.next_count, 1ull);
+      if (slot < (unsigned long long)a.cap)
         a.next[slot] = make_int2(v, s);
       else
         keep |= 1u << b;
@@ -163,12 +163,12 @@ __global__ void __launch_bounds__(256) plain_refresh_kernel(PlainArgs a) {
 // reserve becomes alpha, as in the reference).
 __global__ void plain_seed_kernel(const int32_t *__restrict__ sources, int32_t nsrc,
                                   float *__restrict__ r, int32_t n, int2 *__restrict__ front,
-                                  int32_t *__restrict__ count) {
+                                  unsigned long long *__restrict__ count) {
   for (int32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < nsrc; k += gridDim.x * blockDim.x) {
     r[ppr_cell(sources[k], k, n)] = 1.0f;
     front[k] = make_int2(sources[k], k);
   }
-  if (blockIdx.x == 0 && threadIdx.x == 0) *count = nsrc;
+  if (blockIdx.x == 0 && threadIdx.x == 0) *count = (unsigned long long)nsrc;
 }
 
 __global__ void plain_zero_kernel(float4 *__restrict__ x, int64_t n4) {
@@ -356,16 +356,16 @@ __global__ void __launch_bounds__(256) spmm_kernel(SpmmArgs a) {
 }  // namespace
 
 // ------------------------------------------------------------------ push
-tsvd_status plain_alloc(PlainPpr &Q, int32_t n, int32_t sp) {
+tsvd_status plain_alloc(PlainPpr &Q, int32_t n, int32_t sp, int64_t cap) {
   Q.nwords = ceil_div((int64_t)n * sp, 32);
   TSVD_CUDA(cudaMalloc(&Q.cbits, Q.nwords * sizeof(uint32_t)));
   TSVD_CUDA(cudaMemset(Q.cbits, 0, Q.nwords * sizeof(uint32_t)));
   // bounded frontier: cells that do not fit wait in the bitset for a later round
-  Q.cap = std::min<int64_t>((int64_t)n * sp, (int64_t)1 << 26);
+  Q.cap = std::min<int64_t>((int64_t)n * sp, cap > 0 ? cap : (int64_t)1 << 26);
   for (int i = 0; i < 2; ++i) TSVD_CUDA(cudaMalloc(&Q.front[i], Q.cap * sizeof(int2)));
-  TSVD_CUDA(cudaMalloc(&Q.counters, 8 * sizeof(int32_t)));
-  TSVD_CUDA(cudaMemset(Q.counters, 0, 8 * sizeof(int32_t)));
-  TSVD_CUDA(cudaMallocHost(&Q.host_counters, 8 * sizeof(int32_t)));
+  TSVD_CUDA(cudaMalloc(&Q.counters, 8 * sizeof(unsigned long long)));
+  TSVD_CUDA(cudaMemset(Q.counters, 0, 8 * sizeof(unsigned long long)));
+  TSVD_CUDA(cudaMallocHost(&Q.host_counters, 8 * sizeof(unsigned long long)));
   TSVD_CUDA(cudaMalloc(&Q.stats, 2 * sizeof(unsigned long long)));
   for (auto &e : Q.kev) TSVD_CUDA(cudaEventCreate(&e));
   return TSVD_OK;
@@ -416,7 +416,9 @@ tsvd_status plain_refresh(PlainPpr &Q, PprState &P, const Adjacency &A,
                                                                    cells / 4);
     TSVD_LAUNCH_CHECK();
     TSVD_CUDA(cudaMemsetAsync(Q.cbits, 0, Q.nwords * sizeof(uint32_t), st));
-    if ((int64_t)P.nsrc > Q.cap) return fail(TSVD_ERR_INVALID, "plain push: frontier too small");
+    if ((int64_t)P.nsrc > Q.cap)
+      return fail(TSVD_ERR_INVALID, "plain push: a frontier of %lld entries holds fewer than the "
+                  "%d sources", (long long)Q.cap, P.nsrc);
     plain_seed_kernel<<<grid_for(P.nsrc, 256), 256, 0, st>>>(sources_dev, P.nsrc, P.r, P.n,
                                                              Q.front[0], Q.counters + 0);
     TSVD_LAUNCH_CHECK();
@@ -448,7 +450,7 @@ tsvd_status plain_push(PlainPpr &Q, PprState &P, const Adjacency &A, const PprPa
   Q.cur = 0;
   if (!Q.primed) {
     // first frontier: every cell the refresh marked
-    TSVD_CUDA(cudaMemsetAsync(Q.counters, 0, 8 * sizeof(int32_t), st));
+    TSVD_CUDA(cudaMemsetAsync(Q.counters, 0, 8 * sizeof(unsigned long long), st));
     a.next = Q.front[0];
     a.next_count = Q.counters + 0;
     plain_collect_kernel<<<gcol, 256, 0, st>>>(a);
@@ -465,7 +467,7 @@ tsvd_status plain_push(PlainPpr &Q, PprState &P, const Adjacency &A, const PprPa
       a.front_count = Q.counters + cur;
       a.next = Q.front[nxt];
       a.next_count = Q.counters + nxt;
-      TSVD_CUDA(cudaMemsetAsync(Q.counters + nxt, 0, sizeof(int32_t), st));
+      TSVD_CUDA(cudaMemsetAsync(Q.counters + nxt, 0, sizeof(unsigned long long), st));
       TSVD_CUDA(cudaEventRecord(Q.kev[2 * k], st));
       plain_push_kernel<<<gpush, 256, 0, st>>>(a);
       TSVD_LAUNCH_CHECK();
@@ -475,7 +477,7 @@ tsvd_status plain_push(PlainPpr &Q, PprState &P, const Adjacency &A, const PprPa
       Q.cur = nxt;
       ++rounds;
     }
-    TSVD_CUDA(cudaMemcpyAsync(Q.host_counters, Q.counters, 8 * sizeof(int32_t),
+    TSVD_CUDA(cudaMemcpyAsync(Q.host_counters, Q.counters, 8 * sizeof(unsigned long long),
                               cudaMemcpyDeviceToHost, st));
     TSVD_CUDA(cudaStreamSynchronize(st));
     for (int k = 0; k < per_check; ++k) {

@@ -28,13 +28,14 @@ struct PlainPpr {
   int cur = 0;
   bool seeded = false;
   bool primed = false;                // frontier 0 written by the from-scratch refresh
-  int32_t *counters = nullptr;       // [0],[1] frontier counts, [2] overflow
-  int32_t *host_counters = nullptr;  // pinned
+  unsigned long long *counters = nullptr;  // [0],[1] frontier counts (attempted entries:
+                                           // above cap, the rest waits in the bitset)
+  unsigned long long *host_counters = nullptr;  // pinned
   unsigned long long *stats = nullptr;  // [2]: pushes, edge updates
   cudaEvent_t kev[16] = {};
 };
 
-tsvd_status plain_alloc(PlainPpr &Q, int32_t n, int32_t sp);
+tsvd_status plain_alloc(PlainPpr &Q, int32_t n, int32_t sp, int64_t cap);
 void plain_free(PlainPpr &Q);
 // Refresh of every source (from scratch: r = e_s) on the cell frontier.
 tsvd_status plain_refresh(PlainPpr &Q, PprState &P, const Adjacency &A,

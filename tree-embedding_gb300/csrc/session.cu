@@ -889,7 +889,8 @@ static tsvd_status stage_ppr(tsvd_session *s, int iter, int dir) {
   PprParams prm = ppr_params(s);
   PushStats ps;
   if (s->form == TSVD_FORM_PLAIN) {
-    if (!s->plain[dir].cbits) TSVD_TRY(plain_alloc(s->plain[dir], s->n, s->sp));
+    if (!s->plain[dir].cbits)
+      TSVD_TRY(plain_alloc(s->plain[dir], s->n, s->sp, s->cfg.plain_frontier_cap));
     TSVD_TRY(plain_refresh(s->plain[dir], s->ppr[dir], s->adj[dir], s->sources_dev, scratch, prm,
                            s->st));
     TSVD_TRY(plain_push(s->plain[dir], s->ppr[dir], s->adj[dir], prm, s->vmark, s->st, &ps));
@@ -1208,7 +1209,8 @@ extern "C" tsvd_status tsvd_ppr_refresh(tsvd_session *s, int32_t iter, int32_t t
   const int dir = transpose ? 1 : 0;
   const bool scratch = iter < s->cfg.dynamic_ppr_start_iter;
   if (s->form == TSVD_FORM_PLAIN) {
-    if (!s->plain[dir].cbits) TSVD_TRY(plain_alloc(s->plain[dir], s->n, s->sp));
+    if (!s->plain[dir].cbits)
+      TSVD_TRY(plain_alloc(s->plain[dir], s->n, s->sp, s->cfg.plain_frontier_cap));
     return plain_refresh(s->plain[dir], s->ppr[dir], s->adj[dir], s->sources_dev, scratch, prm,
                          s->st);
   }

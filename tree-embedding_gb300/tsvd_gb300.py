@@ -45,7 +45,7 @@ class Config(ctypes.Structure):
         ("push_levels", ctypes.c_int32), ("push_ratio", ctypes.c_double),
         ("push_cofrac", ctypes.c_double), ("lp_right_factor", ctypes.c_int32),
         ("ppr_host_reserve", ctypes.c_int32), ("form", ctypes.c_int32),
-        ("block_path", ctypes.c_int32),
+        ("block_path", ctypes.c_int32), ("plain_frontier_cap", ctypes.c_int32),
     ]
 
 
@@ -278,7 +278,8 @@ def make_config(n_vertices, sources, directed=False, alpha=0.5, rmax=1e-7, n_par
                 dirty_rule=DIRTY_REFERENCE, dirty_frac=0.01, root_scaling=ROOT_SQRT_SIGMA,
                 refresh_mode=REFRESH_EXACT, seed=20231, device=0, max_push_rounds=0,
                 push_levels=1, push_ratio=8.0, push_cofrac=0.85, lp_right_factor=False,
-                ppr_host_reserve=False, form=FORM_MIXED, block_path=BLOCKS_DENSE):
+                ppr_host_reserve=False, form=FORM_MIXED, block_path=BLOCKS_DENSE,
+                plain_frontier_cap=0):
     """A tsvd_config; `sources` (int32, contiguous) must outlive it."""
     c = Config()
     lib().tsvd_config_default(ctypes.byref(c))
@@ -300,6 +301,7 @@ def make_config(n_vertices, sources, directed=False, alpha=0.5, rmax=1e-7, n_par
     c.ppr_host_reserve = int(bool(ppr_host_reserve))
     c.form = int(form)
     c.block_path = int(block_path)
+    c.plain_frontier_cap = int(plain_frontier_cap)
     return c
 
 
@@ -322,14 +324,14 @@ class Session:
                  root_scaling=ROOT_SQRT_SIGMA, refresh_mode=REFRESH_EXACT, seed=20231, device=0,
                  max_push_rounds=0, push_levels=1, push_ratio=8.0, push_cofrac=0.85,
                  lp_right_factor=False, ppr_host_reserve=False, form=FORM_MIXED,
-                 block_path=BLOCKS_DENSE):
+                 block_path=BLOCKS_DENSE, plain_frontier_cap=0):
         self.sources = np.ascontiguousarray(sources, dtype=np.int32)
         c = make_config(n_vertices, self.sources, directed, alpha, rmax, n_parts, hierarchy_n,
                         rank_d, oversample, passes_q, dynamic_ppr_start_iter,
                         lazy_update_start_iter, delta, transform, dirty_rule, dirty_frac,
                         root_scaling, refresh_mode, seed, device, max_push_rounds, push_levels,
                         push_ratio, push_cofrac, lp_right_factor, ppr_host_reserve, form,
-                        block_path)
+                        block_path, plain_frontier_cap)
         self.cfg = c
         self.n, self.S, self.d = c.n_vertices, c.n_sources, c.rank_d
         self.n_parts, self.h, self.directed = c.n_parts, c.hierarchy_n, bool(directed)
