@@ -527,6 +527,24 @@ def push_roofline(stages):
 PUSH_TRAFFIC_BYTES_PER_ITEM_EDGE = 320.9
 
 
+def tail_attribution(stages):
+    """Where the slowest snapshots spend their extra time: per stage, the mean
+    over the steps at or above the 90th latency percentile minus the median
+    over all steps, with the push work counters that explain the push part."""
+    lat = np.array([s["ms_total"] for s in stages])
+    if len(lat) < 2:
+        return None
+    slow = lat >= np.percentile(lat, 90)
+    keys = ("ms_insert", "ms_push", "ms_log", "ms_frpca", "ms_merge")
+    out = {"slow_steps": int(slow.sum()),
+           "extra_ms": {k: float(np.mean([s[k] for s, f in zip(stages, slow) if f]) -
+                                 np.median([s[k] for s in stages])) for k in keys}}
+    for k in ("push_rounds", "push_item_edges", "dirty_blocks"):
+        med = float(np.median([s[k] for s in stages]))
+        out[k + "_ratio"] = float(np.mean([s[k] for s, f in zip(stages, slow) if f])) / max(med, 1)
+    return out
+
+
 def aggregate(ms, edges, device=None):
     """Whole-job throughput of independent replicas: every rank's edges over
     the slowest rank's time (max over ranks; identity without a process group)."""
@@ -678,6 +696,7 @@ def main():
             "merge_subspace_iters_max": int(max(s["merge_subspace_iters"] for s in res["stages"])),
             "eig_refine_sweeps_max": int(max(s["eig_refine_sweeps"] for s in res["stages"]))}
     line["roofline"] = push_roofline(res["stages"])
+    line["tail"] = tail_attribution(res["stages"])
     if "e2e_ms" in res:
         line["e2e"] = {"value": res["e2e_edges"] * world / (res["e2e_ms"] / 1e3),
                        "unit": "edge updates/s", "steps": res["e2e_steps"],
@@ -702,7 +721,8 @@ def main():
             "deltas": "the %d deltas after the e2e leg, same session" % pl["steps"]}
         line["p50_plain_over_mixed"] = line["plain_form"]["p50_ms"] / line["p50_ms"]
     if rank == 0 and not args.no_cpu:
-        info = cpu_sample(cfg, snaps, sources, steps=1, k=args.cpu_sources)
+        info = cpu_sample(cfg, snaps, sources, steps=1,
+                          k=args.cpu_sources or (os.cpu_count() or 1))
         s0 = info["steps"][0]
         line["cpu_baseline"] = {"value": s0["edges"] / s0["scaled_s"], "unit": "edge updates/s",
                                 "cores": info["threads"], "kind": info["kind"],

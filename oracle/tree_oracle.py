@@ -114,7 +114,10 @@ class OracleTreeSVD:
                  hierarchy_n=2, rank_d=128, oversample=5, passes_q=12,
                  dynamic_ppr_start_iter=100, lazy_update_start_iter=100, delta=0.3,
                  transform=TRANSFORM_LOG10_NC, dirty_rule=DIRTY_REFERENCE, dirty_frac=0.01,
-                 root_scaling=0, refresh_mode=0, seed=20231, threads=1, lp_right_factor=False):
+                 root_scaling=0, refresh_mode=0, seed=20231, threads=1, lp_right_factor=False,
+                 block_path=0):
+        # block_path: the GPU's choice of product path for a block's frPCA; the
+        # oracle's arithmetic is the same either way, so it is accepted and unused
         self.n, self.directed = int(n), bool(directed)
         self.sources = np.ascontiguousarray(sources, dtype=np.int32)
         self.S = len(self.sources)

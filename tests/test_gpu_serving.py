@@ -8,16 +8,21 @@ tenant ran alone or in the mix. Four tenants of different sizes and shapes
 one tenant at a time) and once together (four slots, all requests submitted
 up front, interleaved); after every update a query returns the embedding.
 The two runs execute the same arithmetic except for the order of the push's
-floating-point atomics, so the embeddings agree within rounding: Gram matrices
-within 1e-3 and root singular values within 1e-4 (every block is refreshed
-every snapshot, so no lazy decision can part the two runs).
+floating-point atomics: residues that land within rounding of rmax can be
+pushed in one run and not in the other, so the two runs stop at two valid
+push states, like any two runs of the same session. The results must then
+agree within the tolerance every parity test states: root singular values
+(the squared column norms of the U sqrt(S) embedding) within 1e-3 relative
+and the largest principal-angle sine of the gap-separated leading subspace
+within 1e-2. Every block is refreshed every snapshot, so no lazy decision can
+part the two runs.
 """
 import numpy as np
 import pytest
 
 import tsvd_gb300 as T
 import workloads as W
-from helpers import gram_rel_err
+from helpers import gap_index, max_principal_sine
 
 pytestmark = pytest.mark.gpu
 
@@ -73,10 +78,21 @@ def test_each_result_is_the_same_alone_and_in_the_mix():
     assert st["updates"] == len(tenants) * 4 and st["tenants"] == len(tenants)
     assert st["p99_ms"] >= st["p50_ms"] > 0 and st["edges_per_s"] > 0
     for key, emb in alone.items():
-        assert np.isfinite(emb).all() and np.isfinite(mixed[key]).all()
-        assert gram_rel_err(mixed[key], emb) < 1e-3, key
+        mix = mixed[key]
+        assert np.isfinite(emb).all() and np.isfinite(mix).all()
+        sa = (emb ** 2).sum(axis=0)  # U sqrt(S): column norms squared are S
+        sm = (mix ** 2).sum(axis=0)
+        order = np.argsort(-sa)
+        sa, sm = sa[order], sm[np.argsort(-sm)]
+        j = gap_index(sa, len(sa))
+        assert j > 0, key
+        assert np.allclose(sm[:j], sa[:j], rtol=1e-3), (key, np.abs(sm[:j] / sa[:j] - 1).max())
+        ua = emb[:, order[:j]]
+        um = mix[:, np.argsort(-(mix ** 2).sum(axis=0))[:j]]
+        assert max_principal_sine(um, ua) <= 1e-2, key
     for t in sig_alone:
-        assert np.allclose(sig_mix[t], sig_alone[t], rtol=1e-4), t
+        j = gap_index(sig_alone[t], len(sig_alone[t]))
+        assert np.allclose(sig_mix[t][:j], sig_alone[t][:j], rtol=1e-3), t
 
 
 def test_admission_by_hbm_footprint():

@@ -19,6 +19,8 @@
 //    LAPACKE_dsyevd (frpca.c:102) and the Gram route to LAPACKE_dgesvd
 //    (..._mkl.c:1278) for the merge.
 #include <algorithm>
+#include <map>
+#include <mutex>
 #include <cfloat>
 
 #include <cooperative_groups.h>
@@ -983,8 +985,20 @@ int grid_for(int64_t work_items, int threads_per_block, int blocks_per_sm) {
   return (int)std::max<int64_t>(1, std::min(need, cap));
 }
 
+// A kernel's dynamic shared-memory ceiling is a process-wide attribute, and
+// sessions on other threads launch the same kernels with other sizes: it is
+// only ever raised (under a lock), so no thread's launch can find it lowered
+// below what that launch asks for.
 static tsvd_status set_smem(const void *fn, size_t bytes) {
+  static std::mutex mu;
+  static std::map<std::pair<const void *, int>, size_t> ceiling;
+  int dev = 0;
+  TSVD_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> g(mu);
+  size_t &cur = ceiling[std::make_pair(fn, dev)];
+  if (bytes <= cur) return TSVD_OK;
   TSVD_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+  cur = bytes;
   return TSVD_OK;
 }
 
@@ -1061,12 +1075,8 @@ tsvd_status gram_batched(const float *const *x, const int32_t *rows, int max_row
     return fail(TSVD_ERR_INVALID, "gram: work buffer too small");
   int tiles = (l + 3) / 4;
   int groups = (int)ceil_div(tiles * (tiles + 1) / 2, GRAM_TILES_PER_CTA);
-  static size_t cur_smem = 0;
   size_t smem = (size_t)GRAM_SUB * (4 * tiles) * sizeof(float);
-  if (smem > cur_smem) {
-    TSVD_TRY(set_smem((const void *)gram_partial_kernel, smem));
-    cur_smem = smem;
-  }
+  TSVD_TRY(set_smem((const void *)gram_partial_kernel, smem));
   // chunks past a problem's row count must contribute zeros
   TSVD_CUDA(cudaMemsetAsync(work, 0, gram_work_bytes(max_rows, l, nprob), st));
   GramArgs a{x, rows, ld, l, tiles, nchunks, chunk_rows, work};
@@ -1083,11 +1093,7 @@ tsvd_status chol_inverse_batched(double *const *g, float *const *t, int l, int n
   if (nprob == 0) return TSVD_OK;
   if (l > kLp) return fail(TSVD_ERR_INVALID, "chol: l=%d > %d", l, kLp);
   size_t smem = (size_t)2 * l * (l + 1) * sizeof(float);
-  static size_t cur = 0;
-  if (smem > cur) {
-    TSVD_TRY(set_smem((const void *)chol_inverse_kernel, smem));
-    cur = smem;
-  }
+  TSVD_TRY(set_smem((const void *)chol_inverse_kernel, smem));
   chol_inverse_kernel<<<nprob, CHOL_THREADS, smem, st>>>(g, t, l);
   TSVD_LAUNCH_CHECK();
   return TSVD_OK;
@@ -1240,15 +1246,8 @@ tsvd_status chol_shift_solve_batched(const float *K, float *Lpk, const float *x,
   const size_t csm = (size_t)l * (l + 1) / 2 * sizeof(float);
   const size_t tsm = (((size_t)l * (l + 1) / 2 + 3) & ~(size_t)3) * sizeof(float) +
                      (size_t)32 * l * sizeof(float);
-  static size_t ccur = 0, tcur = 0;
-  if (csm > 48 * 1024 && csm > ccur) {
-    TSVD_TRY(set_smem((const void *)chol_shift_kernel, csm));
-    ccur = csm;
-  }
-  if (tsm > 48 * 1024 && tsm > tcur) {
-    TSVD_TRY(set_smem((const void *)trsm_warp_kernel, tsm));
-    tcur = tsm;
-  }
+  if (csm > 48 * 1024) TSVD_TRY(set_smem((const void *)chol_shift_kernel, csm));
+  if (tsm > 48 * 1024) TSVD_TRY(set_smem((const void *)trsm_warp_kernel, tsm));
   chol_shift_kernel<<<nprob, 1024, csm, st>>>(K, Lpk, l, shift);
   TSVD_LAUNCH_CHECK();
   const int blocks = (int)std::min<int64_t>(ceil_div(rows, 32), 2 * sm_count() / std::max(nprob, 1) + 1);
@@ -1360,11 +1359,7 @@ tsvd_status jacobi_eig_batched(double *const *g, int n, float *const *lambda, fl
   TSVD_CUDA(cudaLaunchKernelEx(&cfg, jacobi_kernel, a));
   const size_t rsmem = (size_t)((REPLAY_ROWS * n + 1) & ~1) * sizeof(float) +
                        (size_t)2 * REPLAY_CHUNK * P * sizeof(float2);
-  static size_t rcur = 0;
-  if (rsmem > 48 * 1024 && rsmem > rcur) {
-    TSVD_TRY(set_smem((const void *)jacobi_replay_kernel, rsmem));
-    rcur = rsmem;
-  }
+  if (rsmem > 48 * 1024) TSVD_TRY(set_smem((const void *)jacobi_replay_kernel, rsmem));
   jacobi_replay_kernel<<<dim3((unsigned)ceil_div(n, REPLAY_ROWS), nprob), 256, rsmem, st>>>(a, v);
   TSVD_LAUNCH_CHECK();
   if (sweeps_out) {
