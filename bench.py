@@ -692,6 +692,8 @@ def main():
             "push_item_edges_mean": float(np.mean([s["push_item_edges"] for s in res["stages"]])),
             "ms_materialize_kernel_mean": float(np.mean([s["ms_materialize_kernel"] for s in res["stages"]])),
             "dirty_blocks_mean": float(np.mean([s["dirty_blocks"] for s in res["stages"]])),
+            "sparse_blocks_mean": float(np.mean([s["sparse_blocks"] for s in res["stages"]])),
+            "autotuner_density": float(res["stages"][-1]["tune_density"]),
             "eig_sweeps_merge_max": int(max(s["eig_sweeps_merge"] for s in res["stages"])),
             "merge_subspace_iters_max": int(max(s["merge_subspace_iters"] for s in res["stages"])),
             "eig_refine_sweeps_max": int(max(s["eig_refine_sweeps"] for s in res["stages"]))}

@@ -5,7 +5,7 @@ autotuner measured (TSVD_BLOCKS_AUTO), on a degree-sorted graph whose
 blocks range from dense (the hubs) to nearly empty. Each session agrees with
 the oracle run on its own reserve (the two paths multiply the same half-
 precision values), every dirty block goes down the path asked for, and the
-autotuner has measured a crossover density."""
+autotuner's crossover density is measured once and followed."""
 import numpy as np
 import pytest
 
@@ -56,4 +56,13 @@ def test_block_paths_agree_on_a_degree_sorted_graph():
           % (nz.max(), nz.min(), nz.max() / nz.min(), out[T.BLOCKS_AUTO][2][-1]["tune_density"],
              [st["sparse_blocks"] for st in out[T.BLOCKS_AUTO][2]]))
     assert nz.max() >= 5 * nz.min()  # uneven blocks (the full-size workloads reach >= 100x)
-    assert out[T.BLOCKS_AUTO][2][0]["tune_density"] > 0
+    # the autotuner measured a crossover once (0 when SpMM never wins: at this
+    # size the CSR build's per-cell cost can exceed the whole tensor-core
+    # pass) and the AUTO session's blocks followed it
+    td = out[T.BLOCKS_AUTO][2][0]["tune_density"]
+    assert np.isfinite(td) and td >= 0
+    assert all(st["tune_density"] == td for st in out[T.BLOCKS_AUTO][2])
+    for st in out[T.BLOCKS_AUTO][2]:
+        assert st["sparse_blocks"] <= st["factorized_blocks"]
+        if td == 0:
+            assert st["sparse_blocks"] == 0

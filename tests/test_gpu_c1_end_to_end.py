@@ -27,7 +27,14 @@ the push-order difference. Checked on every snapshot:
   the ln(x N) transform at rmax = 1e-6 that moves the root singular values
   by up to 5.3e-3, measured on a GB300); the largest principal-angle sine of
   the gap-separated leading subspace within 1e-2 against both (against the
-  independent one while its dirty decisions have agreed).
+  independent one while its dirty decisions have agreed). The leading
+  subspace ends at a relative gap of 5 % against the oracle on the GPU's
+  reserve; against the independent oracle, whose matrix differs from the
+  GPU's by the push-order freedom above (a few 1e-3 of the singular values),
+  it ends at a gap of 10 %, about twenty times that perturbation, so that
+  the subspace compared is separated from the rest by far more than the two
+  matrices differ (with a 5 % gap the first snapshot gave a sine of 1.1e-2,
+  measured on a GB300).
 
 The tree's embedding is not the exact SVD of the current matrix: blocks the
 lazy rule keeps are a snapshot old, and every block is truncated to rank d
@@ -172,13 +179,13 @@ def test_c1_end_to_end_against_the_fp64_oracle():
             emb = s.embedding()
             _, sig = s.tree_factor(0)
             assert np.isfinite(emb).all()
-            for name, ref_emb, ref_sig, tol in (("iso", emb_i, iso.sigma[0], 1e-3),
-                                                ("indep", emb_o, indep.sigma[0], 1e-2)):
+            for name, ref_emb, ref_sig, tol, gap in (("iso", emb_i, iso.sigma[0], 1e-3, 1.05),
+                                                     ("indep", emb_o, indep.sigma[0], 1e-2, 1.1)):
                 if not agreed[name]:
                     continue
                 rel = np.abs(sig - ref_sig) / ref_sig
                 assert rel.max() <= tol, (it, name, rel.max(), int(rel.argmax()))
-                j = gap_index(ref_sig, d)
+                j = gap_index(ref_sig, d, min_gap=gap)
                 assert j > 0
                 sine = max_principal_sine(emb[:, :j], ref_emb[:, :j])
                 assert sine <= 1e-2, (it, name, j, sine)

@@ -1,8 +1,14 @@
-"""Sampled parity at the Patent-sized directed configuration (N = 2,738,013,
-M = 13,960,811, |S| = 3000, 64 blocks, d = 128, q = 6, alpha = 0.2,
-rmax = 1e-7): one bench-sized session, its first (from-scratch) and second
-(dynamic, 1/38 of the edges) snapshots, checked on samples the CPU oracle
-can afford:
+"""Sampled parity at two bench-sized directed configurations, |S| = 3000,
+d = 128, q = 6, alpha = 0.2, rmax = 1e-7:
+
+* Patent-sized: N = 2,738,013, M = 13,960,811, 64 blocks; second snapshot
+  1/38 of the edges;
+* Wikipedia-sized, the latency workload: N = 6,216,199, M = 177,862,656,
+  128 blocks, a 70 % first snapshot then a 1 % (1,778,627-edge) delta; the
+  reserve in pinned host memory, as the bench runs it.
+
+One session each, its first (from-scratch) and second (dynamic) snapshots,
+checked on samples the CPU oracle can afford:
 
 * 64 of the 3000 sources: their PPR rows in both directions, against the
   oracle's FIFO push of the same sources on the same graph (each state within
@@ -58,15 +64,18 @@ def _transition_T(n, off, nbr):
     return P.T.tocsr(), deg
 
 
-def test_patent_sized_session_sampled_against_the_oracle():
+@pytest.mark.parametrize("name,blocks", [("rmat-d-2.7m", (0, 40)),
+                                         ("rmat-d-6.2m-1pct", (0, 90))])
+def test_bench_sized_session_sampled_against_the_oracle(name, blocks):
     try:
         import torch
         torch = torch if torch.cuda.is_available() else None
     except Exception:
         torch = None
-    cfg = W.scaled("rmat-d-2.7m")
+    cfg = W.scaled(name)
     _, snaps, src = W.build(cfg, seed=20231)
     kw = W.session_kwargs(cfg, dynamic_start=2, lazy_start=2)
+    kw["ppr_host_reserve"] = bool(cfg.get("host_reserve"))
     n, alpha, rmax, d = cfg["n"], cfg["alpha"], cfg["rmax"], cfg["rank_d"]
     rng = np.random.default_rng(64)
     rows = np.sort(rng.choice(len(src), 64, replace=False)).astype(np.int32)
@@ -93,7 +102,7 @@ def test_patent_sized_session_sampled_against_the_oracle():
                 assert excess.max() <= 0, (it, t, excess.max())
             if it == 1:
                 # every block was factorized in the first snapshot
-                for b in (0, 40):
+                for b in blocks:
                     A = s.block_dense(b).astype(np.float64)
                     Bg, sg = s.tree_factor(s.leaf_start + b)
                     omega = gaussian_matrix(kw["seed"], b, A.shape[1], d + 5)

@@ -37,7 +37,7 @@ TENANTS = [
 def _tenant(spec):
     cfg = W.scaled(spec["base"], n=spec["n"], m=spec["m"], sources=spec["sources"],
                    n_parts=spec["n_parts"], rank_d=spec["rank_d"], snapshots=4)
-    cfg["rmax"] = 1e-5
+    cfg["rmax"] = 1e-6  # rmax N ~ 0.01-0.03, the regime of the benchmark graphs
     _, snaps, src = W.build(cfg, seed=spec["seed"])
     kw = W.session_kwargs(cfg, dynamic_start=2, lazy_start=2)
     kw["dirty_rule"] = T.DIRTY_ALL
