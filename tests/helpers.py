@@ -58,12 +58,20 @@ def max_principal_sine(A, B):
     return float(np.sqrt(max(0.0, 1 - s.min() ** 2))) if len(s) else 0.0
 
 
-def gap_index(sig, k, min_gap=1.05):
-    """Largest j <= k whose singular value is separated from the next by min_gap."""
+def gap_index(sig, k, min_gap=1.05, min_abs=0.0):
+    """Largest j <= k whose singular value is separated from the next by the
+    ratio min_gap and by at least min_abs * sig[0]."""
     for j in range(k, 0, -1):
-        if j < len(sig) and sig[j] > 0 and sig[j - 1] / sig[j] >= min_gap:
+        if (j < len(sig) and sig[j] > 0 and sig[j - 1] / sig[j] >= min_gap and
+                sig[j - 1] - sig[j] >= min_abs * sig[0]):
             return j
     return 0
+
+
+def spectral_norm(D):
+    """||D||_2 of a wide matrix through its small Gram D D^T."""
+    G = D @ D.T
+    return float(np.sqrt(max(np.linalg.eigvalsh(G).max(), 0.0)))
 
 
 def gram_rel_err(B, B_ref):

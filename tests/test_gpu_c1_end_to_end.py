@@ -28,13 +28,12 @@ the push-order difference. Checked on every snapshot:
   by up to 5.3e-3, measured on a GB300); the largest principal-angle sine of
   the gap-separated leading subspace within 1e-2 against both (against the
   independent one while its dirty decisions have agreed). The leading
-  subspace ends at a relative gap of 5 % against the oracle on the GPU's
-  reserve; against the independent oracle, whose matrix differs from the
-  GPU's by the push-order freedom above (a few 1e-3 of the singular values),
-  it ends at a gap of 10 %, about twenty times that perturbation, so that
-  the subspace compared is separated from the rest by far more than the two
-  matrices differ (with a 5 % gap the first snapshot gave a sine of 1.1e-2,
-  measured on a GB300).
+  subspace ends at a relative gap of 5 %. Against the independent oracle the
+  two inputs differ (the push-order freedom above), and no algorithm can do
+  better than the rotation that difference itself causes: there the bound is
+  1e-2 or twice the sin-theta bound ||A_gpu - A_oracle||_2 / (sigma_j -
+  sigma_j+1) of the two log matrices, whichever is larger (the first
+  snapshot's 5 %-gap subspace turned by 1.1e-2, measured on a GB300).
 
 The tree's embedding is not the exact SVD of the current matrix: blocks the
 lazy rule keeps are a snapshot old, and every block is truncated to rank d
@@ -49,7 +48,7 @@ import scipy.sparse as sp
 
 import tsvd_gb300 as T
 import workloads as W
-from helpers import gap_index, max_principal_sine
+from helpers import gap_index, max_principal_sine, spectral_norm
 from oracle.tree_oracle import OracleTreeSVD, log_transform
 
 pytestmark = pytest.mark.gpu
@@ -179,16 +178,21 @@ def test_c1_end_to_end_against_the_fp64_oracle():
             emb = s.embedding()
             _, sig = s.tree_factor(0)
             assert np.isfinite(emb).all()
-            for name, ref_emb, ref_sig, tol, gap in (("iso", emb_i, iso.sigma[0], 1e-3, 1.05),
-                                                     ("indep", emb_o, indep.sigma[0], 1e-2, 1.1)):
+            dA = spectral_norm(log_transform(p, rmax, cfg["transform"], n) -
+                               log_transform(po, rmax, cfg["transform"], n))
+            for name, ref_emb, ref_sig, tol in (("iso", emb_i, iso.sigma[0], 1e-3),
+                                                ("indep", emb_o, indep.sigma[0], 1e-2)):
                 if not agreed[name]:
                     continue
                 rel = np.abs(sig - ref_sig) / ref_sig
                 assert rel.max() <= tol, (it, name, rel.max(), int(rel.argmax()))
-                j = gap_index(ref_sig, d, min_gap=gap)
+                j = gap_index(ref_sig, d)
                 assert j > 0
                 sine = max_principal_sine(emb[:, :j], ref_emb[:, :j])
-                assert sine <= 1e-2, (it, name, j, sine)
+                bound = 1e-2
+                if name == "indep":
+                    bound = max(bound, 2 * dA / (ref_sig[j - 1] - ref_sig[j]))
+                assert sine <= bound, (it, name, j, sine, bound)
             # ---- the algorithm's own distance to the exact SVD (reported)
             exact_sine = None
             if it in (0, len(snaps) // 2, len(snaps) - 1):

@@ -108,7 +108,11 @@ def test_bench_sized_session_sampled_against_the_oracle(name, blocks):
                     omega = gaussian_matrix(kw["seed"], b, A.shape[1], d + 5)
                     Uo, So, _ = oracle_frpca(A, d, cfg["passes_q"], omega=omega)
                     So, Uo = So[::-1], Uo[:, ::-1]
-                    j = gap_index(So, d)
+                    # the subspace whose gap is also 1e-3 of sigma_1: the
+                    # tensor-core products carry errors near 1e-5 of sigma_1,
+                    # which a smaller gap turns into a larger rotation
+                    # (sin-theta theorem)
+                    j = gap_index(So, d, min_abs=1e-3)
                     assert j > 0
                     rel = np.abs(sg[:j] / So[:j] - 1).max()
                     assert rel < 1e-3, (b, rel)

@@ -14,8 +14,10 @@ push states, like any two runs of the same session. The results must then
 agree within the tolerance every parity test states: root singular values
 (the squared column norms of the U sqrt(S) embedding) within 1e-3 relative
 and the largest principal-angle sine of the gap-separated leading subspace
-within 1e-2. Every block is refreshed every snapshot, so no lazy decision can
-part the two runs.
+within 1e-2 (the subspace ends where the gap is at least 5 % of the next
+singular value and 1e-3 of the largest, so rounding-level differences
+between the runs cannot rotate it). Every block is refreshed every
+snapshot, so no lazy decision can part the two runs.
 """
 import numpy as np
 import pytest
@@ -37,7 +39,7 @@ TENANTS = [
 def _tenant(spec):
     cfg = W.scaled(spec["base"], n=spec["n"], m=spec["m"], sources=spec["sources"],
                    n_parts=spec["n_parts"], rank_d=spec["rank_d"], snapshots=4)
-    cfg["rmax"] = 1e-6  # rmax N ~ 0.01-0.03, the regime of the benchmark graphs
+    cfg["rmax"] = 1e-7  # the serving workload's configured rmax
     _, snaps, src = W.build(cfg, seed=spec["seed"])
     kw = W.session_kwargs(cfg, dynamic_start=2, lazy_start=2)
     kw["dirty_rule"] = T.DIRTY_ALL
@@ -84,14 +86,14 @@ def test_each_result_is_the_same_alone_and_in_the_mix():
         sm = (mix ** 2).sum(axis=0)
         order = np.argsort(-sa)
         sa, sm = sa[order], sm[np.argsort(-sm)]
-        j = gap_index(sa, len(sa))
+        j = gap_index(sa, len(sa), min_abs=1e-3)
         assert j > 0, key
         assert np.allclose(sm[:j], sa[:j], rtol=1e-3), (key, np.abs(sm[:j] / sa[:j] - 1).max())
         ua = emb[:, order[:j]]
         um = mix[:, np.argsort(-(mix ** 2).sum(axis=0))[:j]]
         assert max_principal_sine(um, ua) <= 1e-2, key
     for t in sig_alone:
-        j = gap_index(sig_alone[t], len(sig_alone[t]))
+        j = gap_index(sig_alone[t], len(sig_alone[t]), min_abs=1e-3)
         assert np.allclose(sig_mix[t][:j], sig_alone[t][:j], rtol=1e-3), t
 
 

@@ -7,8 +7,8 @@
 //    layout the PPR state has) and the skinny operand split into hi + lo
 //    halves so that it keeps ~22 significant bits. 5th-generation tensor
 //    cores: tcgen05.mma kind::f16 into a tensor-memory accumulator (fp32),
-//    operands staged by a 4-stage cp.async pipeline, stages recycled on the
-//    MMAs' mbarrier.
+//    operands brought into shared memory by TMA (cp.async.bulk.tensor) in a
+//    5-stage pipeline of full / empty mbarriers.
 //  gram_batched : X^T X with error-free products and compensated sums per
 //    row chunk, chunks summed in fp64 (Code/frpca.c:101, cblas_dgemm TN).
 //  chol_inverse_batched / apply_right_batched : CholeskyQR2 normalization,
@@ -22,6 +22,7 @@
 #include <map>
 #include <mutex>
 #include <cfloat>
+#include <cstring>
 
 #include <cooperative_groups.h>
 
@@ -38,11 +39,6 @@ constexpr unsigned kFull = 0xffffffffu;
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
   return (uint32_t)__cvta_generic_to_shared(p);
 }
-__device__ __forceinline__ void cp_async16(void *smem, const void *gmem, bool valid) {
-  uint32_t s = smem_u32(smem);
-  int n = valid ? 16 : 0;
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(s), "l"(gmem), "r"(n));
-}
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
 template <int N>
 __device__ __forceinline__ void cp_async_wait() {
@@ -51,40 +47,54 @@ __device__ __forceinline__ void cp_async_wait() {
 // ------------------------------------------------------------------ GEMM tiles
 // The two frPCA products run on the 5th-generation tensor cores: one CTA
 // computes three 128 x 144 fp32 tiles in tensor memory (TMEM) with tcgen05.mma
-// kind::f16, issued by one thread; operand tiles are staged in shared memory
-// by cp.async in the no-swizzle core-matrix layout (8 rows x 16 bytes per
-// core matrix; LBO = distance between core matrices adjacent along K, SBO =
-// along M/N). A (the block, fp16) is K-major in the backward product
-// (A^T rows, k contiguous) and MN-major in the forward one; the skinny
-// operand (fp16 hi and lo halves, [k][144]) is MN-major in both, so every
-// operand row is copied from global memory as 16-byte pieces, unchanged.
-// A CTA computes MH = 3 row tiles of BM = 128 (three accumulators in TMEM,
-// 160 columns apart), so each staged tile of the skinny operand, which every
-// row tile re-reads from L2, serves 384 rows; K advances 32 at a time through
-// five stages.
+// kind::f16, issued by one thread. The operand tiles are brought into shared
+// memory by the Tensor Memory Accelerator: one producer thread issues
+// cp.async.bulk.tensor copies whose completion is counted (in bytes) on the
+// stage's "full" mbarrier; the MMA thread waits on it, issues the stage's
+// MMAs and commits them to the stage's "empty" mbarrier, which the producer
+// waits on before refilling the stage. Five stages of 32 K values are in
+// flight.
+//
+// Shared-memory layout: no-swizzle core matrices (8 rows x 16 bytes, 128
+// contiguous bytes; LBO = distance between core matrices adjacent along K,
+// SBO = along M/N). Each operand is described to the TMA as a 3-D view of
+// its row-major fp16 storage: {8 values (one 16-byte piece), rows, pieces
+// of a row (stride 16 bytes)}. A box of that view lands in shared memory in
+// that order, so the eight rows of a core matrix sit 16 bytes apart:
+//  * skinny operand (hi and lo halves, [k][144], MN-major in both
+//    products): box {8, 32 rows of K, 18 pieces of N}; piece (k, nb) at
+//    nb * 512 + k * 16 (LBO 128, SBO 512);
+//  * A of the forward product (A^T rows are K; MN-major): box {8, 32, 48};
+//    piece (k, mb) at mb * 512 + k * 16, so the three 128-row tiles are
+//    8 KB apart (LBO 128, SBO 512);
+//  * A of the backward product (A^T rows are M; K-major): one box
+//    {8, 128 rows, 4 pieces of K} per row tile; piece (m, kb) at
+//    kb * 2048 + m * 16 (LBO 2048, SBO 128).
+// Rows past a block's n_c and K past its end lie outside the view, and the
+// TMA fills them with zeros. Every copy starts at piece coordinate 0 of the
+// innermost dimension, on a 16-byte boundary.
 constexpr int BM = 128, MH = 3, BN = kLp, BK = 32, STAGES = 5, GEMM_THREADS = 128;
-constexpr int kKB = BK / 8;  // core matrices along K per stage
-constexpr int kCoreBytes = 128;                       // one 8 x 16-byte core matrix
-constexpr int kKBlockStride = kCoreBytes;             // LBO: next 8 values of K
-constexpr int kRowBlockStride = (BK / 8) * kCoreBytes;  // SBO: next 8 rows (M or N)
-constexpr int SA_BYTES = (BM / 8) * kRowBlockStride;  // 16 KB per row tile
-constexpr int SB_BYTES = (BN / 8) * kRowBlockStride;  // 18 KB
+constexpr int SA_BYTES = BM * BK * 2;  // 8 KB per row tile
+constexpr int SB_BYTES = BN * BK * 2;  // 9 KB per skinny half
 constexpr int STAGE_BYTES = MH * SA_BYTES + 2 * SB_BYTES;
 constexpr size_t kGemmSmem = (size_t)STAGES * STAGE_BYTES + 1024;  // + barriers, TMEM slot
+constexpr int kLboMn = 128, kSboMn = (BK / 8) * 128;  // MN-major operands
+constexpr int kLboK = BM * 16, kSboK = 128;           // K-major A (backward)
 constexpr int kTmemCols = 512;                        // MH accumulators, kAccStride apart
 constexpr int kAccStride = 160;
 static_assert(MH * kAccStride <= kTmemCols && kAccStride >= BN, "accumulators fit in TMEM");
-static_assert(kKB == 4 || kKB == 8, "load mappings assume 4 or 8 core matrices along K");
 static_assert(BN % 16 == 0 && BN <= 256, "tcgen05.mma with M = 128 needs N % 16 == 0, N <= 256");
+static_assert(STAGE_BYTES % 1024 == 0 && SA_BYTES % 128 == 0 && SB_BYTES % 128 == 0,
+              "TMA destinations stay 128-byte aligned");
 
 // Counts waits that ran out (a kernel that gives up skips its tile and
 // frees its tensor memory; the host turns a non-zero count into an error).
 __device__ int g_umma_timeouts = 0;
 
-__device__ __forceinline__ uint64_t umma_smem_desc(uint32_t saddr) {
+__device__ __forceinline__ uint64_t umma_smem_desc(uint32_t saddr, int lbo, int sbo) {
   uint64_t d = (uint64_t)((saddr >> 4) & 0x3FFFu);
-  d |= (uint64_t)((kKBlockStride >> 4) & 0x3FFF) << 16;
-  d |= (uint64_t)((kRowBlockStride >> 4) & 0x3FFF) << 32;
+  d |= (uint64_t)((lbo >> 4) & 0x3FFF) << 16;
+  d |= (uint64_t)((sbo >> 4) & 0x3FFF) << 32;
   d |= (uint64_t)1 << 46;  // descriptor version of tcgen05; base offset 0, no swizzle
   return d;
 }
@@ -96,26 +106,56 @@ __host__ __device__ constexpr uint32_t umma_idesc(int a_mn) {
          ((uint32_t)(BM >> 4) << 24);
 }
 
+__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
+  uint32_t done;
+  asm volatile(
+      "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      "selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(done)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return done != 0;
+}
+
 __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+  for (int it = 0; it < (1 << 24); ++it)
+    if (mbar_try(bar, parity)) return true;
+  return false;
+}
+
+// The same wait, also ending (false) once the CTA's failure flag is set.
+__device__ __forceinline__ bool mbar_wait_or_fail(uint32_t bar, uint32_t parity,
+                                                  volatile int *failed) {
   for (int it = 0; it < (1 << 24); ++it) {
-    uint32_t done;
-    asm volatile(
-        "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-        "selp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(done)
-        : "r"(bar), "r"(parity)
-        : "memory");
-    if (done) return true;
+    if (mbar_try(bar, parity)) return true;
+    if (*failed) return false;
   }
   return false;
 }
 
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bar), "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap *map, int c0, int c1,
+                                            int c2, uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3, %4}], [%5];\n" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(bar)
+      : "memory");
+}
+
 struct GemmArgs {
-  const __half *const *at;
+  const CUtensorMap *maps;  // 3 per problem: A, skinny hi, skinny lo
   const int32_t *ncols;
   int lda;  // Sp
-  const __half *const *bhi;
-  const __half *const *blo;
+  int has_lo;
   float *const *out;
   float scale;
   int splits;  // fwd split-K
@@ -128,8 +168,10 @@ template <bool FWD>
 __global__ void __launch_bounds__(GEMM_THREADS, 1) umma_gemm_kernel(GemmArgs a) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char *stage_base = smem_raw;
-  uint64_t *bars = reinterpret_cast<uint64_t *>(smem_raw + (size_t)STAGES * STAGE_BYTES);
-  uint32_t *tslot = reinterpret_cast<uint32_t *>(bars + STAGES);
+  uint64_t *full = reinterpret_cast<uint64_t *>(smem_raw + (size_t)STAGES * STAGE_BYTES);
+  uint64_t *empty = full + STAGES;
+  uint32_t *tslot = reinterpret_cast<uint32_t *>(empty + STAGES);
+  volatile int *failed = reinterpret_cast<volatile int *>(tslot + 1);
   const int prob = blockIdx.z;
   const int nc = a.ncols[prob];
   const int m0 = blockIdx.x * (BM * MH);
@@ -139,99 +181,90 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1) umma_gemm_kernel(GemmArgs a) 
   const int per = (nk_total + a.splits - 1) / a.splits;
   const int kt0 = blockIdx.y * per, kt1 = min(nk_total, kt0 + per);
   if (kt0 >= kt1) return;
-  const int krows = FWD ? nc : a.lda;  // valid K
-  const __half *at = a.at[prob];
-  const __half *bhi = a.bhi[prob];
-  const __half *blo = a.blo ? a.blo[prob] : nullptr;
-  const int tid = threadIdx.x, warp = tid >> 5;
+  const int nk = kt1 - kt0;
+  const CUtensorMap *map_a = a.maps + 3 * (int64_t)prob;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const uint32_t tx_bytes = MH * SA_BYTES + (a.has_lo ? 2 : 1) * SB_BYTES;
 
-  // Operand tiles of stage `st` for K tile kt, as 16-byte pieces. Eight
-  // consecutive lanes fill the eight 16-byte rows of one core matrix (one
-  // shared-memory wavefront, no bank conflicts); four such groups of a warp
-  // read four adjacent pieces of the same global row (64 contiguous bytes).
-  auto load_stage = [&](int st, int kt) {
-    // the MH row tiles' A operands are adjacent: row block mb of the CTA at
-    // mb * SBO (tile mb / 16 starts at SA_BYTES * (mb / 16))
-    unsigned char *sa = stage_base + (size_t)st * STAGE_BYTES;
-    unsigned char *sbh = sa + MH * SA_BYTES, *sbl = sbh + SB_BYTES;
-    const int k0 = kt * BK;
-    if (FWD) {  // A MN-major: piece (k, rows mb*8..+7) = A^T[k0 + k][m0 + mb*8 ..]
-      for (int c = tid; c < BK * (MH * BM / 8); c += GEMM_THREADS) {
-        const int kq = c & 7, mbq = (c >> 3) & 3, rest = c >> 5;
-        const int k = (rest % kKB) * 8 + kq, mb = (rest / kKB) * 4 + mbq;
-        const bool valid = k0 + k < krows && m0 + mb * 8 < a.lda;
-        const __half *g = valid ? at + (int64_t)(k0 + k) * a.lda + m0 + mb * 8 : at;
-        cp_async16(sa + mb * kRowBlockStride + k * 16, g, valid);
-      }
-    } else {  // A K-major: piece (row m, k = kb*8..+7) = A^T[m0 + m][k0 + kb*8 ..]
-      for (int c = tid; c < MH * BM * (BK / 8); c += GEMM_THREADS) {
-        const int mq = c & 7, kb = (c >> 3) % kKB, m = ((c >> 3) / kKB) * 8 + mq;
-        const bool valid = m0 + m < nc;
-        const __half *g = valid ? at + (int64_t)(m0 + m) * a.lda + k0 + kb * 8 : at;
-        cp_async16(sa + (m >> 3) * kRowBlockStride + kb * kKBlockStride + mq * 16, g, valid);
-      }
+  if (tid == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      mbar_init(smem_u32(full + s), 1);
+      mbar_init(smem_u32(empty + s), 1);
     }
-    // skinny operand MN-major: piece (k, columns nb*8..+7) = B[k0 + k][nb*8 ..]
-    constexpr int kPieces = BK * (BN / 8);
-    for (int c = tid; c < 2 * kPieces; c += GEMM_THREADS) {
-      const int which = c >= kPieces, cc = c - which * kPieces;
-      const int kq = cc & 7, rest = cc >> 3;
-      const int nb = rest % (BN / 8), k = (rest / (BN / 8)) * 8 + kq;
-      const __half *src = which ? blo : bhi;
-      const bool valid = k0 + k < krows && src != nullptr;
-      const __half *g = valid ? src + (int64_t)(k0 + k) * BN + nb * 8 : bhi;
-      cp_async16((which ? sbl : sbh) + nb * kRowBlockStride + k * 16, g, valid);
-    }
-  };
-
-  if (tid == 0)
-    for (int s = 0; s < STAGES; ++s)
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(bars + s)));
+    *failed = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(
                      smem_u32(tslot)),
                  "n"(kTmemCols));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::);
   }
-  for (int s = 0; s < STAGES - 1; ++s) {
-    if (kt0 + s < kt1) load_stage(s, kt0 + s);
-    cp_async_commit();
-  }
   asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
   const uint32_t tmem = *tslot;
-  constexpr uint32_t idesc = umma_idesc(FWD ? 1 : 0);
-  // every decision below is the same in all threads (__syncthreads_and), so
-  // no thread leaves the loop while another waits at its barrier
-  bool ok = true;
-  int issued = 0;  // K tiles whose MMAs were issued
-  for (int kt = kt0; kt < kt1; ++kt) {
-    const int i = kt - kt0, st = i % STAGES;
-    cp_async_wait<STAGES - 2>();
-    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");  // copies -> tensor core reads
-    if (!__syncthreads_and(ok)) {
-      ok = false;
-      break;
+
+  if (warp == 0 && lane == 0) {
+    // producer: fill stage i % STAGES with K tile kt0 + i once the MMAs that
+    // read its previous contents (tile i - STAGES) have completed
+    for (int j = 0; j < 3; ++j)
+      asm volatile("prefetch.tensormap [%0];\n" ::"l"(reinterpret_cast<uint64_t>(map_a + j))
+                   : "memory");
+    int filled = 0;
+    for (int i = 0; i < nk; ++i) {
+      const int st = i % STAGES;
+      if (i >= STAGES &&
+          !mbar_wait_or_fail(smem_u32(empty + st), (uint32_t)((i / STAGES - 1) & 1), failed)) {
+        *failed = 1;
+        break;
+      }
+      const uint32_t fb = smem_u32(full + st);
+      const uint32_t sa = smem_u32(stage_base + (size_t)st * STAGE_BYTES);
+      const int k0 = (kt0 + i) * BK;
+      mbar_expect_tx(fb, tx_bytes);
+      if (FWD) {
+        tma_load_3d(sa, map_a, 0, k0, m0 / 8, fb);
+      } else {
+#pragma unroll
+        for (int h = 0; h < MH; ++h) tma_load_3d(sa + h * SA_BYTES, map_a, 0, m0 + h * BM, k0 / 8, fb);
+      }
+      tma_load_3d(sa + MH * SA_BYTES, map_a + 1, 0, k0, 0, fb);
+      if (a.has_lo) tma_load_3d(sa + MH * SA_BYTES + SB_BYTES, map_a + 2, 0, k0, 0, fb);
+      filled = i + 1;
     }
-    if (tid == 0) {
+    // no copy may still be writing shared memory when the CTA exits: wait for
+    // the last fill of every stage (those the MMA thread consumed are done)
+    for (int i = max(0, filled - STAGES); i < filled; ++i)
+      if (!mbar_wait(smem_u32(full + i % STAGES), (uint32_t)((i / STAGES) & 1))) *failed = 1;
+  } else if (warp == 1 && lane == 0) {
+    // MMA issuer
+    constexpr uint32_t idesc = umma_idesc(FWD ? 1 : 0);
+    constexpr int a_lbo = FWD ? kLboMn : kLboK, a_sbo = FWD ? kSboMn : kSboK;
+    int issued = 0;
+    for (int i = 0; i < nk; ++i) {
+      const int st = i % STAGES;
+      if (!mbar_wait_or_fail(smem_u32(full + st), (uint32_t)((i / STAGES) & 1), failed)) {
+        *failed = 1;
+        break;
+      }
       asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
       const uint32_t sa = smem_u32(stage_base + (size_t)st * STAGE_BYTES);
       const uint32_t sbh = sa + MH * SA_BYTES, sbl = sbh + SB_BYTES;
 #pragma unroll
       for (int ks = 0; ks < BK / 16; ++ks) {
-        const uint64_t bdh = umma_smem_desc(sbh + ks * 2 * kKBlockStride);
-        const uint64_t bdl = umma_smem_desc(sbl + ks * 2 * kKBlockStride);
+        const uint64_t bdh = umma_smem_desc(sbh + ks * 2 * kLboMn, kLboMn, kSboMn);
+        const uint64_t bdl = umma_smem_desc(sbl + ks * 2 * kLboMn, kLboMn, kSboMn);
         const uint32_t acc0 = (i > 0 || ks > 0) ? 1u : 0u;
 #pragma unroll
         for (int h = 0; h < MH; ++h) {
-          const uint64_t ad = umma_smem_desc(sa + h * SA_BYTES + ks * 2 * kKBlockStride);
+          const uint64_t ad = umma_smem_desc(sa + h * SA_BYTES + ks * 2 * a_lbo, a_lbo, a_sbo);
           const uint32_t td = tmem + (uint32_t)(h * kAccStride);
           asm volatile(
               "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
               "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(td),
               "l"(ad), "l"(bdh), "r"(idesc), "r"(acc0));
-          if (blo)
+          if (a.has_lo)
             asm volatile(
                 "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
                 "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(td),
@@ -240,33 +273,22 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1) umma_gemm_kernel(GemmArgs a) 
       }
       asm volatile(
           "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
-              smem_u32(bars + st))
+              smem_u32(empty + st))
           : "memory");
+      issued = i + 1;
     }
-    issued = i + 1;
-    // refill the stage the previous tile's MMAs read, once they are done
-    const int nxt = kt + STAGES - 1;
-    if (nxt < kt1) {
-      if (i >= 1) {
-        const int pi = i - 1;
-        ok = mbar_wait(smem_u32(bars + pi % STAGES), (uint32_t)((pi / STAGES) & 1));
-      }
-      if (ok) load_stage((nxt - kt0) % STAGES, nxt);
+    // the last commit covers every MMA issued before it; wait for it even
+    // after a failure, so no MMA still writes the tensor memory freed below
+    if (issued > 0) {
+      const int li = issued - 1;
+      if (!mbar_wait(smem_u32(empty + li % STAGES), (uint32_t)((li / STAGES) & 1))) *failed = 1;
     }
-    cp_async_commit();
   }
-  // the last commit covers every MMA issued before it; wait for it even
-  // after a timeout, so no MMA still writes the tensor memory freed below
-  bool done = issued == 0;
-  if (issued > 0) {
-    const int li = issued - 1;
-    done = mbar_wait(smem_u32(bars + li % STAGES), (uint32_t)((li / STAGES) & 1));
-  }
-  ok = __syncthreads_and(ok && done);
-  cp_async_wait<0>();
+  __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+  const bool ok = *failed == 0;
   if (!ok) {
-    if ((tid & 31) == 0) atomicAdd(&g_umma_timeouts, 1);
+    if (lane == 0) atomicAdd(&g_umma_timeouts, 1);
   } else {
     // epilogue: warp w reads TMEM lanes 32w..32w+31 of accumulator h = output
     // rows m0 + 128 h + 32 w + lane
@@ -274,7 +296,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1) umma_gemm_kernel(GemmArgs a) 
     const bool atomic = FWD && a.splits > 1;
 #pragma unroll 1
     for (int h = 0; h < MH; ++h) {
-      const int row = m0 + h * BM + warp * 32 + (tid & 31);
+      const int row = m0 + h * BM + warp * 32 + lane;
 #pragma unroll 1
       for (int c0 = 0; c0 < BN; c0 += 16) {
         uint32_t v[16];
@@ -1002,11 +1024,75 @@ static tsvd_status set_smem(const void *fn, size_t bytes) {
   return TSVD_OK;
 }
 
-tsvd_status gemm_fwd(const GemmBatch &gb, const __half *const *xhi, const __half *const *xlo,
-                     float *const *y, float *y_base, size_t y_bytes, int sp, int max_nc,
-                     float inv_xscale, cudaStream_t st) {
+// cuTensorMapEncodeTiled, resolved from the driver at run time (the library
+// links only the runtime).
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
+                                  const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
+                                  const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn tensor_map_encoder() {
+  static const EncodeTiledFn fn = [] {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    cudaError_t e =
+        cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q);
+    if (e != cudaSuccess || q != cudaDriverEntryPointSuccess) {
+      cudaGetLastError();
+      return (EncodeTiledFn) nullptr;
+    }
+    return reinterpret_cast<EncodeTiledFn>(p);
+  }();
+  return fn;
+}
+
+// The 3-D piece view of a row-major fp16 matrix [rows][pitch]: {8 values,
+// rows (stride 2 pitch bytes), pitch / 8 pieces (stride 16 bytes)}, with a
+// {8, box_rows, box_pieces} box.
+static tsvd_status encode_pieces(CUtensorMap *m, const __half *base, int64_t rows, int pitch,
+                                 int box_rows, int box_pieces) {
+  const EncodeTiledFn fn = tensor_map_encoder();
+  if (!fn) return fail(TSVD_ERR_DEVICE, "cuTensorMapEncodeTiled is not available from the driver");
+  if (!base || (reinterpret_cast<uintptr_t>(base) & 15) != 0 || pitch % 8 != 0)
+    return fail(TSVD_ERR_INVALID, "tensor map: operand %p / pitch %d not 16-byte aligned",
+                (const void *)base, pitch);
+  const cuuint64_t dims[3] = {8, (cuuint64_t)std::max<int64_t>(rows, 1), (cuuint64_t)(pitch / 8)};
+  const cuuint64_t strides[2] = {(cuuint64_t)pitch * 2, 16};
+  const cuuint32_t box[3] = {8, (cuuint32_t)box_rows, (cuuint32_t)box_pieces};
+  const cuuint32_t estride[3] = {1, 1, 1};
+  const CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 3, (void *)base, dims, strides, box,
+                        estride, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                        CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS)
+    return fail(TSVD_ERR_DEVICE, "cuTensorMapEncodeTiled: error %d (rows %lld, pitch %d, box %d x %d)",
+                (int)r, (long long)rows, pitch, box_rows, box_pieces);
+  return TSVD_OK;
+}
+
+tsvd_status gemm_encode_maps(int fwd, int nprob, const __half *const *at, const int32_t *nc,
+                             int lda, const __half *const *hi, const __half *const *lo,
+                             CUtensorMap *out) {
+  for (int i = 0; i < nprob; ++i) {
+    CUtensorMap *m = out + 3 * (int64_t)i;
+    if (fwd)
+      TSVD_TRY(encode_pieces(m, at[i], nc[i], lda, BK, MH * BM / 8));
+    else
+      TSVD_TRY(encode_pieces(m, at[i], nc[i], lda, BM, BK / 8));
+    const int64_t brows = fwd ? nc[i] : lda;
+    TSVD_TRY(encode_pieces(m + 1, hi[i], brows, BN, BK, BN / 8));
+    if (lo && lo[i])
+      TSVD_TRY(encode_pieces(m + 2, lo[i], brows, BN, BK, BN / 8));
+    else
+      memset(m + 2, 0, sizeof(CUtensorMap));
+  }
+  return TSVD_OK;
+}
+
+tsvd_status gemm_fwd(const GemmBatch &gb, bool has_lo, float *const *y, float *y_base,
+                     size_t y_bytes, int sp, int max_nc, float inv_xscale, cudaStream_t st) {
   if (gb.nprob == 0) return TSVD_OK;
   if (sp % BM != 0) return fail(TSVD_ERR_INVALID, "gemm_fwd: Sp = %d not a multiple of %d", sp, BM);
+  if (!gb.maps) return fail(TSVD_ERR_INVALID, "gemm_fwd: no tensor maps");
   TSVD_TRY(set_smem((const void *)umma_gemm_kernel<true>, kGemmSmem));
   const int mtiles = (int)ceil_div(sp, BM * MH);
   int splits = 1;
@@ -1017,19 +1103,20 @@ tsvd_status gemm_fwd(const GemmBatch &gb, const __half *const *xhi, const __half
                                     std::max<int64_t>(1, ceil_div(max_nc, 1024)));
   // split-K partial tiles are accumulated with atomics into zeroed outputs
   if (splits > 1) TSVD_CUDA(cudaMemsetAsync(y_base, 0, y_bytes, st));
-  GemmArgs a{gb.at, gb.ncols, gb.lda, xhi, xlo, y, inv_xscale, splits};
+  GemmArgs a{gb.maps, gb.ncols, gb.lda, has_lo ? 1 : 0, y, inv_xscale, splits};
   dim3 grid(mtiles, splits, gb.nprob);
   umma_gemm_kernel<true><<<grid, GEMM_THREADS, kGemmSmem, st>>>(a);
   TSVD_LAUNCH_CHECK();
   return TSVD_OK;
 }
 
-tsvd_status gemm_bwd(const GemmBatch &gb, const __half *const *yhi, const __half *const *ylo,
-                     float *const *z, int sp, int max_nc, float inv_yscale, cudaStream_t st) {
+tsvd_status gemm_bwd(const GemmBatch &gb, bool has_lo, float *const *z, int sp, int max_nc,
+                     float inv_yscale, cudaStream_t st) {
   if (gb.nprob == 0 || max_nc == 0) return TSVD_OK;
   if (sp % BK != 0) return fail(TSVD_ERR_INVALID, "gemm_bwd: Sp = %d not a multiple of %d", sp, BK);
+  if (!gb.maps) return fail(TSVD_ERR_INVALID, "gemm_bwd: no tensor maps");
   TSVD_TRY(set_smem((const void *)umma_gemm_kernel<false>, kGemmSmem));
-  GemmArgs a{gb.at, gb.ncols, sp, yhi, ylo, z, inv_yscale, 1};
+  GemmArgs a{gb.maps, gb.ncols, sp, has_lo ? 1 : 0, z, inv_yscale, 1};
   dim3 grid((unsigned)ceil_div(max_nc, BM * MH), 1, gb.nprob);
   umma_gemm_kernel<false><<<grid, GEMM_THREADS, kGemmSmem, st>>>(a);
   TSVD_LAUNCH_CHECK();

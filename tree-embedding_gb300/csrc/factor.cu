@@ -213,6 +213,9 @@ tsvd_status frpca_work_alloc(FrpcaWork &W, int nmax, int64_t rows_max, int sp, i
   TSVD_CUDA(cudaMallocHost(&W.hptr, W.ptr_slots * sizeof(void *)));
   TSVD_CUDA(cudaMalloc(&W.dint, W.ptr_slots * sizeof(int32_t)));
   TSVD_CUDA(cudaMallocHost(&W.hint, W.ptr_slots * sizeof(int32_t)));
+  W.tmap_slots = (size_t)nmax * 6;
+  TSVD_CUDA(cudaMalloc(&W.tmap_dev, W.tmap_slots * sizeof(CUtensorMap)));
+  TSVD_CUDA(cudaMallocHost(&W.tmap_host, W.tmap_slots * sizeof(CUtensorMap)));
   for (double **p : {&W.dv, &W.dt, &W.dh})
     TSVD_CUDA(cudaMalloc(p, (size_t)nmax * 256 * 256 * sizeof(double)));
   {
@@ -229,6 +232,7 @@ void frpca_work_free(FrpcaWork &W) {
   cudaFree(W.qlo); cudaFree(W.g); cudaFree(W.t); cudaFree(W.lambda); cudaFree(W.v);
   cudaFree(W.colscale); cudaFree(W.sums); cudaFree(W.gram_work); cudaFree(W.jac_work); cudaFree(W.dptr);
   cudaFreeHost(W.hptr); cudaFree(W.dint); cudaFreeHost(W.hint);
+  cudaFree(W.tmap_dev); cudaFreeHost(W.tmap_host);
   cudaFree(W.wm); cudaFree(W.wv); cudaFree(W.ww); cudaFree(W.wy); cudaFree(W.wy2);
   cudaFree(W.wchol); cudaFree(W.wnorm); cudaFree(W.wk);
   cudaFree(W.dv); cudaFree(W.dt); cudaFree(W.dh); cudaFree(W.dh_ptrs);
@@ -375,8 +379,19 @@ tsvd_status frpca_batch(FrpcaWork &W, const FrpcaProblem *probs, int nprob, int 
                 *d_cbase = pk.add_int(cbase), *d_blk = pk.add_int(blk),
                 *d_srcrows = pk.add_int(srcrows);
   TSVD_TRY(pk.upload(st));
-
-  GemmBatch gb{d_at, d_nc, sp, nprob};
+  // tensor maps of the products: forward (A, X hi, X lo), backward (A, Q hi, Q lo)
+  if (!sparse) {
+    if ((size_t)nprob * 6 > W.tmap_slots)
+      return fail(TSVD_ERR_INVALID, "frpca: %d problems exceed the tensor-map area", nprob);
+    TSVD_TRY(gemm_encode_maps(1, nprob, at.data(), ncols.data(), sp, xhi.data(), xlo.data(),
+                              W.tmap_host));
+    TSVD_TRY(gemm_encode_maps(0, nprob, at.data(), ncols.data(), sp, qhi.data(), qlo.data(),
+                              W.tmap_host + 3 * (size_t)nprob));
+    TSVD_CUDA(cudaMemcpyAsync(W.tmap_dev, W.tmap_host, sizeof(CUtensorMap) * 6 * nprob,
+                              cudaMemcpyHostToDevice, st));
+  }
+  const GemmBatch gb_fwd{d_nc, sp, nprob, W.tmap_dev};
+  const GemmBatch gb_bwd{d_nc, sp, nprob, W.tmap_dev + 3 * (size_t)nprob};
   const size_t ybytes = (size_t)nprob * SK * sizeof(float);
   // Y = A X (sp x kLp) and Z = A^T Q (n_c x kLp): tensor-core GEMMs on the
   // half-precision A^T, or FP32 SpMM over the block's CSR / CSC
@@ -384,13 +399,13 @@ tsvd_status frpca_batch(FrpcaWork &W, const FrpcaProblem *probs, int nprob, int 
                       float scale) -> tsvd_status {
     if (sparse)
       return spmm_batched(d_rptr, d_ridx, d_rval, d_sprows, sp, hi, lo, d_y, scale, nprob, st);
-    return gemm_fwd(gb, hi, lo, d_y, W.y, ybytes, sp, max_nc, scale, st);
+    return gemm_fwd(gb_fwd, lo != nullptr, d_y, W.y, ybytes, sp, max_nc, scale, st);
   };
   auto prod_bwd = [&](const __half *const *hi, const __half *const *lo,
                       float scale) -> tsvd_status {
     if (sparse)
       return spmm_batched(d_cptr, d_cidx, d_cval, d_nc, max_nc, hi, lo, d_z, scale, nprob, st);
-    return gemm_bwd(gb, hi, lo, d_z, sp, max_nc, scale, st);
+    return gemm_bwd(gb_bwd, lo != nullptr, d_z, sp, max_nc, scale, st);
   };
   const int niter = (q - 1) / 2;
   float in_scale = 1.f / kSplitScale;
@@ -771,14 +786,18 @@ tsvd_status lp_right_batch(FrpcaWork &W, const LpProblem *probs, int nprob, cons
     max_nc = std::max(max_nc, (int)probs[i].ncols);
   }
   if (max_nc == 0) return TSVD_OK;
+  if ((size_t)nprob * 3 > W.tmap_slots)
+    return fail(TSVD_ERR_INVALID, "lp: %d blocks exceed the tensor-map area", nprob);
   PtrPack pk(W);
-  auto d_at = pk.add(at);
-  auto d_yhi = pk.add(yhi), d_ylo = pk.add(ylo);
   auto d_z = pk.add(z);
   const int32_t *d_nc = pk.add_int(nc);
   TSVD_TRY(pk.upload(st));
-  GemmBatch gb{d_at, d_nc, W.sp, nprob};
-  TSVD_TRY(gemm_bwd(gb, d_yhi, d_ylo, d_z, W.sp, max_nc, 1.f / kSplitScale, st));
+  TSVD_TRY(gemm_encode_maps(0, nprob, at.data(), nc.data(), W.sp, yhi.data(), ylo.data(),
+                            W.tmap_host));
+  TSVD_CUDA(cudaMemcpyAsync(W.tmap_dev, W.tmap_host, sizeof(CUtensorMap) * 3 * nprob,
+                            cudaMemcpyHostToDevice, st));
+  const GemmBatch gb{d_nc, W.sp, nprob, W.tmap_dev};
+  TSVD_TRY(gemm_bwd(gb, true, d_z, W.sp, max_nc, 1.f / kSplitScale, st));
   return gemm_check(st);
 }
 

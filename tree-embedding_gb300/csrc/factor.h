@@ -27,6 +27,9 @@ struct FrpcaWork {
   size_t ptr_slots = 0;
   int32_t *dint = nullptr; // device int area (row counts, block ids)
   int32_t *hint = nullptr;
+  CUtensorMap *tmap_dev = nullptr;   // tensor maps of the products: 6 per problem
+  CUtensorMap *tmap_host = nullptr;  // pinned staging for them
+  size_t tmap_slots = 0;
   int last_sweeps = 0;
   double *dv = nullptr, *dt = nullptr, *dh = nullptr;  // [nmax][256*256] eigen refinement
   double **dh_ptrs = nullptr;  // device: dh + i 256^2 for each problem i

@@ -75,6 +75,7 @@ constexpr size_t kSigB = al(kNaMaxK * 4);
 constexpr size_t kMiscB = al(16);
 constexpr size_t kRefB = al((size_t)kNaMaxL * kNaMaxL * 8);  // eigen refinement (fp64)
 constexpr size_t kHpB = al(8);                                // device pointer to dh
+constexpr size_t kTmapB = al(6 * sizeof(CUtensorMap));        // the products' tensor maps
 
 constexpr size_t kOffAt = 0;
 constexpr size_t kOffXhi = kOffAt + kAtB;
@@ -106,7 +107,8 @@ constexpr size_t kOffDv = kOffMisc + kMiscB;
 constexpr size_t kOffDt = kOffDv + kRefB;
 constexpr size_t kOffDh = kOffDt + kRefB;
 constexpr size_t kOffHp = kOffDh + kRefB;
-constexpr size_t kNoallocScratchBytes = kOffHp + kHpB;
+constexpr size_t kOffTmap = kOffHp + kHpB;
+constexpr size_t kNoallocScratchBytes = kOffTmap + kTmapB;
 
 __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocScratchBytes];
 
@@ -117,6 +119,7 @@ float g_hu[kNaMaxRows * kNaMaxK];
 float g_hv[kNaMaxUsedCols * kNaMaxK];
 float g_hs[kNaMaxK];
 int32_t g_hcmap[kNaMaxUsedCols];
+alignas(64) CUtensorMap g_htmap[6];
 
 constexpr int kMaxDevices = 64;
 unsigned char *g_dev_scratch[kMaxDevices] = {nullptr};
@@ -329,6 +332,9 @@ extern "C" tsvd_status tsvd_frpca_noalloc(int32_t nrows, int32_t ncols, int64_t 
     W.dt = (double *)(base + kOffDt);
     W.dh = (double *)(base + kOffDh);
     W.dh_ptrs = (double **)(base + kOffHp);
+    W.tmap_dev = (CUtensorMap *)(base + kOffTmap);
+    W.tmap_host = g_htmap;
+    W.tmap_slots = 6;
     FrpcaProblem P;
     P.block = 0;
     P.at = (const __half *)(base + kOffAt);

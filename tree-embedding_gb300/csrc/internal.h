@@ -1,5 +1,6 @@
 // Internal declarations shared by the CUDA translation units.
 #pragma once
+#include <cuda.h>  // CUtensorMap (the encoder is resolved at run time; no libcuda link)
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -82,22 +83,29 @@ void adjacency_free(Adjacency &A);
 // ---------------------------------------------------------------- dense ops
 struct GemmBatch {
   // Per problem (device arrays of length nprob):
-  const __half *const *at;   // A^T storage: [rows_k][lda] (vertex-major block)
   const int32_t *ncols;      // n_c of each block (the K of fwd / M of bwd)
   int lda;                   // = Sp
   int nprob;
+  // device, 3 per problem (gemm_encode_maps): A^T, skinny hi, skinny lo
+  const CUtensorMap *maps;
 };
+
+// Tensor maps of one batch of products, written to out[3 i .. 3 i + 2] for
+// problem i: the block A^T (at[i], nc[i] rows of pitch lda, fp16) as the
+// forward (fwd = 1) or backward product's A operand, and the skinny hi / lo
+// halves (kLp columns; nc[i] rows in the forward product, lda in the
+// backward one; lo may be null). Host pointers; out is host memory.
+tsvd_status gemm_encode_maps(int fwd, int nprob, const __half *const *at, const int32_t *nc,
+                             int lda, const __half *const *hi, const __half *const *lo,
+                             CUtensorMap *out);
 
 // Y[b] (Sp x Lp fp32) = A_b (Sp x n_c) * (Xhi + Xlo)[b] (n_c x Lp) * scale.
 // y_base/y_bytes: the contiguous allocation behind y (zeroed for split-K).
-tsvd_status gemm_fwd(const GemmBatch &gb, const __half *const *xhi,
-                     const __half *const *xlo, float *const *y, float *y_base,
-                     size_t y_bytes, int sp, int max_nc, float inv_xscale,
-                     cudaStream_t st);
+tsvd_status gemm_fwd(const GemmBatch &gb, bool has_lo, float *const *y, float *y_base,
+                     size_t y_bytes, int sp, int max_nc, float inv_xscale, cudaStream_t st);
 // Z[b] (n_c x Lp fp32) = A_b^T (n_c x Sp) * (Yhi + Ylo)[b] (Sp x Lp) * scale
-tsvd_status gemm_bwd(const GemmBatch &gb, const __half *const *yhi,
-                     const __half *const *ylo, float *const *z, int sp,
-                     int max_nc, float inv_yscale, cudaStream_t st);
+tsvd_status gemm_bwd(const GemmBatch &gb, bool has_lo, float *const *z, int sp, int max_nc,
+                     float inv_yscale, cudaStream_t st);
 // Non-zero if a tensor-core GEMM gave up waiting for its MMAs since the last
 // check (a bounded wait ran out); synchronizes the stream.
 tsvd_status gemm_check(cudaStream_t st);
