@@ -80,6 +80,11 @@ def parse():
     ap.add_argument("--cpu-sources", type=int, default=None,
                     help="sources in the CPU sample (default: two per host thread)")
     ap.add_argument("--seed", type=int, default=20231)
+    ap.add_argument("--push-levels", type=int, default=None,
+                    help="threshold schedule levels of the push (default: the library's)")
+    ap.add_argument("--push-ratio", type=float, default=None)
+    ap.add_argument("--push-hub-degree", type=int, default=None,
+                    help="apply the threshold schedule to vertices of at least this degree only")
     ap.add_argument("--serve", action="store_true",
                     help="serving measurement instead of the headline: tenants of different sizes "
                          "on one GPU, Poisson-arriving edge batches, p50/p99 request latency")
@@ -191,6 +196,9 @@ def run_ours(args, cfg, snaps, sources, device):
     kw["device"] = device
     kw["seed"] = args.seed
     kw["ppr_host_reserve"] = host_reserve(args, cfg)
+    for key in ("push_levels", "push_ratio", "push_hub_degree"):
+        if getattr(args, key) is not None:
+            kw[key] = getattr(args, key)
     t0i, t1i = 1 + args.warmup, 1 + args.warmup + args.steps
     timed = snaps[t0i:t1i]
     off = np.concatenate([[0], np.cumsum([len(e) for e in timed])]).astype(np.int64)
@@ -677,6 +685,9 @@ def main():
                        "l2": "working set (PPR state) larger than L2",
                        "parallelism": "replicas x%d" % world,
                        "ppr_reserve": "pinned host memory" if host_reserve(args, cfg) else "HBM",
+                       "push_schedule": {k: getattr(args, k) for k in
+                                         ("push_levels", "push_ratio", "push_hub_degree")
+                                         if getattr(args, k) is not None} or "library default",
                        "driver": ("tsvd_session_run: factor stage of snapshot k overlapped "
                                   "with the push of k+1") if args.pipelined
                        else "tsvd_session_step per snapshot"},

@@ -243,6 +243,10 @@ typedef struct tsvd_config {
   int32_t plain_frontier_cap; /* plain form: entries of its frontier list (0: 2^26);  */
                             /* cells beyond it wait in the touched bitset for the    */
                             /* next round                                            */
+  int32_t push_hub_degree;  /* > 0: the push_levels schedule holds back only         */
+                            /* vertices of at least this degree (a hub waits until   */
+                            /* its residue reaches rmax*ratio^k, while the rest push */
+                            /* at rmax); 0: it applies to every vertex               */
 } tsvd_config;
 
 /* Fills the reference's defaults (Tree_u_NC, run.sh: alpha .5, q 12, ...). */

@@ -98,12 +98,24 @@ def test_ppr_from_scratch_and_dynamic(directed):
                 _ppr_checks(s, g, src, cfg, bool(t), ors[t])
 
 
+SCHEDULES = {
+    "rmax": {},
+    # threshold schedule rmax * 8^k, k = 2, 1, 0, for every vertex
+    "levels": dict(push_levels=3, push_ratio=8.0),
+    # the same schedule for hubs only (deg >= 1024); the rest push at rmax
+    "hub-levels": dict(push_levels=3, push_ratio=8.0, push_hub_degree=1024),
+}
+
+
+@pytest.mark.parametrize("schedule", sorted(SCHEDULES))
 @pytest.mark.parametrize("directed", [False, True])
-def test_ppr_hub_vertices(directed):
+def test_ppr_hub_vertices(directed, schedule):
     """Vertices with thousands of neighbours take the hub path: their pushes
     are split into 1024-neighbour units (push_heavy_kernel). Three hubs of
     2500-3000 neighbours on top of a small R-MAT graph, sources among the
-    hubs and their neighbours; same checks against the FIFO oracle."""
+    hubs and their neighbours; same checks against the FIFO oracle, under
+    each threshold schedule (the last level of every schedule is the plain
+    rmax test, so each leaves the same invariant)."""
     cfg = small_cfg(directed, n=5000, m=20000)
     _, snaps, _ = W.build(cfg, seed=9)
     rng = np.random.default_rng(9)
@@ -119,6 +131,7 @@ def test_ppr_hub_vertices(directed):
     g = native.OracleGraph(cfg["n"], directed)
     ors = [native.OraclePPR(cfg["n"], src) for _ in range(2 if directed else 1)]
     kw = W.session_kwargs(cfg, dynamic_start=2)
+    kw.update(SCHEDULES[schedule])
     with T.Session(cfg["n"], src, **kw) as s:
         for it, e in enumerate([first, snaps[1], snaps[2]], start=1):
             s.graph_insert(e)

@@ -113,20 +113,22 @@ __global__ void __launch_bounds__(256) push_kernel(PushArgs a) {
     const int32_t *nb = a.nbr + o;
     const int32_t mine0 = lane < d ? __ldg(nb + lane) : 0;
     const bool in0 = s0 < a.nsrc, in1 = s0 + 1 < a.nsrc;
-    // push above the current level of the threshold schedule; sources between
-    // rmax and that level are parked in the pending set for a later level
-    bool act0 = in0 && x.x > a.theta_f, act1 = in1 && x.y > a.theta_f;
+    // push above the current level of the threshold schedule (for hubs only
+    // when hub_deg is set); sources between rmax and that level are parked
+    // in the pending set for a later level
+    const float th = (a.hub_deg > 0 && d < a.hub_deg) ? a.rmax_f : a.theta_f;
+    bool act0 = in0 && x.x > th, act1 = in1 && x.y > th;
     const bool any = __any_sync(kFull, act0 || act1);
     // Co-push: once the lines are pushed for some source, the other sources
     // of the chunk with a residue above co_f ride along. The 256-byte atomic
     // per neighbour is paid either way; pushing a residue below rmax is a
     // valid push step (the push identity holds) that the FIFO would do later
     // or not at all, so it only tightens the error bound.
-    if (any && a.co_f < a.theta_f) {
+    if (any && a.co_f < th) {
       act0 = in0 && x.x > a.co_f;
       act1 = in1 && x.y > a.co_f;
     }
-    if (a.theta_f > a.rmax_f && d > 0 &&
+    if (th > a.rmax_f && d > 0 &&
         __any_sync(kFull, (in0 && !act0 && x.x > a.rmax_f) || (in1 && !act1 && x.y > a.rmax_f)) &&
         lane == 0)
       mark_pair(a.pend, v, c, a.n);
@@ -240,14 +242,16 @@ __global__ void __launch_bounds__(256) collect_kernel(CollectArgs a) {
           if (g == grp) mybit = bpos;
         }
         bits = rest;
-        int32_t u = 0, c = 0;
+        int32_t u = 0, c = 0, du = 0;
         bool live = mybit >= 0;
         if (live) {
           const int64_t idx = wi * 32 + mybit;
           u = (int32_t)(idx % a.n);
           c = (int32_t)(idx / a.n);
-          live = a.deg[u] != 0;
+          du = a.deg[u];
+          live = du != 0;
         }
+        const float th = (a.hub_deg > 0 && du < a.hub_deg) ? a.rmax_f : a.theta_f;
         float m = 0.f;
         if (live) {
           const float4 *line =
@@ -260,9 +264,9 @@ __global__ void __launch_bounds__(256) collect_kernel(CollectArgs a) {
                                  fmaxf(fmaxf(x3.x, x3.y), fmaxf(x3.z, x3.w)));
           m = fmaxf(m0, m1);
         }
-        const unsigned above = __ballot_sync(kFull, live && m > a.theta_f);
-        const unsigned parked = a.theta_f > a.rmax_f
-                                    ? __ballot_sync(kFull, live && m > a.rmax_f) & ~above : 0u;
+        const unsigned above = __ballot_sync(kFull, live && m > th);
+        const unsigned parked =
+            __ballot_sync(kFull, live && th > a.rmax_f && m > a.rmax_f) & ~above;
         const unsigned gmask = 0xFu << (grp * 4);
         if (gl == 0 && live) {
           if (above & gmask) buf[atomicAdd(&nbuf, 1)] = make_int2(u, c);
@@ -501,7 +505,7 @@ tsvd_status ppr_refresh(PprState &P, const Adjacency &A, const int32_t *sources_
   CollectArgs ca;
   ca.tflag = P.tflag; ca.nwords = P.nwords; ca.n = P.n; ca.chunks = P.chunks; ca.nsrc = P.nsrc;
   ca.sp = P.sp; ca.r = P.r; ca.deg = A.deg; ca.rmax_f = largest_float_not_above(prm.rmax);
-  ca.theta_f = ca.rmax_f; ca.pend = P.pend;
+  ca.theta_f = ca.rmax_f; ca.hub_deg = 0; ca.pend = P.pend;
   ca.next = P.front[0]; ca.next_count = P.counters + 0; ca.cap = P.cap;
   ca.overflow = P.counters + 4;
   collect_kernel<<<grid_for(ceil_div(P.nwords, 64) * 256, 256, 8), 256, 0, st>>>(ca);
@@ -538,6 +542,7 @@ tsvd_status job_begin(PushJob &J, PprState &P, const Adjacency &A, const PprPara
   pa.n = P.n; pa.sp = P.sp; pa.nsrc = P.nsrc; pa.chunks = P.chunks; pa.tflag = P.tflag; pa.pend = P.pend;
   pa.alpha_f = (float)prm.alpha; pa.one_minus_alpha_f = (float)(1.0 - prm.alpha);
   pa.rmax_f = rmax_f; pa.undirected = prm.undirected; pa.vmark = vmark;
+  pa.hub_deg = prm.hub_degree;
   pa.co_f = prm.cofrac >= 1.0 ? rmax_f : (float)(prm.rmax * std::max(prm.cofrac, 0.0));
   pa.heavy_w = P.heavy_w; pa.heavy_item = P.heavy_item;
   pa.heavy_count = P.counters + 2; pa.heavy_cap = P.heavy_cap;
@@ -547,6 +552,7 @@ tsvd_status job_begin(PushJob &J, PprState &P, const Adjacency &A, const PprPara
   ca.tflag = P.tflag; ca.pend = P.pend; ca.nwords = P.nwords; ca.n = P.n; ca.chunks = P.chunks;
   ca.nsrc = P.nsrc; ca.sp = P.sp; ca.r = P.r; ca.deg = A.deg; ca.rmax_f = rmax_f;
   ca.cap = P.cap; ca.overflow = P.counters + 4;
+  ca.hub_deg = prm.hub_degree;
   J.gpush = grid_for((int64_t)1 << 30, 256, 8);
   J.gcol = grid_for(ceil_div(P.nwords, 64) * 256, 256, 8);
   J.level = std::max(1, prm.levels) - 1;

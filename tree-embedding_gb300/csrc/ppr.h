@@ -47,6 +47,7 @@ struct PprParams {
   int levels = 1;       // threshold schedule: rmax * ratio^(levels-1) ... rmax
   double ratio = 8.0;
   double cofrac = 1.0;  // co-push residues above rmax * cofrac on pushed lines
+  int32_t hub_degree = 0;  // > 0: the threshold schedule applies to deg >= hub_degree only
 };
 
 struct PushStats {
@@ -64,6 +65,7 @@ struct PushArgs {
   int32_t n, sp, nsrc, chunks;
   uint32_t *tflag, *pend;
   float alpha_f, one_minus_alpha_f, rmax_f, theta_f, co_f;
+  int32_t hub_deg;  // > 0: theta_f applies to deg >= hub_deg only (rmax_f below)
   int undirected;
   uint8_t *vmark;
   float *heavy_w;
@@ -80,6 +82,7 @@ struct PushArgs {
 struct CollectArgs {
   uint32_t *tflag, *pend;
   float theta_f;
+  int32_t hub_deg;
   int64_t nwords;
   int32_t n, chunks, nsrc, sp;
   const float *r;

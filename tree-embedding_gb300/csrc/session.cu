@@ -467,6 +467,7 @@ static PprParams ppr_params(const tsvd_session *s) {
   p.levels = std::max(1, s->cfg.push_levels);
   p.ratio = s->cfg.push_ratio > 1.0 ? s->cfg.push_ratio : 8.0;
   p.cofrac = s->cfg.push_cofrac;
+  p.hub_degree = std::max(0, s->cfg.push_hub_degree);
   return p;
 }
 

@@ -46,6 +46,7 @@ class Config(ctypes.Structure):
         ("push_cofrac", ctypes.c_double), ("lp_right_factor", ctypes.c_int32),
         ("ppr_host_reserve", ctypes.c_int32), ("form", ctypes.c_int32),
         ("block_path", ctypes.c_int32), ("plain_frontier_cap", ctypes.c_int32),
+        ("push_hub_degree", ctypes.c_int32),
     ]
 
 
@@ -279,7 +280,7 @@ def make_config(n_vertices, sources, directed=False, alpha=0.5, rmax=1e-7, n_par
                 refresh_mode=REFRESH_EXACT, seed=20231, device=0, max_push_rounds=0,
                 push_levels=1, push_ratio=8.0, push_cofrac=0.85, lp_right_factor=False,
                 ppr_host_reserve=False, form=FORM_MIXED, block_path=BLOCKS_DENSE,
-                plain_frontier_cap=0):
+                plain_frontier_cap=0, push_hub_degree=0):
     """A tsvd_config; `sources` (int32, contiguous) must outlive it."""
     c = Config()
     lib().tsvd_config_default(ctypes.byref(c))
@@ -302,6 +303,7 @@ def make_config(n_vertices, sources, directed=False, alpha=0.5, rmax=1e-7, n_par
     c.form = int(form)
     c.block_path = int(block_path)
     c.plain_frontier_cap = int(plain_frontier_cap)
+    c.push_hub_degree = int(push_hub_degree)
     return c
 
 
@@ -324,14 +326,14 @@ class Session:
                  root_scaling=ROOT_SQRT_SIGMA, refresh_mode=REFRESH_EXACT, seed=20231, device=0,
                  max_push_rounds=0, push_levels=1, push_ratio=8.0, push_cofrac=0.85,
                  lp_right_factor=False, ppr_host_reserve=False, form=FORM_MIXED,
-                 block_path=BLOCKS_DENSE, plain_frontier_cap=0):
+                 block_path=BLOCKS_DENSE, plain_frontier_cap=0, push_hub_degree=0):
         self.sources = np.ascontiguousarray(sources, dtype=np.int32)
         c = make_config(n_vertices, self.sources, directed, alpha, rmax, n_parts, hierarchy_n,
                         rank_d, oversample, passes_q, dynamic_ppr_start_iter,
                         lazy_update_start_iter, delta, transform, dirty_rule, dirty_frac,
                         root_scaling, refresh_mode, seed, device, max_push_rounds, push_levels,
                         push_ratio, push_cofrac, lp_right_factor, ppr_host_reserve, form,
-                        block_path, plain_frontier_cap)
+                        block_path, plain_frontier_cap, push_hub_degree)
         self.cfg = c
         self.n, self.S, self.d = c.n_vertices, c.n_sources, c.rank_d
         self.n_parts, self.h, self.directed = c.n_parts, c.hierarchy_n, bool(directed)
