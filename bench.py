@@ -204,7 +204,8 @@ def run_ours(args, cfg, snaps, sources, device):
     off = np.concatenate([[0], np.cumsum([len(e) for e in timed])]).astype(np.int64)
     dev = [torch.from_numpy(np.ascontiguousarray(e)).to(f"cuda:{device}") for e in snaps[:t0i]]
     dev_timed = torch.from_numpy(np.ascontiguousarray(np.concatenate(timed))).to(f"cuda:{device}")
-    res = {}
+    res = {"push_schedule": {k: kw.get(k, d) for k, d in
+                             (("push_levels", 1), ("push_ratio", 8.0), ("push_hub_degree", 0))}}
     with T.Session(cfg["n"], sources, **kw) as s:
         t = time.perf_counter()
         s.step_device(dev[0].data_ptr(), len(snaps[0]))  # set-up: first snapshot, from scratch
@@ -514,11 +515,9 @@ def push_roofline(stages):
     sec = ms / 1e3
     achieved = byts / sec / 1e9 if ms > 0 else 0.0
     achieved_min = byts_min / sec / 1e9 if ms > 0 else 0.0
-    traffic = None
-    if PUSH_TRAFFIC_BYTES_PER_ITEM_EDGE is not None and launches:
-        traffic = PUSH_TRAFFIC_BYTES_PER_ITEM_EDGE * iedges / launches
     return {"kernel": "push_kernel+push_heavy_kernel", "bound": "hbm", "achieved": achieved,
-            "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
+            "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+            "traffic_note": TRAFFIC_NOTE,
             "algorithmic_bytes_per_launch": byts / max(1, launches),
             "achieved_min": achieved_min, "frac_min": achieved_min / peak,
             "min_bytes_per_launch": byts_min / max(1, launches),
@@ -527,12 +526,13 @@ def push_roofline(stages):
             "peak_source": "MEASURED_PEAKS.json hbm_gbs (copy bandwidth), of measured"}
 
 
-# DRAM bytes (read + write) of push_kernel + push_heavy_kernel per pushed
-# item-neighbour (one 256-byte residue-run atomic), measured by ncu
-# (dram__bytes_read.sum + dram__bytes_write.sum) over the push launches of
-# one dynamic snapshot of a small directed case whose state exceeds L2,
-# scaled per launch by the item-neighbours the run reports.
-PUSH_TRAFFIC_BYTES_PER_ITEM_EDGE = 320.9
+# DRAM counters are only captured on cases of a few GB. The push's traffic
+# per item-neighbour depends on how many reductions a residue run receives
+# per round (its L2 reuse), which differs between such a case and the
+# full-size state, so a small-case figure does not scale to this launch.
+TRAFFIC_NOTE = ("not measured at this size: DRAM counters are captured on cases of a few GB "
+                "only, and the push's DRAM bytes per item-neighbour depend on the reductions "
+                "a residue run receives per round, which do not scale from such a case")
 
 
 def tail_attribution(stages):
@@ -685,9 +685,7 @@ def main():
                        "l2": "working set (PPR state) larger than L2",
                        "parallelism": "replicas x%d" % world,
                        "ppr_reserve": "pinned host memory" if host_reserve(args, cfg) else "HBM",
-                       "push_schedule": {k: getattr(args, k) for k in
-                                         ("push_levels", "push_ratio", "push_hub_degree")
-                                         if getattr(args, k) is not None} or "library default",
+                       "push_schedule": res["push_schedule"],
                        "driver": ("tsvd_session_run: factor stage of snapshot k overlapped "
                                   "with the push of k+1") if args.pipelined
                        else "tsvd_session_step per snapshot"},

@@ -115,9 +115,11 @@ class OracleTreeSVD:
                  dynamic_ppr_start_iter=100, lazy_update_start_iter=100, delta=0.3,
                  transform=TRANSFORM_LOG10_NC, dirty_rule=DIRTY_REFERENCE, dirty_frac=0.01,
                  root_scaling=0, refresh_mode=0, seed=20231, threads=1, lp_right_factor=False,
-                 block_path=0):
-        # block_path: the GPU's choice of product path for a block's frPCA; the
-        # oracle's arithmetic is the same either way, so it is accepted and unused
+                 block_path=0, push_levels=1, push_ratio=8.0, push_hub_degree=0):
+        # block_path (the GPU's product path for a block's frPCA) and the push's
+        # threshold schedule (the order in which the GPU pushes; its last level is
+        # the rmax test the FIFO applies) do not change what the oracle computes:
+        # accepted and unused
         self.n, self.directed = int(n), bool(directed)
         self.sources = np.ascontiguousarray(sources, dtype=np.int32)
         self.S = len(self.sources)

@@ -22,7 +22,11 @@ the push-order difference. Checked on every snapshot:
   the independent oracle outside near-ties (decision margin below 2 %, where
   the two pushes' matrices may legitimately fall on either side).
 * root singular values within 1e-3 relative against the oracle run on the
-  GPU's reserve (the factorization arithmetic alone), within 1e-2 against the
+  GPU's reserve (the factorization arithmetic alone), plus the error the
+  mixed form's half-precision block storage allows by Weyl's inequality:
+  each stored entry is within 2^-12 of itself, so every singular value moves
+  by at most 2^-12 ||A||_F (this term matters only in the tail of the 128
+  kept values, which sit far below the first); within 1e-2 against the
   independent oracle (the two pushes stop at different valid states; with
   the ln(x N) transform at rmax = 1e-6 that moves the root singular values
   by up to 5.3e-3, measured on a GB300); the largest principal-angle sine of
@@ -178,14 +182,18 @@ def test_c1_end_to_end_against_the_fp64_oracle():
             emb = s.embedding()
             _, sig = s.tree_factor(0)
             assert np.isfinite(emb).all()
-            dA = spectral_norm(log_transform(p, rmax, cfg["transform"], n) -
-                               log_transform(po, rmax, cfg["transform"], n))
+            A_g = log_transform(p, rmax, cfg["transform"], n)
+            dA = spectral_norm(A_g - log_transform(po, rmax, cfg["transform"], n))
+            fp16_storage = 2.0 ** -12 * float(np.linalg.norm(A_g))
+            del A_g
             for name, ref_emb, ref_sig, tol in (("iso", emb_i, iso.sigma[0], 1e-3),
                                                 ("indep", emb_o, indep.sigma[0], 1e-2)):
                 if not agreed[name]:
                     continue
-                rel = np.abs(sig - ref_sig) / ref_sig
-                assert rel.max() <= tol, (it, name, rel.max(), int(rel.argmax()))
+                err = np.abs(sig - ref_sig)
+                allowed = tol * ref_sig + (fp16_storage if name == "iso" else 0.0)
+                assert (err <= allowed).all(), (it, name, (err / ref_sig).max(),
+                                                int((err - allowed).argmax()))
                 j = gap_index(ref_sig, d)
                 assert j > 0
                 sine = max_principal_sine(emb[:, :j], ref_emb[:, :j])
