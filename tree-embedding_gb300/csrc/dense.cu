@@ -52,50 +52,56 @@ __device__ __forceinline__ void cp_async_wait() {
 // cp.async.bulk.tensor copies whose completion is counted (in bytes) on the
 // stage's "full" mbarrier; the MMA thread waits on it, issues the stage's
 // MMAs and commits them to the stage's "empty" mbarrier, which the producer
-// waits on before refilling the stage. Five stages of 32 K values are in
+// waits on before refilling the stage. Four stages of 32 K values are in
 // flight.
 //
-// Shared-memory layout: no-swizzle core matrices (8 rows x 16 bytes, 128
-// contiguous bytes; LBO = distance between core matrices adjacent along K,
-// SBO = along M/N). Each operand is described to the TMA as a 3-D view of
-// its row-major fp16 storage: {8 values (one 16-byte piece), rows, pieces
-// of a row (stride 16 bytes)}. A box of that view lands in shared memory in
-// that order, so the eight rows of a core matrix sit 16 bytes apart:
-//  * skinny operand (hi and lo halves, [k][144], MN-major in both
-//    products): box {8, 32 rows of K, 18 pieces of N}; piece (k, nb) at
-//    nb * 512 + k * 16 (LBO 128, SBO 512);
-//  * A of the forward product (A^T rows are K; MN-major): box {8, 32, 48};
-//    piece (k, mb) at mb * 512 + k * 16, so the three 128-row tiles are
-//    8 KB apart (LBO 128, SBO 512);
-//  * A of the backward product (A^T rows are M; K-major): one box
-//    {8, 128 rows, 4 pieces of K} per row tile; piece (m, kb) at
-//    kb * 2048 + m * 16 (LBO 2048, SBO 128).
-// Rows past a block's n_c and K past its end lie outside the view, and the
-// TMA fills them with zeros. Every copy starts at piece coordinate 0 of the
-// innermost dimension, on a 16-byte boundary.
-constexpr int BM = 128, MH = 3, BN = kLp, BK = 32, STAGES = 5, GEMM_THREADS = 128;
-constexpr int SA_BYTES = BM * BK * 2;  // 8 KB per row tile
-constexpr int SB_BYTES = BN * BK * 2;  // 9 KB per skinny half
+// Shared-memory layouts are the swizzled canonical ones of the tensor cores,
+// written by the TMA with the matching swizzle, so that every copy moves
+// whole 64- or 128-byte rows:
+//  * skinny operand (hi and lo halves, [k][144] in global memory, MN-major):
+//    three 64-column atoms of 32 K rows x 128 bytes, 128-byte swizzle
+//    (columns 144-191 of the third atom are outside the tensor: zeros, never
+//    read by an N = 144 MMA). Descriptor: LBO = 4 KB between atoms along N,
+//    SBO = 1 KB between 8-row groups along K;
+//  * A of the forward product (A^T [n_c][Sp]: M = Sp contiguous, MN-major):
+//    six 64-row atoms of 32 K rows x 128 bytes, 128-byte swizzle; row tile h
+//    is atoms 2h, 2h + 1 (LBO 4 KB, SBO 1 KB);
+//  * A of the backward product (A^T rows are M, K = Sp contiguous, K-major):
+//    one 128-row x 64-byte box per row tile, 64-byte swizzle (SBO = 512
+//    bytes between 8-row groups); the second 16-deep K step starts 32 bytes
+//    into the rows.
+// Rows past a block's n_c and K past its end lie outside the tensors, and the
+// TMA fills them with zeros. Every copy starts at an innermost coordinate
+// that is a multiple of 8 values (16 bytes).
+constexpr int BM = 128, MH = 3, BN = kLp, BK = 32, STAGES = 4, GEMM_THREADS = 128;
+constexpr int kAtom = 64;                              // values per 128-byte swizzle row
+constexpr int kAtomBytes = BK * 128;                   // one 32-row x 128-byte atom: 4 KB
+constexpr int kBAtoms = (BN + kAtom - 1) / kAtom;      // 3
+constexpr int SA_BYTES = BM * BK * 2;                  // 8 KB per row tile (two atoms)
+constexpr int SB_BYTES = kBAtoms * kAtomBytes;         // 12 KB per skinny half
 constexpr int STAGE_BYTES = MH * SA_BYTES + 2 * SB_BYTES;
-constexpr size_t kGemmSmem = (size_t)STAGES * STAGE_BYTES + 1024;  // + barriers, TMEM slot
-constexpr int kLboMn = 128, kSboMn = (BK / 8) * 128;  // MN-major operands
-constexpr int kLboK = BM * 16, kSboK = 128;           // K-major A (backward)
-constexpr int kTmemCols = 512;                        // MH accumulators, kAccStride apart
+constexpr size_t kGemmSmem = (size_t)STAGES * STAGE_BYTES + 2048;  // + alignment slack, barriers
+constexpr int kLayoutSw128 = 2, kLayoutSw64 = 4;       // descriptor swizzle modes
+constexpr int kTmemCols = 512;                         // MH accumulators, kAccStride apart
 constexpr int kAccStride = 160;
 static_assert(MH * kAccStride <= kTmemCols && kAccStride >= BN, "accumulators fit in TMEM");
 static_assert(BN % 16 == 0 && BN <= 256, "tcgen05.mma with M = 128 needs N % 16 == 0, N <= 256");
-static_assert(STAGE_BYTES % 1024 == 0 && SA_BYTES % 128 == 0 && SB_BYTES % 128 == 0,
-              "TMA destinations stay 128-byte aligned");
+static_assert(STAGE_BYTES % 1024 == 0 && SA_BYTES % 1024 == 0 && kAtomBytes % 1024 == 0,
+              "swizzle atoms stay 1024-byte aligned");
+static_assert(BM % kAtom == 0 && SA_BYTES == 2 * kAtomBytes, "a row tile is two atoms");
 
 // Counts waits that ran out (a kernel that gives up skips its tile and
 // frees its tensor memory; the host turns a non-zero count into an error).
 __device__ int g_umma_timeouts = 0;
 
-__device__ __forceinline__ uint64_t umma_smem_desc(uint32_t saddr, int lbo, int sbo) {
+// tcgen05 shared-memory descriptor: start, leading / stride byte offsets (16-
+// byte units), version 1, base offset 0, swizzle mode.
+__device__ __forceinline__ uint64_t umma_smem_desc(uint32_t saddr, int lbo, int sbo, int layout) {
   uint64_t d = (uint64_t)((saddr >> 4) & 0x3FFFu);
   d |= (uint64_t)((lbo >> 4) & 0x3FFF) << 16;
   d |= (uint64_t)((sbo >> 4) & 0x3FFF) << 32;
-  d |= (uint64_t)1 << 46;  // descriptor version of tcgen05; base offset 0, no swizzle
+  d |= (uint64_t)1 << 46;
+  d |= (uint64_t)(layout & 7) << 61;
   return d;
 }
 
@@ -142,12 +148,12 @@ __device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
                : "memory");
 }
 
-__device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap *map, int c0, int c1,
-                                            int c2, uint32_t bar) {
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map, int x, int y,
+                                            uint32_t bar) {
   asm volatile(
-      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
-      " [%0], [%1, {%2, %3, %4}], [%5];\n" ::"r"(dst),
-      "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(bar)
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3}], [%4];\n" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar)
       : "memory");
 }
 
@@ -167,8 +173,10 @@ struct GemmArgs {
 template <bool FWD>
 __global__ void __launch_bounds__(GEMM_THREADS, 1) umma_gemm_kernel(GemmArgs a) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
-  unsigned char *stage_base = smem_raw;
-  uint64_t *full = reinterpret_cast<uint64_t *>(smem_raw + (size_t)STAGES * STAGE_BYTES);
+  // swizzle atoms must sit on 1024-byte boundaries of the shared window
+  unsigned char *stage_base =
+      smem_raw + ((1024 - (smem_u32(smem_raw) & 1023)) & 1023);
+  uint64_t *full = reinterpret_cast<uint64_t *>(stage_base + (size_t)STAGES * STAGE_BYTES);
   uint64_t *empty = full + STAGES;
   uint32_t *tslot = reinterpret_cast<uint32_t *>(empty + STAGES);
   volatile int *failed = reinterpret_cast<volatile int *>(tslot + 1);
@@ -223,14 +231,20 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1) umma_gemm_kernel(GemmArgs a) 
       const uint32_t sa = smem_u32(stage_base + (size_t)st * STAGE_BYTES);
       const int k0 = (kt0 + i) * BK;
       mbar_expect_tx(fb, tx_bytes);
-      if (FWD) {
-        tma_load_3d(sa, map_a, 0, k0, m0 / 8, fb);
-      } else {
+      if (FWD) {  // six 64-row atoms of M at K rows k0 .. k0 + 31
 #pragma unroll
-        for (int h = 0; h < MH; ++h) tma_load_3d(sa + h * SA_BYTES, map_a, 0, m0 + h * BM, k0 / 8, fb);
+        for (int t = 0; t < MH * BM / kAtom; ++t)
+          tma_load_2d(sa + t * kAtomBytes, map_a, m0 + t * kAtom, k0, fb);
+      } else {  // per row tile: 128 rows of M, K values k0 .. k0 + 31
+#pragma unroll
+        for (int h = 0; h < MH; ++h) tma_load_2d(sa + h * SA_BYTES, map_a, k0, m0 + h * BM, fb);
       }
-      tma_load_3d(sa + MH * SA_BYTES, map_a + 1, 0, k0, 0, fb);
-      if (a.has_lo) tma_load_3d(sa + MH * SA_BYTES + SB_BYTES, map_a + 2, 0, k0, 0, fb);
+#pragma unroll
+      for (int t = 0; t < kBAtoms; ++t) {
+        tma_load_2d(sa + MH * SA_BYTES + t * kAtomBytes, map_a + 1, t * kAtom, k0, fb);
+        if (a.has_lo)
+          tma_load_2d(sa + MH * SA_BYTES + SB_BYTES + t * kAtomBytes, map_a + 2, t * kAtom, k0, fb);
+      }
       filled = i + 1;
     }
     // no copy may still be writing shared memory when the CTA exits: wait for
@@ -240,7 +254,10 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1) umma_gemm_kernel(GemmArgs a) 
   } else if (warp == 1 && lane == 0) {
     // MMA issuer
     constexpr uint32_t idesc = umma_idesc(FWD ? 1 : 0);
-    constexpr int a_lbo = FWD ? kLboMn : kLboK, a_sbo = FWD ? kSboMn : kSboK;
+    // per 16-deep K step: MN-major tiles advance two 8-row groups (2 KB),
+    // the K-major A 32 bytes along its rows
+    constexpr int a_lbo = FWD ? kAtomBytes : 16, a_sbo = FWD ? 1024 : 512;
+    constexpr int a_layout = FWD ? kLayoutSw128 : kLayoutSw64, a_kstep = FWD ? 2048 : 32;
     int issued = 0;
     for (int i = 0; i < nk; ++i) {
       const int st = i % STAGES;
@@ -253,12 +270,13 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1) umma_gemm_kernel(GemmArgs a) 
       const uint32_t sbh = sa + MH * SA_BYTES, sbl = sbh + SB_BYTES;
 #pragma unroll
       for (int ks = 0; ks < BK / 16; ++ks) {
-        const uint64_t bdh = umma_smem_desc(sbh + ks * 2 * kLboMn, kLboMn, kSboMn);
-        const uint64_t bdl = umma_smem_desc(sbl + ks * 2 * kLboMn, kLboMn, kSboMn);
+        const uint64_t bdh = umma_smem_desc(sbh + ks * 2048, kAtomBytes, 1024, kLayoutSw128);
+        const uint64_t bdl = umma_smem_desc(sbl + ks * 2048, kAtomBytes, 1024, kLayoutSw128);
         const uint32_t acc0 = (i > 0 || ks > 0) ? 1u : 0u;
 #pragma unroll
         for (int h = 0; h < MH; ++h) {
-          const uint64_t ad = umma_smem_desc(sa + h * SA_BYTES + ks * 2 * a_lbo, a_lbo, a_sbo);
+          const uint64_t ad =
+              umma_smem_desc(sa + h * SA_BYTES + ks * a_kstep, a_lbo, a_sbo, a_layout);
           const uint32_t td = tmem + (uint32_t)(h * kAccStride);
           asm volatile(
               "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
@@ -312,9 +330,14 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1) umma_gemm_kernel(GemmArgs a) 
         asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
         if (row < mrows) {
           float *o = out + (int64_t)row * BN + c0;
-          if (atomic) {
+          if (atomic) {  // split-K partial tiles: float4 reductions (rows are 576-byte aligned)
 #pragma unroll
-            for (int j = 0; j < 16; ++j) atomicAdd(o + j, __uint_as_float(v[j]) * a.scale);
+            for (int j = 0; j < 16; j += 4)
+              atomicAdd(reinterpret_cast<float4 *>(o + j),
+                        make_float4(__uint_as_float(v[j]) * a.scale,
+                                    __uint_as_float(v[j + 1]) * a.scale,
+                                    __uint_as_float(v[j + 2]) * a.scale,
+                                    __uint_as_float(v[j + 3]) * a.scale));
           } else {
 #pragma unroll
             for (int j = 0; j < 16; j += 4)
@@ -1046,26 +1069,28 @@ static EncodeTiledFn tensor_map_encoder() {
   return fn;
 }
 
-// The 3-D piece view of a row-major fp16 matrix [rows][pitch]: {8 values,
-// rows (stride 2 pitch bytes), pitch / 8 pieces (stride 16 bytes)}, with a
-// {8, box_rows, box_pieces} box.
-static tsvd_status encode_pieces(CUtensorMap *m, const __half *base, int64_t rows, int pitch,
-                                 int box_rows, int box_pieces) {
+// A row-major fp16 matrix [rows][pitch] (the first `cols` values of each row
+// in use) as a 2-D tensor for the TMA: {cols, rows}, a {box_cols, box_rows}
+// box, the given shared-memory swizzle.
+static tsvd_status encode_2d(CUtensorMap *m, const __half *base, int64_t cols, int64_t rows,
+                             int pitch, int box_cols, int box_rows, CUtensorMapSwizzle swz) {
   const EncodeTiledFn fn = tensor_map_encoder();
   if (!fn) return fail(TSVD_ERR_DEVICE, "cuTensorMapEncodeTiled is not available from the driver");
   if (!base || (reinterpret_cast<uintptr_t>(base) & 15) != 0 || pitch % 8 != 0)
     return fail(TSVD_ERR_INVALID, "tensor map: operand %p / pitch %d not 16-byte aligned",
                 (const void *)base, pitch);
-  const cuuint64_t dims[3] = {8, (cuuint64_t)std::max<int64_t>(rows, 1), (cuuint64_t)(pitch / 8)};
-  const cuuint64_t strides[2] = {(cuuint64_t)pitch * 2, 16};
-  const cuuint32_t box[3] = {8, (cuuint32_t)box_rows, (cuuint32_t)box_pieces};
-  const cuuint32_t estride[3] = {1, 1, 1};
-  const CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 3, (void *)base, dims, strides, box,
-                        estride, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+  const cuuint64_t dims[2] = {(cuuint64_t)std::max<int64_t>(cols, 1),
+                              (cuuint64_t)std::max<int64_t>(rows, 1)};
+  const cuuint64_t strides[1] = {(cuuint64_t)pitch * 2};
+  const cuuint32_t box[2] = {(cuuint32_t)box_cols, (cuuint32_t)box_rows};
+  const cuuint32_t estride[2] = {1, 1};
+  const CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, (void *)base, dims, strides, box,
+                        estride, CU_TENSOR_MAP_INTERLEAVE_NONE, swz,
                         CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS)
-    return fail(TSVD_ERR_DEVICE, "cuTensorMapEncodeTiled: error %d (rows %lld, pitch %d, box %d x %d)",
-                (int)r, (long long)rows, pitch, box_rows, box_pieces);
+    return fail(TSVD_ERR_DEVICE,
+                "cuTensorMapEncodeTiled: error %d (%lld x %lld, pitch %d, box %d x %d)", (int)r,
+                (long long)rows, (long long)cols, pitch, box_rows, box_cols);
   return TSVD_OK;
 }
 
@@ -1074,14 +1099,14 @@ tsvd_status gemm_encode_maps(int fwd, int nprob, const __half *const *at, const 
                              CUtensorMap *out) {
   for (int i = 0; i < nprob; ++i) {
     CUtensorMap *m = out + 3 * (int64_t)i;
-    if (fwd)
-      TSVD_TRY(encode_pieces(m, at[i], nc[i], lda, BK, MH * BM / 8));
-    else
-      TSVD_TRY(encode_pieces(m, at[i], nc[i], lda, BM, BK / 8));
+    if (fwd)  // M = Sp along the rows of A^T, K = its n_c rows: 64 x 32 boxes
+      TSVD_TRY(encode_2d(m, at[i], lda, nc[i], lda, kAtom, BK, CU_TENSOR_MAP_SWIZZLE_128B));
+    else      // K = Sp along the rows, M = the n_c rows: 32 x 128 boxes
+      TSVD_TRY(encode_2d(m, at[i], lda, nc[i], lda, BK, BM, CU_TENSOR_MAP_SWIZZLE_64B));
     const int64_t brows = fwd ? nc[i] : lda;
-    TSVD_TRY(encode_pieces(m + 1, hi[i], brows, BN, BK, BN / 8));
+    TSVD_TRY(encode_2d(m + 1, hi[i], BN, brows, BN, kAtom, BK, CU_TENSOR_MAP_SWIZZLE_128B));
     if (lo && lo[i])
-      TSVD_TRY(encode_pieces(m + 2, lo[i], brows, BN, BK, BN / 8));
+      TSVD_TRY(encode_2d(m + 2, lo[i], BN, brows, BN, kAtom, BK, CU_TENSOR_MAP_SWIZZLE_128B));
     else
       memset(m + 2, 0, sizeof(CUtensorMap));
   }
