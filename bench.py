@@ -730,7 +730,14 @@ def main():
                               for k in ("ms_insert", "ms_push", "ms_log", "ms_frpca",
                                         "ms_merge")},
             "deltas": "the %d deltas after the e2e leg, same session" % pl["steps"]}
-        line["p50_plain_over_mixed"] = line["plain_form"]["p50_ms"] / line["p50_ms"]
+        # the graph grows with every delta, so the plain leg (the last deltas)
+        # is compared with the mixed form's latest snapshots: the e2e leg's
+        # deltas when it ran (the ones just before), else the timed ones
+        near = line.get("e2e", {}).get("p50_ms") or line["p50_ms"]
+        line["p50_plain_over_mixed"] = line["plain_form"]["p50_ms"] / near
+        line["p50_plain_over_mixed_basis"] = (
+            "plain p50 / mixed e2e-leg p50 (adjacent deltas)" if line.get("e2e", {}).get("p50_ms")
+            else "plain p50 / mixed timed p50")
     if rank == 0 and not args.no_cpu:
         info = cpu_sample(cfg, snaps, sources, steps=1,
                           k=args.cpu_sources or (os.cpu_count() or 1))

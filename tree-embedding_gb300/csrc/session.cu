@@ -713,17 +713,17 @@ static tsvd_status tune_block_paths(tsvd_session *s, const FactorJob &job,
 
 // Mixed form with TSVD_BLOCKS_SPARSE / TSVD_BLOCKS_AUTO: one batch of dense
 // blocks on the tensor cores and one batch of sparse blocks through SpMM.
-static tsvd_status factorize_two_paths(tsvd_session *s, FactorJob &job,
-                                       std::vector<FrpcaProblem> &probs,
-                                       std::vector<double> &ssum, cudaStream_t st) {
+// Factorizes the dirty blocks with those below density `threshold` (or all,
+// for TSVD_BLOCKS_SPARSE) through SpMM and the rest on the tensor cores.
+static tsvd_status factorize_split(tsvd_session *s, FactorJob &job,
+                                   std::vector<FrpcaProblem> &probs, std::vector<double> &ssum,
+                                   double threshold, cudaStream_t st, int *nsparse) {
   const int nf = (int)job.factor_now.size();
-  if (s->cfg.block_path == TSVD_BLOCKS_AUTO && !s->tuned)
-    TSVD_TRY(tune_block_paths(s, job, probs, st));
   std::vector<int> di, si;
   for (int i = 0; i < nf; ++i) {
     const int b = job.factor_now[i];
     const double rho = (double)s->nnz_h[b] / std::max(1.0, (double)s->S * job.ncols[b]);
-    const bool sparse = s->cfg.block_path == TSVD_BLOCKS_SPARSE || rho < s->tune_density;
+    const bool sparse = s->cfg.block_path == TSVD_BLOCKS_SPARSE || rho < threshold;
     (sparse ? si : di).push_back(i);
   }
   if (!di.empty()) {
@@ -747,7 +747,48 @@ static tsvd_status factorize_two_paths(tsvd_session *s, FactorJob &job,
     TSVD_TRY(frpca_batch(s->fw, ps.data(), (int)ps.size(), s->q, s->cfg.seed, s->S, st, sv.data()));
     for (size_t k = 0; k < si.size(); ++k) ssum[si[k]] = sv[k];
   }
-  job.stats.sparse_blocks = (int)si.size();
+  *nsparse = (int)si.size();
+  return TSVD_OK;
+}
+
+// Mixed form with TSVD_BLOCKS_SPARSE / TSVD_BLOCKS_AUTO: one batch of dense
+// blocks on the tensor cores and one batch of sparse blocks through SpMM.
+// The single-block trials of the autotuner see the tensor-core path at a
+// fraction of the GPU, while the real batch fills it; so at the first
+// factorization the split they suggest is timed against the whole batch on
+// the tensor cores, and the faster of the two is kept.
+static tsvd_status factorize_two_paths(tsvd_session *s, FactorJob &job,
+                                       std::vector<FrpcaProblem> &probs,
+                                       std::vector<double> &ssum, cudaStream_t st) {
+  int nsparse = 0;
+  if (s->cfg.block_path == TSVD_BLOCKS_AUTO && !s->tuned) {
+    TSVD_TRY(tune_block_paths(s, job, probs, st));
+    if (s->tune_density > 0) {
+      cudaEvent_t e0 = s->tev[0], e1 = s->tev[1];
+      TSVD_CUDA(cudaEventRecord(e0, st));
+      TSVD_TRY(factorize_split(s, job, probs, ssum, s->tune_density, st, &nsparse));
+      TSVD_CUDA(cudaEventRecord(e1, st));
+      TSVD_CUDA(cudaEventSynchronize(e1));
+      const double t_split = ms_between(e0, e1);
+      if (nsparse > 0) {
+        TSVD_CUDA(cudaEventRecord(e0, st));
+        TSVD_TRY(factorize_split(s, job, probs, ssum, 0.0, st, &nsparse));
+        TSVD_CUDA(cudaEventRecord(e1, st));
+        TSVD_CUDA(cudaEventSynchronize(e1));
+        const double t_dense = ms_between(e0, e1);
+        if (t_dense <= t_split) {
+          s->tune_density = 0.0;  // this batch (now factorized) stays on the tensor cores
+        } else {
+          TSVD_TRY(factorize_split(s, job, probs, ssum, s->tune_density, st, &nsparse));
+        }
+      }
+      job.stats.sparse_blocks = nsparse;
+      job.stats.tune_density = s->tune_density;
+      return TSVD_OK;
+    }
+  }
+  TSVD_TRY(factorize_split(s, job, probs, ssum, s->tune_density, st, &nsparse));
+  job.stats.sparse_blocks = nsparse;
   job.stats.tune_density = s->tune_density;
   return TSVD_OK;
 }
