@@ -289,54 +289,73 @@ __global__ void __launch_bounds__(256) collect_kernel(CollectArgs a) {
 // Dynamic refresh of the new adjacency slots of vertex u, for one chunk of
 // sources: for slot j >= 1 (the reference skips j == 0, ppr:2086-2093),
 //   p_u *= (j+1)/j ; r_u -= p_u/(j+1)/alpha ; r_w += (1-alpha) p_u/(j+1)/alpha.
+// The work is walked chunk by chunk and, within a chunk, in vertex order: a
+// warp takes 32 consecutive vertices of one chunk and refreshes those that
+// gained slots, so consecutive warps read and write consecutive stretches of
+// the chunk's reserve runs. (With the reserve in host memory these accesses
+// cross NVLink-C2C, where scattered 256-byte requests run several times
+// slower than ordered ones.)
 __global__ void __launch_bounds__(256) refresh_kernel(RefreshArgs a) {
   const int lane = threadIdx.x & 31;
   const int64_t gw = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  const int64_t nitems = (int64_t)(*a.nupd) * a.chunks;
+  const int64_t groups = ((int64_t)a.n + 31) / 32;
+  const int64_t nitems = groups * a.chunks;
   for (int64_t i = gw; i < nitems; i += nw) {
-    const int32_t u = a.upd[i / a.chunks];
-    const int32_t c = (int32_t)(i % a.chunks);
-    const int32_t s0 = c * kChunk + 2 * lane;  // this lane's sources: s0, s0 + 1
-    const bool valid = s0 < a.nsrc;            // padding sources hold zeros and stay zero
-    const int32_t j0 = a.former[u], j1 = a.deg[u];
-    const int32_t *nb = a.nbr + a.off[u];
-    float2 *pu = reinterpret_cast<float2 *>(a.p + ppr_cell(u, s0, a.n));
-    float2 pf = valid ? *pu : make_float2(0.0f, 0.0f);
-    float2 rdelta = make_float2(0.0f, 0.0f);
-    bool any = false;
-    for (int32_t j = max(j0, 1); j < j1; ++j) {
-      any = true;
-      const int32_t w = __ldg(nb + j);
-      const float jp1 = (float)(j + 1);
-      if (a.intdiv) {
-        const float f = (float)((j + 1) / j);
-        pf.x = pf.x * f;
-        pf.y = pf.y * f;
-      } else {
-        const float f = jp1 / (float)j;
-        pf.x = pf.x * f;
-        pf.y = pf.y * f;
-      }
-      const float2 q = make_float2(pf.x / jp1, pf.y / jp1);  // p_u / (j+1)
-      rdelta.x -= q.x * a.inv_alpha_f;
-      rdelta.y -= q.y * a.inv_alpha_f;
-      if (valid)
-        atomicAdd(reinterpret_cast<float2 *>(a.r + ppr_cell(w, s0, a.n)),
-                  make_float2(q.x * a.oma_over_alpha_f, q.y * a.oma_over_alpha_f));
-      if (lane == 0) mark_pair(a.tflag, w, c, a.n);
+    const int32_t c = (int32_t)(i / groups);
+    const int32_t ubase = (int32_t)((i % groups) * 32);
+    const int32_t mine = ubase + lane;
+    int32_t j0m = 0, j1m = 0;
+    if (mine < a.n) {
+      j0m = __ldg(a.former + mine);
+      j1m = __ldg(a.deg + mine);
     }
-    if (any) {
-      if (valid) {
-        *pu = pf;
-        atomicAdd(reinterpret_cast<float2 *>(a.r + ppr_cell(u, s0, a.n)), rdelta);
+    unsigned todo = __ballot_sync(kFull, j1m > j0m);
+    while (todo) {
+      const int k = __ffs(todo) - 1;
+      todo &= todo - 1;
+      const int32_t u = ubase + k;
+      const int32_t j0 = __shfl_sync(kFull, j0m, k), j1 = __shfl_sync(kFull, j1m, k);
+      const int32_t s0 = c * kChunk + 2 * lane;  // this lane's sources: s0, s0 + 1
+      const bool valid = s0 < a.nsrc;            // padding sources hold zeros and stay zero
+      const int32_t *nb = a.nbr + a.off[u];
+      float2 *pu = reinterpret_cast<float2 *>(a.p + ppr_cell(u, s0, a.n));
+      float2 pf = valid ? *pu : make_float2(0.0f, 0.0f);
+      float2 rdelta = make_float2(0.0f, 0.0f);
+      bool any = false;
+      for (int32_t j = max(j0, 1); j < j1; ++j) {
+        any = true;
+        const int32_t w = __ldg(nb + j);
+        const float jp1 = (float)(j + 1);
+        if (a.intdiv) {
+          const float f = (float)((j + 1) / j);
+          pf.x = pf.x * f;
+          pf.y = pf.y * f;
+        } else {
+          const float f = jp1 / (float)j;
+          pf.x = pf.x * f;
+          pf.y = pf.y * f;
+        }
+        const float2 q = make_float2(pf.x / jp1, pf.y / jp1);  // p_u / (j+1)
+        rdelta.x -= q.x * a.inv_alpha_f;
+        rdelta.y -= q.y * a.inv_alpha_f;
+        if (valid)
+          atomicAdd(reinterpret_cast<float2 *>(a.r + ppr_cell(w, s0, a.n)),
+                    make_float2(q.x * a.oma_over_alpha_f, q.y * a.oma_over_alpha_f));
+        if (lane == 0) mark_pair(a.tflag, w, c, a.n);
       }
+      if (any) {
+        if (valid) {
+          *pu = pf;
+          atomicAdd(reinterpret_cast<float2 *>(a.r + ppr_cell(u, s0, a.n)), rdelta);
+        }
+      }
+      // A formerly dangling vertex (j0 == 0) may hold residue it could not
+      // push; in exact mode it is re-examined like any touched vertex. The
+      // reference's dense path skips slot 0 entirely (ppr:2086-2093).
+      if ((any || (!a.intdiv && j0 == 0 && j1 > 0)) && lane == 0)
+        mark_pair(a.tflag, u, c, a.n);
     }
-    // A formerly dangling vertex (j0 == 0) may hold residue it could not
-    // push; in exact mode it is re-examined like any touched vertex. The
-    // reference's dense path skips slot 0 entirely (ppr:2086-2093).
-    if ((any || (!a.intdiv && j0 == 0 && j1 > 0)) && lane == 0)
-      mark_pair(a.tflag, u, c, a.n);
   }
 }
 
@@ -353,22 +372,6 @@ __global__ void unpark_kernel(uint32_t *__restrict__ tflag, uint32_t *__restrict
   }
 }
 
-__global__ void list_updated_kernel(const int32_t *__restrict__ deg,
-                                    const int32_t *__restrict__ former, int32_t n,
-                                    int32_t *__restrict__ out, int32_t *__restrict__ count) {
-  const int lane = threadIdx.x & 31;
-  for (int64_t base = (blockIdx.x * (int64_t)blockDim.x) & ~31ll; base < n;
-       base += (int64_t)gridDim.x * blockDim.x) {
-    int64_t v = base + (threadIdx.x & ~31) + lane;
-    bool f = v < n && deg[v] > former[v];
-    unsigned m = __ballot_sync(kFull, f);
-    if (!m) continue;
-    int32_t pos = 0;
-    if (lane == 0) pos = atomicAdd(count, __popc(m));
-    pos = __shfl_sync(kFull, pos, 0);
-    if (f) out[pos + __popc(m & ((1u << lane) - 1u))] = (int32_t)v;
-  }
-}
 
 __global__ void init_sources_kernel(const int32_t *__restrict__ sources, int32_t nsrc,
                                     float *__restrict__ r, int32_t n,
@@ -488,16 +491,13 @@ tsvd_status ppr_refresh(PprState &P, const Adjacency &A, const int32_t *sources_
   }
   // vertices with new slots
   TSVD_CUDA(cudaMemsetAsync(P.counters + 5, 0, sizeof(int32_t), st));
-  list_updated_kernel<<<grid_for(A.n, 256), 256, 0, st>>>(A.deg, A.former, A.n, P.upd,
-                                                            P.counters + 5);
-  TSVD_LAUNCH_CHECK();
   RefreshArgs ra;
-  ra.upd = P.upd; ra.nupd = P.counters + 5; ra.n = P.n; ra.chunks = P.chunks; ra.nsrc = P.nsrc;
+  ra.n = P.n; ra.chunks = P.chunks; ra.nsrc = P.nsrc;
   ra.sp = P.sp; ra.off = A.off; ra.deg = A.deg; ra.former = A.former; ra.nbr = A.nbr;
   ra.r = P.r; ra.p = P.p; ra.tflag = P.tflag; ra.intdiv = prm.intdiv;
   ra.inv_alpha_f = (float)(1.0 / prm.alpha);
   ra.oma_over_alpha_f = (float)((1.0 - prm.alpha) / prm.alpha);
-  refresh_kernel<<<grid_for((int64_t)A.n * 32, 256, 16), 256, 0, st>>>(ra);
+  refresh_kernel<<<grid_for((A.n + 31) / 32 * (int64_t)P.chunks * 32, 256, 16), 256, 0, st>>>(ra);
   TSVD_LAUNCH_CHECK();
   // seed the frontier from the touched (vertex, chunk) pairs
   P.cur = 0;

@@ -95,8 +95,6 @@ struct CollectArgs {
 };
 
 struct RefreshArgs {
-  const int32_t *upd;
-  const int32_t *nupd;
   int32_t n, chunks, nsrc, sp;
   const int64_t *off;
   const int32_t *deg, *former, *nbr;
