@@ -13,7 +13,8 @@ pushed in one run and not in the other, so the two runs stop at two valid
 push states, like any two runs of the same session. The results must then
 agree within the tolerance every parity test states: root singular values
 (the squared column norms of the U sqrt(S) embedding) within 1e-3 relative
-and the largest principal-angle sine of the gap-separated leading subspace
+plus 1e-4 of the largest (the Weyl floor of the two runs' push-order
+difference) and the largest principal-angle sine of the gap-separated leading subspace
 within 1e-2 (the subspace ends where the gap is at least 5 % of the next
 singular value and 1e-3 of the largest, so rounding-level differences
 between the runs cannot rotate it). Every block is refreshed every
@@ -44,6 +45,15 @@ def _tenant(spec):
     kw = W.session_kwargs(cfg, dynamic_start=2, lazy_start=2)
     kw["dirty_rule"] = T.DIRTY_ALL
     return cfg, snaps, src, kw
+
+
+def _sigma_agree(sig, ref):
+    """Every singular value within 1e-3 of itself plus 1e-4 of the largest:
+    two runs' matrices differ by the order of the push's float reductions,
+    and by Weyl's inequality that moves every singular value by the same
+    absolute amount (measured near 4e-5 of the largest at rmax 1e-7), which
+    is a large relative change only in the tail."""
+    return bool((np.abs(sig - ref) <= 1e-3 * np.abs(ref) + 1e-4 * np.abs(ref).max()).all())
 
 
 def _run(server, tenants, interleave):
@@ -86,15 +96,14 @@ def test_each_result_is_the_same_alone_and_in_the_mix():
         sm = (mix ** 2).sum(axis=0)
         order = np.argsort(-sa)
         sa, sm = sa[order], sm[np.argsort(-sm)]
+        assert _sigma_agree(sm, sa), (key, np.abs(sm / sa - 1).max())
         j = gap_index(sa, len(sa), min_abs=1e-3)
         assert j > 0, key
-        assert np.allclose(sm[:j], sa[:j], rtol=1e-3), (key, np.abs(sm[:j] / sa[:j] - 1).max())
         ua = emb[:, order[:j]]
         um = mix[:, np.argsort(-(mix ** 2).sum(axis=0))[:j]]
         assert max_principal_sine(um, ua) <= 1e-2, key
     for t in sig_alone:
-        j = gap_index(sig_alone[t], len(sig_alone[t]), min_abs=1e-3)
-        assert np.allclose(sig_mix[t][:j], sig_alone[t][:j], rtol=1e-3), t
+        assert _sigma_agree(sig_mix[t], sig_alone[t]), t
 
 
 def test_admission_by_hbm_footprint():
