@@ -16,9 +16,10 @@ agree within the tolerance every parity test states: root singular values
 plus 1e-4 of the largest (the Weyl floor of the two runs' push-order
 difference) and the largest principal-angle sine of the gap-separated leading subspace
 within 1e-2 (the subspace ends where the gap is at least 5 % of the next
-singular value and 1e-3 of the largest, so rounding-level differences
-between the runs cannot rotate it). Every block is refreshed every
-snapshot, so no lazy decision can part the two runs.
+singular value and 1e-2 of the largest: a difference of 1e-4 of the largest,
+the floor of the singular-value check, can then turn it by at most 1e-2 by
+the sin-theta theorem). Every block is refreshed every snapshot, so no lazy
+decision can part the two runs.
 """
 import numpy as np
 import pytest
@@ -40,7 +41,9 @@ TENANTS = [
 def _tenant(spec):
     cfg = W.scaled(spec["base"], n=spec["n"], m=spec["m"], sources=spec["sources"],
                    n_parts=spec["n_parts"], rank_d=spec["rank_d"], snapshots=4)
-    cfg["rmax"] = 1e-7  # the serving workload's configured rmax
+    # the runs' push-order difference scales with rmax: at 1e-8 it stays far
+    # below the tolerance, so any dependence on the mix would show
+    cfg["rmax"] = 1e-8
     _, snaps, src = W.build(cfg, seed=spec["seed"])
     kw = W.session_kwargs(cfg, dynamic_start=2, lazy_start=2)
     kw["dirty_rule"] = T.DIRTY_ALL
@@ -97,7 +100,7 @@ def test_each_result_is_the_same_alone_and_in_the_mix():
         order = np.argsort(-sa)
         sa, sm = sa[order], sm[np.argsort(-sm)]
         assert _sigma_agree(sm, sa), (key, np.abs(sm / sa - 1).max())
-        j = gap_index(sa, len(sa), min_abs=1e-3)
+        j = gap_index(sa, len(sa), min_abs=1e-2)
         assert j > 0, key
         ua = emb[:, order[:j]]
         um = mix[:, np.argsort(-(mix ** 2).sum(axis=0))[:j]]
