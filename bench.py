@@ -85,6 +85,8 @@ def parse():
     ap.add_argument("--push-ratio", type=float, default=None)
     ap.add_argument("--push-hub-degree", type=int, default=None,
                     help="apply the threshold schedule to vertices of at least this degree only")
+    ap.add_argument("--push-cofrac", type=float, default=None,
+                    help="co-push residues above this fraction of rmax on runs being pushed")
     ap.add_argument("--serve", action="store_true",
                     help="serving measurement instead of the headline: tenants of different sizes "
                          "on one GPU, Poisson-arriving edge batches, p50/p99 request latency")
@@ -196,7 +198,7 @@ def run_ours(args, cfg, snaps, sources, device):
     kw["device"] = device
     kw["seed"] = args.seed
     kw["ppr_host_reserve"] = host_reserve(args, cfg)
-    for key in ("push_levels", "push_ratio", "push_hub_degree"):
+    for key in ("push_levels", "push_ratio", "push_hub_degree", "push_cofrac"):
         if getattr(args, key) is not None:
             kw[key] = getattr(args, key)
     t0i, t1i = 1 + args.warmup, 1 + args.warmup + args.steps
@@ -205,7 +207,8 @@ def run_ours(args, cfg, snaps, sources, device):
     dev = [torch.from_numpy(np.ascontiguousarray(e)).to(f"cuda:{device}") for e in snaps[:t0i]]
     dev_timed = torch.from_numpy(np.ascontiguousarray(np.concatenate(timed))).to(f"cuda:{device}")
     res = {"push_schedule": {k: kw.get(k, d) for k, d in
-                             (("push_levels", 1), ("push_ratio", 8.0), ("push_hub_degree", 0))}}
+                             (("push_levels", 1), ("push_ratio", 8.0), ("push_hub_degree", 0),
+                              ("push_cofrac", 0.85))}}
     with T.Session(cfg["n"], sources, **kw) as s:
         t = time.perf_counter()
         s.step_device(dev[0].data_ptr(), len(snaps[0]))  # set-up: first snapshot, from scratch
