@@ -40,14 +40,15 @@ CONFIGS = {
     # The same graph refreshed by 1%-insertion snapshots (1.78M edges each)
     # after a 70 % first snapshot: 30 deltas.
     # The push holds hubs (degree >= 1024) back until their residue reaches
-    # 8 rmax, then finishes at rmax (measured on this graph: push -5 %,
-    # snapshot p50 -4.4 %; the same two levels for every vertex: +5.6 %).
+    # 16 rmax, then 4 rmax, then finishes at rmax (measured on this graph:
+    # snapshot p50 -3 % against two levels of ratio 8, which took -4.4 %
+    # against none; the same levels for every vertex: +5.6 %).
     "rmat-d-6.2m-1pct": dict(n=6_216_199, m=177_862_656, directed=True, snapshots=31,
                              first=0.7, sources=3000, alpha=0.2, rmax=1e-7,
                              transform=TRANSFORM_LOG10_NC, n_parts=128, hierarchy_n=2,
                              rank_d=128, passes_q=6, dirty_rule=DIRTY_FROBENIUS,
                              dirty_frac=0.01, delta=0.3, host_reserve=True,
-                             push_levels=2, push_ratio=8.0, push_hub_degree=1024),
+                             push_levels=3, push_ratio=4.0, push_hub_degree=1024),
     # Batched form: two undirected graphs (YouTube- and Flickr-sized), monthly
     # splits (24 snapshots, the first with 40 % of the edges), 256 column
     # blocks made deliberately uneven by numbering the vertices in descending
